@@ -1,0 +1,102 @@
+"""ctypes binding of ``libdgfem_gb300.so`` (C ABI in ``include/dgfem_gb300.h``).
+
+The library is the only compute path: if it is missing or fails to load,
+:func:`lib` raises; nothing falls back to a CPU evaluation.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "libdgfem_gb300.so"
+_lib = None
+
+DG_OK = 0
+DG_ERR_ARGUMENT = 1
+DG_ERR_UNSUPPORTED = 2
+DG_ERR_CUDA = 3
+DG_ERR_TIMEOUT = 4
+DG_ERR_INDEX = 5
+
+DG_WAVE = 0
+DG_EULER = 1
+DG_MAXWELL = 2
+
+#: every entry point declared in include/dgfem_gb300.h
+EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_finish", "dg_plan_destroy",
+                    "dg_plan_info", "dg_fp64_fma_probe", "dg_last_error",
+                    "dg_abi_version")
+
+
+class DGError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[dg status {code}] {msg}")
+        self.code = code
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [
+        ("order", ctypes.c_int32),
+        ("nelements", ctypes.c_int64),
+        ("metric", ctypes.c_void_p),
+        ("face_geom", ctypes.c_void_p),
+        ("gather", ctypes.c_void_p),
+        ("weak_diff", ctypes.c_void_p),
+        ("strong_diff", ctypes.c_void_p),
+        ("lift", ctypes.c_void_p),
+        ("face_nodes", ctypes.c_void_p),
+    ]
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    """Load the CUDA library (building it first when the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from actx_dgfem_suite_gb300.csrc import build as _build
+    if _build.is_stale():
+        try:
+            _build.build()
+        except Exception as exc:  # no nvcc: fall through to the load error
+            if not _LIB_PATH.exists():
+                raise RuntimeError(
+                    f"{_LIB_PATH.name} is missing and could not be built: {exc}"
+                ) from exc
+    if not _LIB_PATH.exists():
+        raise RuntimeError(f"{_LIB_PATH} is missing; run __graft_entry__.build()")
+    L = ctypes.CDLL(str(_LIB_PATH))
+    vp = ctypes.c_void_p
+    L.dg_plan_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int32,
+                                 ctypes.POINTER(MeshDesc),
+                                 ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
+    L.dg_plan_create.restype = ctypes.c_int
+    L.dg_rhs.argtypes = [vp, vp, vp, vp]
+    L.dg_rhs.restype = ctypes.c_int
+    L.dg_finish.argtypes = [vp, vp]
+    L.dg_finish.restype = ctypes.c_int
+    L.dg_plan_destroy.argtypes = [vp]
+    L.dg_plan_destroy.restype = ctypes.c_int
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    L.dg_plan_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), i32p, i32p,
+                               i32p, i32p, i32p]
+    L.dg_plan_info.restype = ctypes.c_int
+    L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
+                                    ctypes.c_int32, vp]
+    L.dg_fp64_fma_probe.restype = ctypes.c_int
+    L.dg_last_error.argtypes = []
+    L.dg_last_error.restype = ctypes.c_char_p
+    L.dg_abi_version.argtypes = []
+    L.dg_abi_version.restype = ctypes.c_int32
+    _lib = L
+    return L
+
+
+def check(code: int) -> None:
+    if code != DG_OK:
+        msg = lib().dg_last_error().decode(errors="replace")
+        raise DGError(code, msg)

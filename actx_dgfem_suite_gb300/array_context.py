@@ -1,0 +1,197 @@
+"""``GB300DGArrayContext``: the drop-in array context for the suite's RHS
+operators on one GB300 GPU.
+
+It plays the role the reference's array contexts play behind
+``_NAME_TO_ACTX_CLASS`` (``actx_dgfem_suite/run/__main__.py:209-216``):
+``actx.compile(rhs)`` returns a callable, ``compiled(*args)`` evaluates the RHS
+and returns the same container type, ``actx.to_numpy`` brings results to the
+host (``actx_dgfem_suite/run/__main__.py:73-96``).  Unlike the tracing
+contexts, ``compile`` does not trace grudge code: it recognises the operator
+objects built by :mod:`actx_dgfem_suite_gb300.rhs_builder` and binds them to a
+:class:`~actx_dgfem_suite_gb300.plan.DevicePlan`, i.e. to the hand-written
+sm_103a kernels.  There is no CPU path: constructing the context without a CUDA
+device, or without the compiled library, raises.
+"""
+
+from __future__ import annotations
+
+from typing import Any
+
+import numpy as np
+import torch
+
+from actx_dgfem_suite_gb300 import _lib
+from actx_dgfem_suite_gb300.containers import (
+    DOFArray,
+    from_stacked,
+    leaves,
+    map_leaves,
+)
+from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+
+
+class _ActxNumpy:
+    """``actx.np``: elementwise functions over DOFArrays and containers."""
+
+    def __init__(self, actx):
+        self._actx = actx
+
+    def _unary(self, f, x):
+        if isinstance(x, DOFArray):
+            return x.map(f)
+        if isinstance(x, torch.Tensor):
+            return f(x)
+        return map_leaves(x, lambda d: d.map(f))
+
+    def exp(self, x):
+        return self._unary(torch.exp, x)
+
+    def sqrt(self, x):
+        return self._unary(torch.sqrt, x)
+
+    def sin(self, x):
+        return self._unary(torch.sin, x)
+
+    def cos(self, x):
+        return self._unary(torch.cos, x)
+
+    def abs(self, x):
+        return self._unary(torch.abs, x)
+
+    def real(self, x):
+        return self._unary(lambda a: a.real if a.is_complex() else a, x)
+
+    def maximum(self, a, b):
+        return a._map2(b, lambda u, v: torch.maximum(u, v if torch.is_tensor(v)
+                                                      else torch.as_tensor(v, dtype=u.dtype, device=u.device)))
+
+    def minimum(self, a, b):
+        return a._map2(b, lambda u, v: torch.minimum(u, v if torch.is_tensor(v)
+                                                      else torch.as_tensor(v, dtype=u.dtype, device=u.device)))
+
+
+class CompiledRHS:
+    """``actx.compile(rhs)``: evaluates the RHS through one DevicePlan."""
+
+    def __init__(self, actx: GB300DGArrayContext, op):
+        self.actx = actx
+        self.op = op
+        self.plan: DevicePlan = op.plan_for(actx)
+
+    def stage(self, state) -> torch.Tensor:
+        """The (nfields, Nel, Np) device tensor holding ``state``; no copy
+        when the state is already a view of such a tensor."""
+        lv = leaves(state)
+        st = lv[0]._stack
+        if (st is not None and st[0].shape[0] == len(lv)
+                and all(d._stack is not None and d._stack[0] is st[0]
+                        and d._stack[1] == k for k, d in enumerate(lv))):
+            base = st[0]
+            if base.device == self.actx.device and base.is_contiguous():
+                return base
+            return base.to(self.actx.device, non_blocking=True)
+        arrs = [torch.as_tensor(d[0]) for d in lv]
+        if all(a.device == self.actx.device for a in arrs):
+            return torch.stack(arrs)
+        host = torch.stack([a.cpu() for a in arrs])
+        return host.to(self.actx.device, non_blocking=True)
+
+    def __call__(self, *args, out: torch.Tensor | None = None):
+        state = args[self.op.state_argnum]
+        q = self.stage(state)
+        res = self.plan.rhs(q, out)
+        return from_stacked(self.actx, state, res)
+
+
+class GB300DGArrayContext:
+    """Array context running the suite's RHS operators on one GB300."""
+
+    def __init__(self, device: str | int | torch.device | None = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("GB300DGArrayContext needs a CUDA device; "
+                               "there is no CPU fallback")
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        _lib.lib()  # load the kernels now, so a missing library fails here
+        self.np = _ActxNumpy(self)
+        self._meshes: dict[int, DeviceMesh] = {}
+
+    # {{{ device data
+
+    def device_mesh(self, disc) -> DeviceMesh:
+        key = id(disc)
+        if key not in self._meshes:
+            self._meshes[key] = DeviceMesh(disc, self.device)
+        return self._meshes[key]
+
+    def from_numpy(self, x):
+        if isinstance(x, np.ndarray) and x.dtype != object:
+            return torch.from_numpy(np.ascontiguousarray(x)).to(self.device)
+        if isinstance(x, DOFArray):
+            return DOFArray(self, [self.from_numpy(a) for a in x])
+        return map_leaves(x, lambda d: DOFArray(self, [self.from_numpy(np.asarray(a)) for a in d]))
+
+    def to_numpy(self, x):
+        if isinstance(x, torch.Tensor):
+            return x.detach().cpu().numpy()
+        if isinstance(x, DOFArray):
+            if x._stack is not None:
+                host = x._stack[0].detach().cpu().numpy()
+                return DOFArray(None, [host[x._stack[1]]])
+            return DOFArray(None, [self.to_numpy(a) for a in x])
+        lv = leaves(x)
+        st = lv[0]._stack
+        if st is not None and all(d._stack is not None and d._stack[0] is st[0]
+                                  for d in lv):
+            host = st[0].detach().cpu().numpy()   # one device->host copy
+            return map_leaves(x, lambda d: DOFArray(None, [host[d._stack[1]]]))
+        return map_leaves(x, lambda d: self.to_numpy(d))
+
+    def zeros(self, shape, dtype=torch.float64):
+        return torch.zeros(shape, dtype=dtype, device=self.device)
+
+    # }}}
+
+    # {{{ freeze / thaw: device tensors carry no queue, only the context tag
+
+    def freeze(self, x):
+        if isinstance(x, DOFArray):
+            return DOFArray(None, list(x), stack=x._stack)
+        return map_leaves(x, lambda d: DOFArray(None, list(d), stack=d._stack))
+
+    def thaw(self, x):
+        if isinstance(x, DOFArray):
+            return DOFArray(self, list(x), stack=x._stack)
+        return map_leaves(x, lambda d: DOFArray(self, list(d), stack=d._stack))
+
+    def freeze_thaw(self, x):
+        return self.thaw(self.freeze(x))
+
+    # }}}
+
+    def compile(self, f) -> CompiledRHS:
+        op = getattr(f, "dg_operator", None)
+        if op is None:
+            raise NotImplementedError(
+                "GB300DGArrayContext compiles the RHS operators built by "
+                "actx_dgfem_suite_gb300.rhs_builder.get_rhs; got "
+                f"{type(f).__name__}")
+        return CompiledRHS(self, op)
+
+    def finish(self) -> None:
+        torch.cuda.synchronize(self.device)
+
+    def clone(self) -> GB300DGArrayContext:
+        return type(self)(self.device)
+
+    def __repr__(self) -> str:
+        return f"GB300DGArrayContext(device={self.device})"
+
+
+def stacked_state(actx: GB300DGArrayContext, template: Any,
+                  fields: np.ndarray):
+    """Upload host fields (nfields, Nel, Np) as one device tensor and return
+    a container of views shaped like ``template``."""
+    dev = torch.from_numpy(np.ascontiguousarray(fields, dtype=np.float64)).to(actx.device)
+    return from_stacked(actx, template, dev)

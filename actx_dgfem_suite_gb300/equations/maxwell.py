@@ -1,0 +1,93 @@
+"""Maxwell's equations, mirroring ``actx_dgfem_suite/equations/maxwell.py``.
+
+Operator: grudge's ``MaxwellOperator`` in 3D with constant epsilon, mu, the
+alpha-weighted upwind flux (alpha = ``flux_type``) and PEC on all boundaries
+(``maxwell.py:55-70``).  The state is (E_x, E_y, E_z, H_x, H_y, H_z).
+
+Problem definitions:
+
+* ``"reference"`` (``maxwell.py:43-74``): box [0, 1]^3, epsilon = mu = 1,
+  alpha = 0.5, state = real part of the rectangular-cavity mode (1, 2, 2) at
+  t = 0, called with t = 0.5.
+* ``"baseline"``: box [0, 1]^3, epsilon = mu = 1, alpha = 1 (upwind), state =
+  a seeded mix of eight plane waves with random directions, polarisations and
+  phases.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from actx_dgfem_suite_gb300.discretization import make_box_discretization
+from actx_dgfem_suite_gb300.equations.common import Problem, make_rhs_and_args
+from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
+
+
+def rectangular_cavity_mode(nodes: np.ndarray, t: float = 0.0,
+                            mode=(1, 2, 2)) -> np.ndarray:
+    """Complex (6, ...) TM cavity mode of the unit cube (grudge's
+    ``get_rectangular_cavity_mode`` in 3D, E_0 = 1)."""
+    kx, ky, kz = (m * np.pi for m in mode)
+    omega = np.sqrt(kx**2 + ky**2 + kz**2)
+    x, y, z = nodes
+    sx, cx = np.sin(kx * x), np.cos(kx * x)
+    sy, cy = np.sin(ky * y), np.cos(ky * y)
+    sz, cz = np.sin(kz * z), np.cos(kz * z)
+    tdep = np.exp(-1j * omega * t)
+    g2 = kx**2 + ky**2
+    return np.stack([
+        -kx * kz * cx * sy * sz * tdep / g2,
+        -ky * kz * sx * cy * sz * tdep / g2,
+        sx * sy * cz * tdep,
+        -1j * omega * ky * sx * cy * cz * tdep / g2,
+        1j * omega * kx * cx * sy * cz / g2 + 0 * x,
+        0 * x + 0j,
+    ])
+
+
+def plane_wave_mix(nodes: np.ndarray, seed: int = 0, nwaves: int = 8) -> np.ndarray:
+    """Sum of vacuum plane waves E = a e cos(k.x + phi), H = a (k^ x e)
+    cos(k.x + phi), |k| in 2 pi [1, 3], from a fixed seed."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((6,) + nodes.shape[1:])
+    for _ in range(nwaves):
+        khat = rng.normal(size=3)
+        khat /= np.linalg.norm(khat)
+        e = np.cross(khat, rng.normal(size=3))
+        e /= np.linalg.norm(e)
+        h = np.cross(khat, e)
+        kmag = 2 * np.pi * rng.uniform(1.0, 3.0)
+        amp = rng.uniform(0.5, 1.0)
+        phase = rng.uniform(0.0, 2 * np.pi)
+        arg = kmag * np.tensordot(khat, nodes, axes=(0, 0)) + phase
+        c = amp * np.cos(arg)
+        for i in range(3):
+            out[i] += e[i] * c
+            out[3 + i] += h[i] * c
+    return out
+
+
+def maxwell_problem(order: int, nel_1d: int, definition: str = "reference",
+                    epsilon: float = 1.0, mu: float = 1.0) -> Problem:
+    disc = make_box_discretization(order, nel_1d, 0.0, 1.0)
+    nodes = disc.nodes()
+    if definition == "reference":
+        fields = np.real(rectangular_cavity_mode(nodes, 0.0)).copy()
+        alpha = 0.5
+    elif definition == "baseline":
+        fields = plane_wave_mix(nodes)
+        alpha = 1.0
+    else:
+        raise ValueError(f"unknown problem definition {definition!r}")
+    return Problem("maxwell", disc, fields, (alpha, float(epsilon), float(mu)),
+                   0.5, definition)
+
+
+def get_maxwell_rhs(*, actx, dim: int, order: int, ndofs: int,
+                    definition: str = "reference", nel_1d: int | None = None):
+    """``(rhs, (t, w))`` as ``maxwell.py:43-74``."""
+    if dim != 3:
+        raise NotImplementedError("only 3D tetrahedral meshes are implemented")
+    if nel_1d is None:
+        nel_1d = get_nel_1d_for_regular_rect_mesh(dim, order, int(ndofs))
+    return make_rhs_and_args(maxwell_problem(order, nel_1d, definition), actx)

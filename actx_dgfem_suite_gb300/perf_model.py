@@ -1,0 +1,130 @@
+"""Analytic FLOP and byte model of one RHS evaluation.
+
+The reference counts FP64 operations on its transformed pytato DAG
+(``actx_dgfem_suite/perf_analysis.py:535-576``): every einsum along the
+``opt_einsum`` "optimal" contraction path at one multiply plus one add per
+iteration point of a reducing contraction and one multiply per point of an
+outer product (``perf_analysis.py:380-417``), and one operation per output
+element for each pointwise +, -, *, /, where, max, min and sqrt
+(``perf_analysis.py:265-377``).  That DAG cannot be built here, so this module
+applies the same rules to the einsums the mass-inverse fusion produces
+(``actx_dgfem_suite/arraycontext/mass_inverse_fuser.py:20-76``), which are
+exact, plus per-node / per-face-point pointwise counts of the restated flux
+and volume-flux expressions, which are estimates.  Agreement with the
+reference's own count is therefore unpinned.
+
+Bytes are the algorithmic minimum a fused implementation moves per RHS:
+state in and RHS out (FP64), the per-element metric (9 doubles), per-face
+normal + sJ/J (16 doubles) and one 4-byte gather index per face node.  The
+reference's ``get_footprint_bytes`` (``perf_analysis.py:581-619``) sums kernel
+arguments of its own kernel split instead.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+NFIELDS = {"wave": 4, "euler": 5, "maxwell": 6}
+
+
+def np_of(order: int) -> int:
+    return (order + 1) * (order + 2) * (order + 3) // 6
+
+
+def nfp_of(order: int) -> int:
+    return (order + 1) * (order + 2) // 2
+
+
+# {{{ einsum counts per element (suite rules; exact)
+
+
+def grad_flops(order: int) -> int:
+    """``re,rji,ej->ei``: 3 Np + 6 Np^2."""
+    n = np_of(order)
+    return 3 * n + 6 * n * n
+
+
+def div_flops(order: int) -> int:
+    """``xre,rji,xej->ei``: 18 Np + 6 Np^2."""
+    n = np_of(order)
+    return 18 * n + 6 * n * n
+
+
+def lift_flops(order: int) -> int:
+    """``jfi,fe,fej->ei``: 4 Nfp + 8 Nfp Np."""
+    return 4 * nfp_of(order) + 8 * nfp_of(order) * np_of(order)
+
+
+# }}}
+
+#: pointwise operations per face point and per volume node (estimates from
+#: the restated expressions; see module docstring)
+_POINTWISE = {
+    "wave": (38, 8),
+    "euler": (251, 48),
+    "maxwell": (72, 30),
+}
+
+
+def einsum_flops_per_element(equation: str, order: int) -> int:
+    if equation == "wave":      # 1 div (u) + 3 grad (v) + 4 LIFT
+        return div_flops(order) + 3 * grad_flops(order) + 4 * lift_flops(order)
+    if equation == "euler":     # 5 div + 5 LIFT
+        return 5 * div_flops(order) + 5 * lift_flops(order)
+    if equation == "maxwell":   # 12 curl derivatives + 6 LIFT
+        return 12 * grad_flops(order) + 6 * lift_flops(order)
+    raise ValueError(equation)
+
+
+def flops_per_element(equation: str, order: int) -> int:
+    face, vol = _POINTWISE[equation]
+    return (einsum_flops_per_element(equation, order)
+            + face * 4 * nfp_of(order) + vol * np_of(order))
+
+
+def bytes_per_element(equation: str, order: int) -> int:
+    return (16 * NFIELDS[equation] * np_of(order) + 9 * 8 + 16 * 8
+            + 4 * 4 * nfp_of(order))
+
+
+def fp64_fma_per_element(equation: str, order: int) -> int:
+    """FP64 fused multiply-adds the CUDA kernel issues per element in its
+    contractions (the reference derivatives of a field are shared by its
+    gradient components; see ``csrc/dg_rhs_fp64.cuh``)."""
+    n, nf = np_of(order), 4 * nfp_of(order)
+    lift = NFIELDS[equation] * n * nf
+    if equation == "wave":
+        return 6 * n * n + lift          # 3 D_r u + sum_r D_r (G v)_r
+    if equation == "euler":
+        return 15 * n * n + lift         # 5 fields x sum_r D_r (G F)_r
+    if equation == "maxwell":
+        return 18 * n * n + lift         # 6 fields x 3 D_r
+    raise ValueError(equation)
+
+
+@dataclass(frozen=True)
+class RhsCost:
+    equation: str
+    order: int
+    nelements: int
+
+    @property
+    def dofs(self) -> int:
+        """DOF updates per RHS: nfields * Nel * Np."""
+        return NFIELDS[self.equation] * self.nelements * np_of(self.order)
+
+    @property
+    def flops(self) -> int:
+        return self.nelements * flops_per_element(self.equation, self.order)
+
+    @property
+    def bytes(self) -> int:
+        return self.nelements * bytes_per_element(self.equation, self.order)
+
+    @property
+    def fma(self) -> int:
+        return self.nelements * fp64_fma_per_element(self.equation, self.order)
+
+    def roofline_seconds(self, peak_flops: float, peak_bytes: float) -> float:
+        """``max(F / peak_F, B / peak_BW)`` (``perf_analysis.py:643-651``)."""
+        return max(self.flops / peak_flops, self.bytes / peak_bytes)

@@ -1,0 +1,140 @@
+"""Device-resident mesh data and RHS plans over the C ABI.
+
+A :class:`DeviceMesh` holds one discretisation's geometry and gather index in
+HBM (shared by every equation on that mesh); a :class:`DevicePlan` is one
+``dg_plan`` for (equation, mesh, parameters).  Tensors are PyTorch CUDA
+tensors used as plain device buffers; only raw pointers cross the C ABI.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from actx_dgfem_suite_gb300 import _lib
+from actx_dgfem_suite_gb300.discretization import DGDiscretization
+
+EQUATIONS = {"wave": _lib.DG_WAVE, "euler": _lib.DG_EULER,
+             "maxwell": _lib.DG_MAXWELL}
+NFIELDS = {"wave": 4, "euler": 5, "maxwell": 6}
+
+
+def _stream_handle(stream) -> ctypes.c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class DeviceMesh:
+    """Geometry, gather index and reference operators of one discretisation,
+    uploaded once."""
+
+    def __init__(self, disc: DGDiscretization, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("DeviceMesh needs a CUDA device")
+        self.disc = disc
+        self.device = torch.device(device or "cuda")
+        self.metric = torch.from_numpy(disc.metric_flat()).to(self.device)
+        self.face_geom = torch.from_numpy(
+            np.ascontiguousarray(disc.face_geometry())).to(self.device)
+        self.gather = torch.from_numpy(
+            disc.gather_index().view(np.int32)).to(self.device)
+        ref = disc.ref
+        self._weak = np.ascontiguousarray(ref.weak_diff, dtype=np.float64)
+        self._strong = np.ascontiguousarray(ref.diff, dtype=np.float64)
+        self._lift = np.ascontiguousarray(ref.lift, dtype=np.float64)
+        self._fnodes = np.ascontiguousarray(ref.face_nodes, dtype=np.int32)
+
+    @property
+    def nelements(self) -> int:
+        return self.disc.nelements
+
+    @property
+    def np_(self) -> int:
+        return self.disc.np_
+
+    def desc(self) -> _lib.MeshDesc:
+        d = _lib.MeshDesc()
+        d.order = self.disc.order
+        d.nelements = self.nelements
+        d.metric = self.metric.data_ptr()
+        d.face_geom = self.face_geom.data_ptr()
+        d.gather = self.gather.data_ptr()
+        d.weak_diff = self._weak.ctypes.data
+        d.strong_diff = self._strong.ctypes.data
+        d.lift = self._lift.ctypes.data
+        d.face_nodes = self._fnodes.ctypes.data
+        return d
+
+    def nbytes(self) -> int:
+        return sum(t.numel() * t.element_size()
+                   for t in (self.metric, self.face_geom, self.gather))
+
+
+class DevicePlan:
+    """One compiled RHS: ``rhs(q, out)`` with q, out of shape (nfields, Nel, Np)."""
+
+    def __init__(self, mesh: DeviceMesh, equation: str, params):
+        if equation not in EQUATIONS:
+            raise ValueError(f"unknown equation {equation!r}")
+        self.mesh = mesh
+        self.equation = equation
+        self.nfields = NFIELDS[equation]
+        self.params = tuple(float(p) for p in params)
+        L = _lib.lib()
+        handle = ctypes.c_void_p()
+        parr = (ctypes.c_double * max(1, len(self.params)))(*self.params)
+        with torch.cuda.device(mesh.device):
+            _lib.check(L.dg_plan_create(ctypes.byref(handle), EQUATIONS[equation],
+                                        ctypes.byref(mesh.desc()), parr,
+                                        len(self.params)))
+        self._handle = handle
+        self._lib = L
+
+    @property
+    def shape(self) -> tuple[int, int, int]:
+        return (self.nfields, self.mesh.nelements, self.mesh.np_)
+
+    def info(self) -> dict:
+        nel = ctypes.c_int64()
+        vals = [ctypes.c_int32() for _ in range(5)]
+        _lib.check(self._lib.dg_plan_info(self._handle, ctypes.byref(nel),
+                                          *[ctypes.byref(v) for v in vals]))
+        order, nf, grid, block, smem = (v.value for v in vals)
+        return dict(nelements=nel.value, order=order, nfields=nf, grid=grid,
+                    block=block, smem_bytes=smem)
+
+    def _check_tensor(self, x: torch.Tensor, name: str):
+        if x.dtype != torch.float64 or x.device != self.mesh.device:
+            raise TypeError(f"{name} must be float64 on {self.mesh.device}")
+        if tuple(x.shape) != self.shape or not x.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous {self.shape} tensor, "
+                             f"got {tuple(x.shape)}")
+
+    def rhs(self, q: torch.Tensor, out: torch.Tensor | None = None,
+            stream=None) -> torch.Tensor:
+        self._check_tensor(q, "state")
+        if out is None:
+            out = torch.empty_like(q)
+        else:
+            self._check_tensor(out, "out")
+        _lib.check(self._lib.dg_rhs(self._handle, ctypes.c_void_p(q.data_ptr()),
+                                    ctypes.c_void_p(out.data_ptr()),
+                                    _stream_handle(stream)))
+        return out
+
+    def finish(self, stream=None) -> None:
+        _lib.check(self._lib.dg_finish(self._handle, _stream_handle(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_handle", None) is not None and self._handle.value:
+            self._lib.dg_plan_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

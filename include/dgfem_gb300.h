@@ -1,0 +1,108 @@
+/*
+ * dgfem_gb300.h -- C ABI of the GB300 (sm_103a) DG-FEM right-hand-side evaluator.
+ *
+ * The suite evaluates an RHS as `compiled = actx.compile(rhs); out = compiled(*args)`
+ * (actx_dgfem_suite/run/__main__.py:73-76).  This library is what sits behind
+ * such a compiled callable: a plan built once per (equation, mesh, order) and
+ * one call per RHS evaluation.  All device arrays are borrowed; the caller keeps
+ * them alive for the plan's lifetime.  No function here allocates per RHS call.
+ *
+ * Data layouts (FP64, C order; Nel elements, Np = (N+1)(N+2)(N+3)/6 volume nodes,
+ * Nfp = (N+1)(N+2)/2 nodes per face, 4 faces):
+ *   state / rhs : (nfields, Nel, Np)   field-major, one meshmode DOFArray per field
+ *                 wave:    u, v_x, v_y, v_z                    (nfields = 4)
+ *                 euler:   mass, energy, momentum_x, _y, _z    (nfields = 5)
+ *                 maxwell: E_x, E_y, E_z, H_x, H_y, H_z        (nfields = 6)
+ *   metric      : (Nel, 3, 3)  dr_r/dx_x per element (affine simplices)
+ *   face_geom   : (Nel, 4, 4)  outward normal n_x, n_y, n_z and sJ/J per face
+ *   gather      : (Nel, 4, Nfp) uint32 flat index e'*Np + i' of the exterior
+ *                 node of every face node; bit 31 set on boundary faces (the low
+ *                 bits then name the element's own node)
+ *
+ * Return values: DG_OK (0) or one of the dg_status codes; dg_last_error()
+ * returns a message for the calling thread's last failure.
+ */
+#ifndef DGFEM_GB300_H
+#define DGFEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum dg_status {
+  DG_OK = 0,
+  DG_ERR_ARGUMENT = 1,     /* null pointer, bad size, bad enum value */
+  DG_ERR_UNSUPPORTED = 2,  /* order or equation not compiled in */
+  DG_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+  DG_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+  DG_ERR_INDEX = 5         /* a gather index was out of range (device-detected) */
+};
+
+enum dg_equation { DG_WAVE = 0, DG_EULER = 1, DG_MAXWELL = 2 };
+
+typedef struct dg_plan dg_plan;
+
+typedef struct dg_mesh_desc {
+  int32_t order;             /* polynomial degree N, 1..4 */
+  int64_t nelements;         /* Nel >= 1, Nel * Np < 2^31 */
+  const double* metric;      /* device, (Nel, 3, 3) */
+  const double* face_geom;   /* device, (Nel, 4, 4) */
+  const uint32_t* gather;    /* device, (Nel, 4, Nfp) */
+  const double* weak_diff;   /* host, (3, Np, Np): M^-1 S_r^T (wave, euler) */
+  const double* strong_diff; /* host, (3, Np, Np): D_r (maxwell) */
+  const double* lift;        /* host, (Np, 4, Nfp): M^-1 E */
+  const int32_t* face_nodes; /* host, (4, Nfp): volume node of each face node */
+} dg_mesh_desc;
+
+/* Build a plan: validate the description, stage the reference operators in
+ * device memory and size the persistent launch.
+ * params: wave {c}; euler {gamma}; maxwell {alpha, epsilon, mu}.
+ * Replaces the compile step of the reference's array contexts:
+ * actx.compile(rhs) (actx_dgfem_suite/run/__main__.py:74) and the DAG/loopy
+ * pipeline behind it (actx_dgfem_suite/arraycontext/dgfem_optimizer.py:182-245). */
+int dg_plan_create(dg_plan** plan, int32_t equation, const dg_mesh_desc* mesh,
+                   const double* params, int32_t nparams);
+
+/* One RHS evaluation, FP64: rhs = L(q).  Enqueued on `stream` (a cudaStream_t,
+ * NULL = legacy default stream); returns without synchronising.
+ * q and rhs are device arrays of nfields * Nel * Np doubles and must not overlap.
+ * Replaces the call of the compiled RHS, compiled_rhs(*args)
+ * (actx_dgfem_suite/run/__main__.py:76,109,126). */
+int dg_rhs(dg_plan* plan, const double* q, double* rhs, void* stream);
+
+/* Block until `stream` has drained, then report any device-side error flag
+ * the plan's kernels raised (DG_ERR_INDEX, DG_ERR_TIMEOUT) and clear it.
+ * Replaces finish_command_queue(actx) (actx_dgfem_suite/measure.py:48-55). */
+int dg_finish(dg_plan* plan, void* stream);
+
+/* Release the plan's device buffers.  Replaces dropping the compiled program
+ * and freeing the memory pool (actx_dgfem_suite/tools/wave_dof_scaling.py:108-126). */
+int dg_plan_destroy(dg_plan* plan);
+
+/* Describe a plan: any output pointer may be NULL.  grid/block/smem are the
+ * persistent launch shape chosen at plan creation. */
+int dg_plan_info(const dg_plan* plan, int64_t* nelements, int32_t* order,
+                 int32_t* nfields, int32_t* grid, int32_t* block,
+                 int32_t* smem_bytes);
+
+/* Measurement helper (no counterpart in the reference, which hard-codes
+ * datasheet peaks in actx_dgfem_suite/consts.py:1-12): runs `grid` x `block`
+ * threads, each issuing 8 independent FP64 FMA chains of `iters` steps, and
+ * writes one double per thread to `out` (device, grid*block doubles).
+ * FP64 work = 16 * iters * grid * block flops; time it with events. */
+int dg_fp64_fma_probe(double* out, int64_t iters, int32_t grid, int32_t block,
+                      void* stream);
+
+/* Thread-local message for the last failing call, "" if none. */
+const char* dg_last_error(void);
+
+/* ABI version, bumped on any incompatible change. */
+int32_t dg_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DGFEM_GB300_H */

@@ -1,0 +1,78 @@
+"""Shared test helpers: oracle evaluation of a problem and small meshes."""
+
+from __future__ import annotations
+
+import numpy as np
+
+from actx_dgfem_suite_gb300.discretization import make_discretization
+from actx_dgfem_suite_gb300.equations.common import Problem
+from actx_dgfem_suite_gb300.mesh import TetMesh, generate_box_tet_mesh
+
+#: relative L2 parity bound for the FP64 path (spec tolerance)
+FP64_RTOL = 1e-12
+
+
+def oracle_rhs(problem: Problem, od=None) -> np.ndarray:
+    from oracle.geometry import build_oracle_disc
+    from oracle.rhs import euler_rhs, maxwell_rhs, wave_rhs
+    d = problem.disc
+    if od is None:
+        od = build_oracle_disc(d.mesh.vertices, d.mesh.elements, d.order)
+    q = problem.fields
+    if problem.equation == "wave":
+        ru, rv = wave_rhs(od, q[0], q[1:4], *problem.params)
+        return np.concatenate([ru[None], rv])
+    if problem.equation == "euler":
+        return euler_rhs(od, q, *problem.params)
+    return maxwell_rhs(od, q, *problem.params)
+
+
+def rel_l2(a, b) -> float:
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(b))
+
+
+def jittered_box_mesh(n: int, amp: float = 0.15, seed: int = 1) -> TetMesh:
+    """Box mesh on [0,1]^3 with interior vertices moved randomly (non-uniform
+    affine elements, still positively oriented for amp < 0.25)."""
+    m = generate_box_tet_mesh(0.0, 1.0, n)
+    v = m.vertices.copy()
+    h = 1.0 / n
+    interior = np.all((v > 1e-12) & (v < 1 - 1e-12), axis=1)
+    rng = np.random.default_rng(seed)
+    v[interior] += amp * h * rng.uniform(-1, 1, size=(interior.sum(), 3))
+    return TetMesh(vertices=v, elements=m.elements)
+
+
+def single_tet_mesh() -> TetMesh:
+    v = np.array([[0.0, 0, 0], [1.0, 0.1, 0], [0.2, 0.9, 0.1], [0.1, 0.2, 0.8]])
+    return TetMesh(vertices=v, elements=np.array([[0, 1, 2, 3]], dtype=np.int64))
+
+
+def smooth_fields(disc, nfields: int, equation: str, seed: int = 0) -> np.ndarray:
+    """Smooth random-ish state; Euler gets positive density and pressure."""
+    x = disc.nodes()
+    rng = np.random.default_rng(seed)
+    out = np.empty((nfields,) + x.shape[1:])
+    for k in range(nfields):
+        a = rng.uniform(0.5, 2.0, size=3)
+        ph = rng.uniform(0, 2 * np.pi, size=3)
+        out[k] = np.sin(a[0] * 3 * x[0] + ph[0]) * np.cos(a[1] * 2 * x[1] + ph[1]) \
+            + 0.3 * np.sin(a[2] * 4 * x[2] + ph[2])
+    if equation == "euler":
+        out[0] = 1.0 + 0.2 * out[0] ** 2
+        out[2:5] *= 0.2
+        kinetic = 0.5 * (out[2:5] ** 2).sum(axis=0) / out[0]
+        out[1] = 2.5 + 0.3 * out[1] ** 2 + kinetic
+    return out
+
+
+def make_problem(equation: str, mesh: TetMesh, order: int, fields=None,
+                 params=None, seed: int = 0) -> Problem:
+    disc = make_discretization(mesh, order)
+    nf = {"wave": 4, "euler": 5, "maxwell": 6}[equation]
+    if params is None:
+        params = {"wave": (1.0,), "euler": (1.4,), "maxwell": (0.5, 1.0, 1.0)}[equation]
+    if fields is None:
+        fields = smooth_fields(disc, nf, equation, seed)
+    return Problem(equation, disc, fields, params,
+                   None if equation == "wave" else 0.5, "test")
