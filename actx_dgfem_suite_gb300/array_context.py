@@ -113,6 +113,10 @@ class GB300DGArrayContext:
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("GB300DGArrayContext runs on CUDA devices only")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
         _lib.lib()  # load the kernels now, so a missing library fails here
         self.np = _ActxNumpy(self)
         self._meshes: dict[int, DeviceMesh] = {}

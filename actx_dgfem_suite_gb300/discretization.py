@@ -198,5 +198,41 @@ def make_discretization(mesh: TetMesh, order: int) -> DGDiscretization:
         ext_index=ext.reshape(nel, NFACES, nfp))
 
 
+def affine_image(disc: DGDiscretization, scale: float,
+                 offset) -> DGDiscretization:
+    """The discretisation of the mesh mapped by x -> scale * x + offset
+    (scale > 0): connectivity and normals are shared, metric terms rescaled."""
+    if not scale > 0:
+        raise ValueError("scale must be positive")
+    offset = np.broadcast_to(np.asarray(offset, dtype=np.float64), (3,))
+    mesh = TetMesh(vertices=disc.mesh.vertices * scale + offset,
+                   elements=disc.mesh.elements)
+    return DGDiscretization(
+        order=disc.order, ref=disc.ref, mesh=mesh, jac=disc.jac * scale**3,
+        metric=disc.metric / scale, normal=disc.normal,
+        face_jac=disc.face_jac * scale**2, neighbor=disc.neighbor,
+        neighbor_face=disc.neighbor_face, ext_index=disc.ext_index)
+
+
+_UNIT_BOX_CACHE: dict = {}
+
+
 def make_box_discretization(order: int, n, a=-0.5, b=0.5) -> DGDiscretization:
+    """Discretisation of the box [a, b]^3 with ``n`` hexahedra per axis.
+
+    For cubes (scalar ``a``, ``b``, ``n``) the unit-cube discretisation of the
+    most recent (order, n) is cached and mapped affinely, so building the same
+    grid on several boxes costs one connectivity pass."""
+    if np.isscalar(a) and np.isscalar(b) and np.isscalar(n):
+        key = (order, int(n))
+        base = _UNIT_BOX_CACHE.get(key)
+        if base is None:
+            _UNIT_BOX_CACHE.clear()
+            base = make_discretization(generate_box_tet_mesh(0.0, 1.0, n), order)
+            _UNIT_BOX_CACHE[key] = base
+        return affine_image(base, float(b) - float(a), float(a))
     return make_discretization(generate_box_tet_mesh(a, b, n), order)
+
+
+def clear_box_cache() -> None:
+    _UNIT_BOX_CACHE.clear()

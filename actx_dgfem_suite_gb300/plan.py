@@ -35,7 +35,10 @@ class DeviceMesh:
         if not torch.cuda.is_available():
             raise RuntimeError("DeviceMesh needs a CUDA device")
         self.disc = disc
-        self.device = torch.device(device or "cuda")
+        dev = torch.device(device or "cuda")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
         self.metric = torch.from_numpy(disc.metric_flat()).to(self.device)
         self.face_geom = torch.from_numpy(
             np.ascontiguousarray(disc.face_geometry())).to(self.device)

@@ -1,0 +1,463 @@
+#!/usr/bin/env python
+"""Benchmark of the plain FP64 DG-FEM RHS on GB300.
+
+Workload (one "step"): one RHS evaluation of each of the 12 benchmark cases
+-- wave, Euler and Maxwell at P1/P2/P3/P4 on box meshes of 6 n^3 tetrahedra
+with n = 95/70/56/46 (the suite's ``large_`` sizes), benchmark ("baseline")
+problem definitions, FP64.  Metric: RHS DOF-updates/s (nfields * Nel * Np per
+RHS), whole job.
+
+* ``value``: device-resident inputs; per-case CUDA events on the launch
+  stream; every case's state is larger than L2 (129 MB), so no L2 flush is
+  needed between launches.
+* ``e2e``: the same step through the public API with host buffers:
+  ``compiled(t, host_state)`` (host->device copy of the state) and
+  ``actx.to_numpy(result)`` (device->host copy) inside the timed region.
+* ``--impl reference``: the CPU FP64 oracle (a restatement of the
+  reference's operators; the reference itself cannot run here) on a bounded
+  sample of every case, one process per case over the host's cores.
+
+Multi-GPU (torchrun): every rank runs an independent replica (the operator
+does not shard without a halo exchange); value = all ranks' DOF updates over
+the max-over-ranks time, ``scaling`` = "weak".
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+CASES = [(eq, p, n) for eq in ("wave", "euler", "maxwell")
+         for p, n in ((1, 95), (2, 70), (3, 56), (4, 46))]
+METRIC = "RHS DOF-updates/s (plain FP64, wave+Euler+Maxwell P1-P4 sweep)"
+UNIT = "DOF-updates/s"
+WORKLOAD = ("plain FP64 RHS sweep: {wave, euler, maxwell} x P1-P4 on box meshes "
+            "of 6 n^3 tets, n = 95/70/56/46; one RHS per case per step")
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# {{{ clocks sampling
+
+
+class ClockSampler:
+    """Samples SM clock and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# }}}
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def _ncu_traffic() -> dict:
+    """Per-launch DRAM bytes from the committed ncu summary, keyed by case."""
+    out = {}
+    p = ROOT / "profiles" / "dram_traffic_fp64_rhs.txt"
+    if p.exists():
+        for ln in p.read_text().splitlines():
+            f = ln.split()
+            if len(f) >= 3 and f[0] == "traffic":
+                out[f[1]] = float(f[2])
+    return out
+
+
+def fp64_peak_tflops(torch) -> float:
+    """FP64 FMA throughput of the device (library probe, CUDA events)."""
+    import ctypes
+
+    from actx_dgfem_suite_gb300 import _lib
+    L = _lib.lib()
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    grid, block, iters = nsm * 8, 256, 4000
+    buf = torch.empty(grid * block, dtype=torch.float64, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    best = 0.0
+    for _ in range(3):
+        s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+        s.record()
+        _lib.check(L.dg_fp64_fma_probe(ctypes.c_void_p(buf.data_ptr()), iters,
+                                       grid, block, st))
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 16.0 * iters * grid * block / (s.elapsed_time(e) * 1e-3))
+    return best / 1e12
+
+
+# {{{ reference arm (CPU oracle)
+
+
+def _oracle_case(args):
+    eq, order, n_sample, reps = args
+    import numpy as np  # noqa: F401
+
+    from actx_dgfem_suite_gb300.rhs_builder import get_problem
+    from oracle.geometry import build_oracle_disc
+    from oracle.rhs import euler_rhs, maxwell_rhs, wave_rhs
+    prob = get_problem(eq, 3, order, definition="baseline", nel_1d=n_sample)
+    d = prob.disc
+    od = build_oracle_disc(d.mesh.vertices, d.mesh.elements, order)
+    q = prob.fields
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        if eq == "wave":
+            wave_rhs(od, q[0], q[1:4], *prob.params)
+        elif eq == "euler":
+            euler_rhs(od, q, *prob.params)
+        else:
+            maxwell_rhs(od, q, *prob.params)
+    dt = (time.perf_counter() - t0) / reps
+    return prob.nfields * d.nelements * d.np_, dt
+
+
+def cpu_sample_sizes(scale: int) -> list[int]:
+    return [max(2, n // scale) for (_, _, n) in CASES]
+
+
+def run_oracle_sweep(scale: int, reps: int = 1, procs: int | None = None):
+    """Times the oracle on every case at n // scale; returns (dofs, seconds,
+    cores) where seconds is the wall time of the sweep with one process per
+    case."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    sizes = cpu_sample_sizes(scale)
+    jobs = [(eq, p, ns, reps) for (eq, p, _), ns in zip(CASES, sizes)]
+    for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"   # one core per worker process
+    cores = procs or min(len(jobs), os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    with ProcessPoolExecutor(max_workers=cores,
+                             mp_context=mp.get_context("spawn")) as ex:
+        res = list(ex.map(_oracle_case, jobs))
+    wall = time.perf_counter() - t0
+    dofs = sum(r[0] for r in res)
+    busy = sum(r[1] for r in res)
+    return dofs, wall, busy, cores
+
+
+def reference_arm(args) -> None:
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    scale = args.cpu_scale
+    # warm-up: spawn cost, imports, operator assembly
+    for _ in range(max(0, args.warmup)):
+        run_oracle_sweep(scale, reps=1)
+    times, dofs, cores = [], 0, 1
+    for _ in range(args.steps):
+        dofs, wall, busy, cores = run_oracle_sweep(scale, reps=1)
+        # per-case evaluation time (excludes process start-up and setup)
+        times.append(busy / cores)
+    t = statistics.mean(times)
+    value = dofs / t
+    sample = (f"every case at n // {scale} ({', '.join(str(s) for s in cpu_sample_sizes(scale))}), "
+              f"one process per case over {cores} host cores; time = summed "
+              f"per-case RHS time / cores")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD + " (bounded CPU sample)",
+                   "problem": "baseline definitions"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# }}}
+
+
+def our_arm(args) -> None:
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from actx_dgfem_suite_gb300 import perf_model as pm
+    from actx_dgfem_suite_gb300.array_context import GB300DGArrayContext
+    from actx_dgfem_suite_gb300.containers import leaves
+    from actx_dgfem_suite_gb300.discretization import clear_box_cache
+    from actx_dgfem_suite_gb300.rhs_builder import get_rhs
+
+    rank, world, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    actx = GB300DGArrayContext(f"cuda:{local}")
+    dev = actx.device
+
+    cases = CASES if not args.cases else [c for c in CASES
+                                          if f"{c[0]}{c[1]}" in args.cases.split(",")]
+    # {{{ setup through the public API (host mesh/geometry/IC, then upload)
+    t_setup = time.perf_counter()
+    runs = []
+    for (eq, order, n) in cases:
+        n_eff = max(2, n // args.scale)
+        rhs, call_args = get_rhs(eq, actx, 3, order, definition="baseline",
+                                 nel_1d=n_eff)
+        compiled = actx.compile(rhs)
+        state = call_args[-1]
+        q = compiled.stage(state)
+        out = torch.empty_like(q)
+        nel = rhs.dg_operator.disc.nelements
+        runs.append(dict(eq=eq, order=order, n=n_eff, compiled=compiled,
+                         call_args=call_args, q=q, out=out,
+                         cost=pm.RhsCost(eq, order, nel)))
+        rhs.dg_operator.disc._cache.clear()
+    clear_box_cache()
+    setup_s = time.perf_counter() - t_setup
+    # }}}
+
+    fp64_peak = fp64_peak_tflops(torch)
+    stream = torch.cuda.current_stream()
+
+    def step(record=None):
+        for k, r in enumerate(runs):
+            if record is not None:
+                record[k][0].record(stream)
+            r["compiled"].plan.rhs(r["q"], r["out"])
+            if record is not None:
+                record[k][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    for r in runs:
+        r["compiled"].plan.finish()
+
+    K = args.steps
+    events = [[(torch.cuda.Event(True), torch.cuda.Event(True)) for _ in runs]
+              for _ in range(K)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_all0 = torch.cuda.Event(True)
+    t_all1 = torch.cuda.Event(True)
+    t_all0.record(stream)
+    for s in range(K):
+        step(events[s])
+    t_all1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clock_info = clocks.stop()
+    for r in runs:
+        r["compiled"].plan.finish()   # raises on any device-side error flag
+    total_ms = t_all0.elapsed_time(t_all1)
+    case_ms = [statistics.mean(events[s][k][0].elapsed_time(events[s][k][1])
+                               for s in range(K)) for k in range(len(runs))]
+    ms_step = total_ms / K
+    if world > 1:
+        t = torch.tensor([ms_step], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    dofs_step = sum(r["cost"].dofs for r in runs)
+    value = world * dofs_step / (ms_step * 1e-3)
+    flops_step = sum(r["cost"].flops for r in runs)
+
+    # {{{ e2e through the public API with host buffers
+    host_states = []
+    for r in runs:
+        hq = r["q"].cpu().pin_memory()
+        tmpl = r["call_args"][-1]
+        from actx_dgfem_suite_gb300.containers import from_stacked
+        hs = from_stacked(actx, tmpl, hq)
+        host_states.append(r["call_args"][:-1] + (hs,))
+    h2d = sum(r["q"].numel() * 8 for r in runs)
+    d2h = h2d
+
+    def e2e_step():
+        res = []
+        for r, a in zip(runs, host_states):
+            out = r["compiled"](*a)
+            res.append(actx.to_numpy(out))
+        return res
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ke = max(1, min(K, 3))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        host_out = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / ke
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    # sanity: the host result equals the device-resident result
+    ok = all(np.array_equal(np.stack([d[0] for d in leaves(h)]),
+                            r["out"].cpu().numpy())
+             for h, r in zip(host_out[:1], runs[:1]))
+    e2e_value = world * dofs_step / e2e_s
+    # }}}
+
+    # {{{ roofline of the dominant launch
+    peaks = _peaks()
+    dom = max(range(len(runs)), key=lambda k: case_ms[k])
+    rd = runs[dom]
+    c = rd["cost"]
+    t_dom = case_ms[dom] * 1e-3
+    achieved_gbs = c.bytes / t_dom / 1e9
+    traffic = _ncu_traffic().get(f"{rd['eq']}{rd['order']}")
+    if traffic is not None and args.scale != 1:
+        traffic = None
+    fp64_achieved = 2.0 * c.fma / t_dom / 1e12
+    roofline = {
+        "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
+        "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
+        "traffic": traffic,
+        "kernel": f"dg_rhs_fp64_kernel<{rd['order']},{rd['eq']}>",
+        "peak_source": peaks["source"],
+        "fp64_pipe": {"achieved_tflops": fp64_achieved,
+                      "peak_tflops": fp64_peak,
+                      "frac": fp64_achieved / fp64_peak,
+                      "peak_source": "measured live (dg_fp64_fma_probe)"},
+        "limiter": "fp64 pipe",
+        "suite_model_frac": c.roofline_seconds(fp64_peak * 1e12,
+                                               peaks["hbm_gbs"] * 1e9) / t_dom,
+    }
+    # }}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        dofs_c, wall, busy, cores = run_oracle_sweep(args.cpu_scale, reps=1)
+        cpu = {"value": dofs_c / (busy / cores), "unit": UNIT, "cores": cores,
+               "kind": "port",
+               "sample": (f"CPU FP64 oracle, every case at n // {args.cpu_scale}, "
+                          f"one process per case")}
+
+    per_case = [{"case": f"{r['eq']} P{r['order']} n={r['n']}",
+                 "nel": r["cost"].nelements, "ms": case_ms[k],
+                 "gdof_s": r["cost"].dofs / case_ms[k] / 1e6,
+                 "gflops_suite": r["cost"].flops / case_ms[k] / 1e6,
+                 "fp64_frac": 2 * r["cost"].fma / (case_ms[k] * 1e-3) / 1e12 / fp64_peak,
+                 "hbm_frac": r["cost"].bytes / (case_ms[k] * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+                for k, r in enumerate(runs)]
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": K, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "problem": "baseline definitions",
+                       "l2": "inputs larger than L2 (every case's state > 129 MB)",
+                       "parallelism": f"replicas x{world}",
+                       "scale_divisor": args.scale},
+            "gflops_suite": world * flops_step / (ms_step * 1e-3) / 1e9,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "host_matches_device": bool(ok)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clock_info,
+            "gpu_launches": len(runs) * K,
+            "setup_s": setup_s,
+            "cases": per_case,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--scale", type=int, default=1,
+                    help="divide every n by this (quick runs; 1 = benchmark sizes)")
+    ap.add_argument("--cpu-scale", type=int, default=4,
+                    help="CPU sample: every case at n // cpu-scale")
+    ap.add_argument("--cases", default="", help="subset, e.g. wave3,euler4")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args(argv)
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

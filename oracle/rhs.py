@@ -49,10 +49,13 @@ def traces(d: OracleDisc, u: np.ndarray):
 # }}}
 
 
-def wave_rhs(d: OracleDisc, u: np.ndarray, v: np.ndarray, c: float = 1.0):
+def wave_rhs(d: OracleDisc, u: np.ndarray, v: np.ndarray, c: float = 1.0,
+             parts: bool = False):
     """``actx_dgfem_suite/equations/wave.py:121-200`` with ``quad_tag=None``.
 
-    Returns ``(rhs_u (Nel, Np), rhs_v (3, Nel, Np))``."""
+    Returns ``(rhs_u (Nel, Np), rhs_v (3, Nel, Np))``; with ``parts=True``
+    returns ``(rhs (4, Nel, Np), volume part, surface part)`` where the parts
+    are the inverse-mass images of the volume and face-mass terms."""
     n = d.normal.transpose(2, 0, 1)[..., None]            # (3, Nel, 4, 1)
     ui, ue = traces(d, u)
     vi = np.empty((3,) + ui.shape)
@@ -81,6 +84,12 @@ def wave_rhs(d: OracleDisc, u: np.ndarray, v: np.ndarray, c: float = 1.0):
     wg = weak_grad(d, u)
     rhs_v = np.stack([inverse_mass(d, -c * wg[x] + face_mass(d, flux_v[x]))
                       for x in range(3)])
+    if parts:
+        vol = np.stack([inverse_mass(d, -c * weak_div(d, v))]
+                       + [inverse_mass(d, -c * wg[x]) for x in range(3)])
+        surf = np.stack([inverse_mass(d, face_mass(d, flux_u))]
+                        + [inverse_mass(d, face_mass(d, flux_v[x])) for x in range(3)])
+        return np.concatenate([rhs_u[None], rhs_v]), vol, surf
     return rhs_u, rhs_v
 
 
@@ -111,13 +120,15 @@ def _wavespeed(rho, rho_e, rho_u, gamma):
     return np.sqrt((u * u).sum(axis=0)) + np.sqrt(gamma * (p / rho))
 
 
-def euler_rhs(d: OracleDisc, q: np.ndarray, gamma: float = 1.4) -> np.ndarray:
+def euler_rhs(d: OracleDisc, q: np.ndarray, gamma: float = 1.4,
+              parts: bool = False):
     """grudge ``EulerOperator.operator`` (flux_type "lf", InviscidWallBC on
     all boundaries, no over-integration), as set up at
     ``actx_dgfem_suite/equations/euler.py:168-179``.
 
     ``q``: (5, Nel, Np) ordered mass, energy, momentum_x, momentum_y,
-    momentum_z.  Returns the RHS in the same layout."""
+    momentum_z.  Returns the RHS in the same layout (with ``parts=True``:
+    ``(rhs, volume part, surface part)``)."""
     rho, rho_e, rho_u = q[0], q[1], q[2:5]
     fvol = _volume_flux(rho, rho_e, rho_u, gamma)          # (5, 3, Nel, Np)
     volume = np.stack([weak_div(d, fvol[k]) for k in range(5)])
@@ -144,8 +155,13 @@ def euler_rhs(d: OracleDisc, q: np.ndarray, gamma: float = 1.4) -> np.ndarray:
     num = num - lam[None, None] * (qe - qi)[:, None] * n[None, :, :, :, None] / 2
     fn = (num * n[None, :, :, :, None]).sum(axis=1)        # num_flux @ normal
 
-    return np.stack([inverse_mass(d, volume[k] - face_mass(d, fn[k]))
-                     for k in range(5)])
+    rhs = np.stack([inverse_mass(d, volume[k] - face_mass(d, fn[k]))
+                    for k in range(5)])
+    if parts:
+        vol = np.stack([inverse_mass(d, volume[k]) for k in range(5)])
+        surf = np.stack([inverse_mass(d, -face_mass(d, fn[k])) for k in range(5)])
+        return rhs, vol, surf
+    return rhs
 
 
 # }}}
@@ -161,7 +177,7 @@ def _cross(a, b):
 
 
 def maxwell_rhs(d: OracleDisc, w: np.ndarray, alpha: float = 0.5,
-                epsilon: float = 1.0, mu: float = 1.0) -> np.ndarray:
+                epsilon: float = 1.0, mu: float = 1.0, parts: bool = False):
     """grudge ``MaxwellOperator.operator`` (3D, constant material, numeric
     flux_type ``alpha``, PEC on all boundaries), as set up at
     ``actx_dgfem_suite/equations/maxwell.py:55-70``.
@@ -192,7 +208,10 @@ def maxwell_rhs(d: OracleDisc, w: np.ndarray, alpha: float = 0.5,
     lifted = np.stack([inverse_mass(d, face_mass(d, fl[k])) for k in range(6)])
     local = np.concatenate([-curl_h, curl_e])
     div = np.array([epsilon] * 3 + [mu] * 3)[:, None, None]
-    return (-local - lifted) / div
+    rhs = (-local - lifted) / div
+    if parts:
+        return rhs, -local / div, -lifted / div
+    return rhs
 
 
 # }}}

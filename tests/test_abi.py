@@ -1,0 +1,61 @@
+"""The C-ABI library loads without a GPU and exports every entry point that
+include/*.h declares; argument validation needs no device."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from actx_dgfem_suite_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _declared_functions():
+    names = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?\w+\s*\*?\s*(dg_\w+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_known_symbols():
+    declared = _declared_functions()
+    assert declared == set(_lib.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_all_declared_symbols():
+    L = _lib.lib()
+    for name in _declared_functions():
+        assert hasattr(L, name), name
+        assert ctypes.cast(getattr(L, name), ctypes.c_void_p).value
+
+
+def test_version_and_error_strings():
+    L = _lib.lib()
+    assert L.dg_abi_version() == 1
+    assert isinstance(L.dg_last_error(), bytes)
+
+
+def test_argument_errors_without_device():
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    # NULL mesh description -> DG_ERR_ARGUMENT, no CUDA call made
+    assert L.dg_plan_create(ctypes.byref(h), 0, None, None, 0) == _lib.DG_ERR_ARGUMENT
+    assert b"NULL" in L.dg_last_error()
+    d = _lib.MeshDesc()
+    d.order = 7
+    d.nelements = 10
+    assert L.dg_plan_create(ctypes.byref(h), 0, ctypes.byref(d), None, 0) \
+        == _lib.DG_ERR_UNSUPPORTED
+    d.order = 2
+    assert L.dg_plan_create(ctypes.byref(h), 9, ctypes.byref(d), None, 0) \
+        == _lib.DG_ERR_ARGUMENT
+    assert L.dg_rhs(None, None, None, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_finish(None, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_plan_destroy(None) == _lib.DG_OK
+    assert L.dg_fp64_fma_probe(None, 1, 1, 1, None) == _lib.DG_ERR_ARGUMENT
+    with pytest.raises(_lib.DGError):
+        _lib.check(L.dg_rhs(None, None, None, None))

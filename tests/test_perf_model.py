@@ -1,0 +1,43 @@
+"""FLOP/byte model: einsum counts follow the reference's counting rule."""
+
+import numpy as np
+import pytest
+
+from actx_dgfem_suite_gb300 import perf_model as pm
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_einsum_counts_match_opt_einsum(order):
+    oe = pytest.importorskip("opt_einsum")
+    from math import prod
+    E = 7
+    n, nfp = pm.np_of(order), pm.nfp_of(order)
+
+    def count(spec, shapes):
+        ops = [np.empty(s) for s in shapes]
+        _, info = oe.contract_path(spec, *ops, optimize="optimal", use_blas=False)
+        tot = 0
+        for (_, contracted, es, _, _) in info.contraction_list:
+            it = prod(info.size_dict[c]
+                      for c in set(es.translate(str.maketrans("", "", " ->,"))))
+            tot += 2 * it if contracted else it
+        return tot // E
+
+    assert count("re,rji,ej->ei", [(3, E), (3, n, n), (E, n)]) == pm.grad_flops(order)
+    assert count("xre,rji,xej->ei", [(3, 3, E), (3, n, n), (3, E, n)]) \
+        == pm.div_flops(order)
+    assert count("jfi,fe,fej->ei", [(nfp, 4, n), (4, E), (4, E, nfp)]) \
+        == pm.lift_flops(order)
+
+
+def test_known_values():
+    assert [pm.grad_flops(p) for p in (1, 2, 3, 4)] == [108, 630, 2460, 7455]
+    assert [pm.div_flops(p) for p in (1, 2, 3, 4)] == [168, 780, 2760, 7980]
+    assert [pm.lift_flops(p) for p in (1, 2, 3, 4)] == [108, 504, 1640, 4260]
+
+
+def test_cost_object():
+    c = pm.RhsCost("wave", 3, 1000)
+    assert c.dofs == 4 * 1000 * 20
+    assert c.bytes == 1000 * (16 * 4 * 20 + 72 + 128 + 16 * 10)
+    assert c.roofline_seconds(1e12, 1e12) == max(c.flops, c.bytes) / 1e12
