@@ -23,8 +23,12 @@ DG_WAVE = 0
 DG_EULER = 1
 DG_MAXWELL = 2
 
+DG_FP64 = 0
+DG_FP32_MIXED = 1
+
 #: every entry point declared in include/dgfem_gb300.h
-EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_finish", "dg_plan_destroy",
+EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
+                    "dg_plan_destroy",
                     "dg_plan_info", "dg_fp64_fma_probe", "dg_last_error",
                     "dg_abi_version")
 
@@ -72,11 +76,14 @@ def lib() -> ctypes.CDLL:
     L = ctypes.CDLL(str(_LIB_PATH))
     vp = ctypes.c_void_p
     L.dg_plan_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int32,
-                                 ctypes.POINTER(MeshDesc),
+                                 ctypes.c_int32, ctypes.POINTER(MeshDesc),
                                  ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
     L.dg_plan_create.restype = ctypes.c_int
     L.dg_rhs.argtypes = [vp, vp, vp, vp]
     L.dg_rhs.restype = ctypes.c_int
+    dbl = ctypes.c_double
+    L.dg_rk_stage.argtypes = [vp, vp, vp, vp, dbl, dbl, dbl, vp]
+    L.dg_rk_stage.restype = ctypes.c_int
     L.dg_finish.argtypes = [vp, vp]
     L.dg_finish.restype = ctypes.c_int
     L.dg_plan_destroy.argtypes = [vp]

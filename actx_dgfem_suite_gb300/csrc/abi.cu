@@ -8,7 +8,7 @@
 
 #include "../../include/dgfem_gb300.h"
 #include "dg_launch.h"
-#include "dg_rhs_fp64.cuh"  // RhsArgs, kBlock
+#include "dg_rhs.cuh"  // RhsArgs, kBlock
 
 namespace {
 
@@ -20,8 +20,7 @@ int fail(int code, const std::string& msg) {
 }
 
 int cuda_fail(cudaError_t err, const char* what) {
-  return fail(DG_ERR_CUDA,
-              std::string(what) + ": " + cudaGetErrorString(err));
+  return fail(DG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
 }
 
 int nfields_of(int eq) {
@@ -35,19 +34,45 @@ int nfields_of(int eq) {
 
 int nparams_of(int eq) { return eq == DG_MAXWELL ? 3 : 1; }
 
+cudaError_t shape_of(int eq, int order, int precision, int mode,
+                     dg::LaunchShape* out) {
+  switch (eq) {
+    case DG_WAVE: return dg::shape_wave(order, precision, mode, out);
+    case DG_EULER: return dg::shape_euler(order, precision, mode, out);
+    case DG_MAXWELL: return dg::shape_maxwell(order, precision, mode, out);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_of(int eq, int order, int precision, int mode,
+                      const dg::RhsArgs& a, int grid, cudaStream_t s) {
+  switch (eq) {
+    case DG_WAVE: return dg::launch_wave(order, precision, mode, a, grid, s);
+    case DG_EULER: return dg::launch_euler(order, precision, mode, a, grid, s);
+    case DG_MAXWELL: return dg::launch_maxwell(order, precision, mode, a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+bool overlap(const void* a, const void* b, int64_t bytes) {
+  const char* x = static_cast<const char*>(a);
+  const char* y = static_cast<const char*>(b);
+  return x < y + bytes && y < x + bytes;
+}
+
 __global__ void fp64_fma_probe_kernel(double* out, int64_t iters) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double a[8];
+  double v[8];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-9 * (double)(tid + k);
+  for (int k = 0; k < 8; ++k) v[k] = 1.0 + 1e-9 * (double)(tid + k);
   const double b = 0.9999999, c = 1e-7;
   for (int64_t it = 0; it < iters; ++it) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+    for (int k = 0; k < 8; ++k) v[k] = fma(v[k], b, c);
   }
   double s = 0.0;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) s += a[k];
+  for (int k = 0; k < 8; ++k) s += v[k];
   out[tid] = s;
 }
 
@@ -55,13 +80,14 @@ __global__ void fp64_fma_probe_kernel(double* out, int64_t iters) {
 
 struct dg_plan {
   int32_t equation = 0;
+  int32_t precision = 0;
   int32_t order = 0;
   int32_t np = 0, nfp = 0, nfields = 0;
   int64_t nel = 0;
   const double* metric = nullptr;
   const double* face_geom = nullptr;
   const uint32_t* gather = nullptr;
-  double* d_ops = nullptr;
+  void* d_ops = nullptr;
   uint32_t ops_bytes = 0;
   int* d_status = nullptr;
   double params[3] = {0, 0, 0};
@@ -70,13 +96,50 @@ struct dg_plan {
   int device = 0;
 };
 
+namespace {
+
+dg::RhsArgs base_args(const dg_plan* p) {
+  dg::RhsArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.metric = p->metric;
+  a.face_geom = p->face_geom;
+  a.gather = p->gather;
+  a.ops = p->d_ops;
+  a.ops_bytes = p->ops_bytes;
+  a.nel = p->nel;
+  a.status = p->d_status;
+  a.p0 = p->params[0];
+  a.p1 = p->params[1];
+  a.p2 = p->params[2];
+  return a;
+}
+
+template <typename Real>
+void pack_ops(std::vector<unsigned char>& buf, const dg::OpsOffsets& off,
+              int np, int nfp, const double* diff, const double* lift,
+              const int32_t* face_nodes) {
+  Real* w = reinterpret_cast<Real*>(buf.data() + off.w);
+  Real* l = reinterpret_cast<Real*>(buf.data() + off.l);
+  int32_t* fn = reinterpret_cast<int32_t*>(buf.data() + off.fn);
+  for (int r = 0; r < 3; ++r)
+    for (int i = 0; i < np; ++i)
+      for (int j = 0; j < np; ++j)
+        w[(r * np + j) * np + i] = (Real)diff[(r * np + i) * np + j];
+  for (int i = 0; i < np; ++i)
+    for (int fj = 0; fj < 4 * nfp; ++fj)
+      l[fj * np + i] = (Real)lift[i * 4 * nfp + fj];
+  for (int k = 0; k < 4 * nfp; ++k) fn[k] = face_nodes[k];
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* dg_last_error(void) { return g_last_error.c_str(); }
 
-int32_t dg_abi_version(void) { return 1; }
+int32_t dg_abi_version(void) { return 2; }
 
-int dg_plan_create(dg_plan** plan_out, int32_t equation,
+int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,
                    int32_t nparams) {
   g_last_error.clear();
@@ -85,6 +148,8 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation,
   if (!mesh) return fail(DG_ERR_ARGUMENT, "mesh description is NULL");
   const int nf = nfields_of(equation);
   if (nf == 0) return fail(DG_ERR_ARGUMENT, "unknown equation");
+  if (precision != DG_FP64 && precision != DG_FP32_MIXED)
+    return fail(DG_ERR_ARGUMENT, "unknown precision");
   if (mesh->order < 1 || mesh->order > 4)
     return fail(DG_ERR_UNSUPPORTED, "order must be 1..4");
   if (mesh->nelements < 1) return fail(DG_ERR_ARGUMENT, "nelements must be >= 1");
@@ -99,9 +164,8 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation,
   const double* diff =
       equation == DG_MAXWELL ? mesh->strong_diff : mesh->weak_diff;
   if (!diff)
-    return fail(DG_ERR_ARGUMENT,
-                equation == DG_MAXWELL ? "strong_diff is NULL"
-                                       : "weak_diff is NULL");
+    return fail(DG_ERR_ARGUMENT, equation == DG_MAXWELL ? "strong_diff is NULL"
+                                                         : "weak_diff is NULL");
   if (nparams != nparams_of(equation) || (nparams > 0 && !params))
     return fail(DG_ERR_ARGUMENT, "wrong number of equation parameters");
   for (int k = 0; k < 4 * nfp; ++k)
@@ -119,34 +183,28 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation,
     }
   }
 
-  dg::LaunchShape shape;
-  cudaError_t err = cudaErrorInvalidValue;
-  switch (equation) {
-    case DG_WAVE: err = dg::fp64_shape_wave(N, &shape); break;
-    case DG_EULER: err = dg::fp64_shape_euler(N, &shape); break;
-    case DG_MAXWELL: err = dg::fp64_shape_maxwell(N, &shape); break;
-  }
+  dg::LaunchShape shape, shape_stage;
+  cudaError_t err = shape_of(equation, N, precision, 0, &shape);
+  if (err == cudaSuccess) err = shape_of(equation, N, precision, 1, &shape_stage);
   if (err != cudaSuccess) return cuda_fail(err, "kernel configuration");
+  if (shape_stage.blocks_per_sm < shape.blocks_per_sm)
+    shape.blocks_per_sm = shape_stage.blocks_per_sm;
   if (shape.blocks_per_sm < 1)
     return fail(DG_ERR_UNSUPPORTED, "kernel does not fit on an SM");
-  const dg::OpsOffsets off = dg::ops_offsets(np, nfp);
-  if (off.size != shape.ops_doubles)
+  const int rs = precision == DG_FP64 ? 8 : 4;
+  const dg::OpsOffsets off = dg::ops_offsets(np, nfp, rs);
+  if (off.size != shape.ops_bytes)
     return fail(DG_ERR_CUDA, "operator layout mismatch between host and kernel");
 
-  // pack [Wt | Lt | face_nodes]
-  std::vector<double> ops(off.size, 0.0);
-  for (int r = 0; r < 3; ++r)
-    for (int i = 0; i < np; ++i)
-      for (int j = 0; j < np; ++j)
-        ops[off.w + (r * np + j) * np + i] = diff[(r * np + i) * np + j];
-  for (int i = 0; i < np; ++i)
-    for (int fj = 0; fj < 4 * nfp; ++fj)
-      ops[off.l + fj * np + i] = mesh->lift[i * 4 * nfp + fj];
-  int32_t* fn = reinterpret_cast<int32_t*>(ops.data() + off.fn);
-  for (int k = 0; k < 4 * nfp; ++k) fn[k] = mesh->face_nodes[k];
+  std::vector<unsigned char> ops(off.size, 0);
+  if (precision == DG_FP64)
+    pack_ops<double>(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
+  else
+    pack_ops<float>(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
 
   dg_plan* p = new dg_plan;
   p->equation = equation;
+  p->precision = precision;
   p->order = N;
   p->np = np;
   p->nfp = nfp;
@@ -156,7 +214,7 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation,
   p->face_geom = mesh->face_geom;
   p->gather = mesh->gather;
   p->shape = shape;
-  p->ops_bytes = static_cast<uint32_t>(off.size * sizeof(double));
+  p->ops_bytes = static_cast<uint32_t>(off.size);
   for (int k = 0; k < nparams; ++k) p->params[k] = params[k];
   cudaGetDevice(&p->device);
 
@@ -182,32 +240,36 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation,
 int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (!q || !rhs) return fail(DG_ERR_ARGUMENT, "state or rhs pointer is NULL");
-  const int64_t n = (int64_t)p->nfields * p->nel * p->np;
-  const char* qb = reinterpret_cast<const char*>(q);
-  const char* rb = reinterpret_cast<const char*>(rhs);
-  if (qb < rb + n * 8 && rb < qb + n * 8)
-    return fail(DG_ERR_ARGUMENT, "state and rhs overlap");
-  dg::RhsArgs a;
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  if (overlap(q, rhs, bytes)) return fail(DG_ERR_ARGUMENT, "state and rhs overlap");
+  dg::RhsArgs a = base_args(p);
   a.q = q;
   a.rhs = rhs;
-  a.metric = p->metric;
-  a.face_geom = p->face_geom;
-  a.gather = p->gather;
-  a.ops = p->d_ops;
-  a.ops_bytes = p->ops_bytes;
-  a.nel = p->nel;
-  a.status = p->d_status;
-  a.p0 = p->params[0];
-  a.p1 = p->params[1];
-  a.p2 = p->params[2];
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  cudaError_t err = cudaErrorInvalidValue;
-  switch (p->equation) {
-    case DG_WAVE: err = dg::fp64_launch_wave(p->order, a, p->grid, s); break;
-    case DG_EULER: err = dg::fp64_launch_euler(p->order, a, p->grid, s); break;
-    case DG_MAXWELL: err = dg::fp64_launch_maxwell(p->order, a, p->grid, s); break;
-  }
+  cudaError_t err = launch_of(p->equation, p->order, p->precision, 0, a, p->grid,
+                              reinterpret_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(err, "rhs launch");
+  return DG_OK;
+}
+
+int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
+                double a_coef, double b_coef, double dt, void* stream) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!q_in || !q_out || !res)
+    return fail(DG_ERR_ARGUMENT, "state, output or residual pointer is NULL");
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  if (overlap(q_in, q_out, bytes) || overlap(q_in, res, bytes) ||
+      overlap(q_out, res, bytes))
+    return fail(DG_ERR_ARGUMENT, "q_in, q_out and res must not overlap");
+  dg::RhsArgs a = base_args(p);
+  a.q = q_in;
+  a.q_out = q_out;
+  a.res = res;
+  a.rk_a = a_coef;
+  a.rk_b = b_coef;
+  a.rk_dt = dt;
+  cudaError_t err = launch_of(p->equation, p->order, p->precision, 1, a, p->grid,
+                              reinterpret_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
   return DG_OK;
 }
 
@@ -221,9 +283,8 @@ int dg_finish(dg_plan* p, void* stream) {
   if (err != cudaSuccess) return cuda_fail(err, "status read");
   if (status != 0) {
     cudaMemset(p->d_status, 0, sizeof(int));
-    return fail(status, status == DG_ERR_INDEX
-                            ? "a gather index was out of range"
-                            : "a device-side wait timed out");
+    return fail(status, status == DG_ERR_INDEX ? "a gather index was out of range"
+                                               : "a device-side wait timed out");
   }
   return DG_OK;
 }

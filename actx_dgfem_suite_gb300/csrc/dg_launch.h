@@ -14,35 +14,37 @@ struct LaunchShape {
   int smem_bytes = 0;      // dynamic shared memory per CTA
   int blocks_per_sm = 0;   // resident CTAs per SM at that footprint
   int elems_per_tile = 0;  // elements per CTA tile
-  int ops_doubles = 0;     // size of the staged operator block
+  int ops_bytes = 0;       // size of the staged operator block
 };
 
-// Layout of the operator block (in doubles), shared by host packing and the
-// kernels' OpsLayout<N>: [Wt (3 Np Np) | Lt (4 Nfp Np) | int32 face_nodes].
+// Byte layout of the operator block, shared by host packing and the kernels'
+// OpsLayout<N, Real>: [Wt (3 Np Np) | Lt (4 Nfp Np) | int32 face_nodes],
+// each segment padded to 16 bytes; `rs` = sizeof(Real).
 struct OpsOffsets {
   int w, l, fn, size;
 };
-inline int pad2_host(int n) { return (n + 1) & ~1; }
-inline OpsOffsets ops_offsets(int np, int nfp) {
+inline int pad16_host(int n) { return (n + 15) & ~15; }
+inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
   OpsOffsets o;
   o.w = 0;
-  o.l = o.w + pad2_host(3 * np * np);
-  o.fn = o.l + pad2_host(4 * nfp * np);
-  o.size = o.fn + pad2_host((4 * nfp + 1) / 2);
+  o.l = o.w + pad16_host(3 * np * np * rs);
+  o.fn = o.l + pad16_host(4 * nfp * np * rs);
+  o.size = o.fn + pad16_host(4 * nfp * 4);
   return o;
 }
 
 // Per equation: shape query (also raises the kernel's shared-memory limit on
-// the current device) and launch.  Return cudaErrorInvalidValue for an order
-// that is not compiled in.
-cudaError_t fp64_shape_wave(int order, LaunchShape* out);
-cudaError_t fp64_shape_euler(int order, LaunchShape* out);
-cudaError_t fp64_shape_maxwell(int order, LaunchShape* out);
-cudaError_t fp64_launch_wave(int order, const RhsArgs& a, int grid,
-                             cudaStream_t s);
-cudaError_t fp64_launch_euler(int order, const RhsArgs& a, int grid,
-                              cudaStream_t s);
-cudaError_t fp64_launch_maxwell(int order, const RhsArgs& a, int grid,
-                                cudaStream_t s);
+// the current device) and launch, for precision 0 (FP64) or 1 (FP32
+// arithmetic, FP64 state) and mode 0 (RHS) or 1 (fused RK stage).  Return
+// cudaErrorInvalidValue for a combination that is not compiled in.
+#define DG_DECLARE_EQ(name)                                                   \
+  cudaError_t shape_##name(int order, int precision, int mode,               \
+                           LaunchShape* out);                                \
+  cudaError_t launch_##name(int order, int precision, int mode,              \
+                            const RhsArgs& a, int grid, cudaStream_t s);
+DG_DECLARE_EQ(wave)
+DG_DECLARE_EQ(euler)
+DG_DECLARE_EQ(maxwell)
+#undef DG_DECLARE_EQ
 
 }  // namespace dg

@@ -1,0 +1,465 @@
+// Fused DG-FEM RHS kernel for affine tetrahedra on sm_103a.
+//
+// One persistent launch evaluates the whole RHS of one equation.  Each CTA
+// stages the reference operators (weak or strong D_r and LIFT, with the face
+// node table) into shared memory once, by a single TMA bulk copy, then loops
+// over tiles of E = 256 / Np elements:
+//
+//   1. load the tile's state (all fields, FP64) and geometry into shared memory;
+//   2. pointwise pre-pass per node: metric-combined inputs of the weak
+//      divergence (wave: v, euler: the flux F(q)); maxwell needs none;
+//   3. volume term per output node, in registers:
+//        wave    -c * sum_r W_r (G v)_r        and  -c * G^T (W_r u)
+//        euler    sum_r W_r (G F(q))_r
+//        maxwell  curl via sum_r G[r][x] D_r q
+//      (the fused einsums ``xre,rij,xej->ei`` and ``re,rij,ej->ei`` of
+//      actx_dgfem_suite/arraycontext/mass_inverse_fuser.py:39-74, with the
+//      three reference derivatives of a field shared by its gradient
+//      components);
+//   4. face gather + numerical flux per face node, scaled by sJ/J, into
+//      shared memory (exterior values through the flat gather index of
+//      actx_dgfem_suite/arraycontext/constants_folder.py:69-100);
+//   5. LIFT ``jfi,fe,fej->ei`` (mass_inverse_fuser.py:21-38 after the
+//      transpose of transpose_consts_in_einsums.py:5-35) added to the volume
+//      term, then either stored (MODE_RHS) or folded into a low-storage
+//      Runge-Kutta stage (MODE_STAGE): res = a res + dt L(q), q_out = q + b res.
+//
+// ``Real`` is the arithmetic type of steps 2-5.  double: the plain FP64 path.
+// float: the mixed-precision path -- derivative, flux and LIFT arithmetic in
+// FP32 while the state, the RK accumulation and the Euler pressure recovery
+// from total energy stay FP64.
+//
+// The flux formulas follow actx_dgfem_suite/equations/wave.py:80-114 (wave),
+// grudge's euler_numerical_flux with LF stabilisation and InviscidWallBC
+// (configured at equations/euler.py:168-174) and grudge's MaxwellOperator
+// alpha-flux with PEC (configured at equations/maxwell.py:55-59).
+#pragma once
+
+#include <type_traits>
+
+#include "dg_common.cuh"
+
+namespace dg {
+
+enum { MODE_RHS = 0, MODE_STAGE = 1 };
+
+struct RhsArgs {
+  const double* q;
+  double* rhs;             // MODE_RHS output
+  double* q_out;           // MODE_STAGE outputs
+  double* res;
+  double rk_a, rk_b, rk_dt;
+  const double* metric;
+  const double* face_geom;
+  const uint32_t* gather;
+  const void* ops;         // [Wt | Lt | face_nodes], see OpsLayout
+  uint32_t ops_bytes;
+  int64_t nel;
+  int* status;
+  double p0, p1, p2;       // equation parameters
+};
+
+template <int N>
+struct Shape {
+  static constexpr int NP = (N + 1) * (N + 2) * (N + 3) / 6;
+  static constexpr int NFP = (N + 1) * (N + 2) / 2;
+  static constexpr int NFPT = 4 * NFP;  // face points per element
+};
+
+template <int EQ>
+struct EqInfo;
+template <>
+struct EqInfo<DG_WAVE> {
+  static constexpr int NF = 4, NAUX = 3;
+};
+template <>
+struct EqInfo<DG_EULER> {
+  static constexpr int NF = 5, NAUX = 15;
+};
+template <>
+struct EqInfo<DG_MAXWELL> {
+  static constexpr int NF = 6, NAUX = 0;
+};
+
+constexpr int pad16(int bytes) { return (bytes + 15) & ~15; }
+
+// Layout of the operator block in bytes, identical in global and shared memory.
+template <int N, typename Real>
+struct OpsLayout {
+  static constexpr int NP = Shape<N>::NP, NFPT = Shape<N>::NFPT;
+  static constexpr int W = 0;                                      // Wt[r][j][i]
+  static constexpr int L = W + pad16(3 * NP * NP * (int)sizeof(Real));  // Lt[fj][i]
+  static constexpr int FN = L + pad16(NFPT * NP * (int)sizeof(Real));   // int32[fj]
+  static constexpr int SIZE = FN + pad16(NFPT * 4);
+};
+
+// Shared-memory layout of one CTA, in bytes.
+template <int N, int EQ, typename Real>
+struct Tile {
+  static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP,
+                       NFPT = Shape<N>::NFPT;
+  static constexpr int NF = EqInfo<EQ>::NF, NAUX = EqInfo<EQ>::NAUX;
+  static constexpr int E = kBlock / NP;
+  static constexpr bool MIXED = !std::is_same<Real, double>::value;
+  static constexpr int RS = (int)sizeof(Real);
+  static constexpr int Q = OpsLayout<N, Real>::SIZE;              // double
+  static constexpr int QR = Q + pad16(NF * E * NP * 8);           // Real copy
+  static constexpr int AUX = QR + (MIXED ? pad16(NF * E * NP * RS) : 0);
+  static constexpr int FLUX = AUX + pad16(NAUX * E * NP * RS);
+  static constexpr int GEO = FLUX + pad16(NF * E * NFPT * RS);
+  static constexpr int FGEO = GEO + pad16(9 * E * RS);
+  static constexpr int SMEM_BYTES = FGEO + pad16(16 * E * RS);
+};
+
+template <int N, int EQ, typename Real, int MODE>
+__global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
+  using T = Tile<N, EQ, Real>;
+  using Ops = OpsLayout<N, Real>;
+  constexpr int NP = T::NP, NFPT = T::NFPT, NF = T::NF, E = T::E;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar;
+  __shared__ int ops_ok;
+
+  const Real* sW = reinterpret_cast<const Real*>(smem + Ops::W);
+  const Real* sL = reinterpret_cast<const Real*>(smem + Ops::L);
+  const int* sFN = reinterpret_cast<const int*>(smem + Ops::FN);
+  double* sQ = reinterpret_cast<double*>(smem + T::Q);
+  Real* sQr = T::MIXED ? reinterpret_cast<Real*>(smem + T::QR)
+                       : reinterpret_cast<Real*>(smem + T::Q);
+  Real* sAux = reinterpret_cast<Real*>(smem + T::AUX);
+  Real* sFlux = reinterpret_cast<Real*>(smem + T::FLUX);
+  Real* sG = reinterpret_cast<Real*>(smem + T::GEO);
+  Real* sFG = reinterpret_cast<Real*>(smem + T::FGEO);
+
+  const int t = threadIdx.x;
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    mbar_arrive_expect_tx(&bar, a.ops_bytes);
+    bulk_g2s(smem, a.ops, a.ops_bytes, &bar);
+    const bool ok = mbar_wait_bounded(&bar, 0);
+    if (!ok) {
+      raise_status(a.status, DG_ERR_TIMEOUT);
+      mbar_wait_bounded(&bar, 0);  // give the copy one more bounded chance
+    }
+    ops_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  if (!ops_ok) return;
+
+  const int el = t / NP;
+  const int i = t - el * NP;
+  const bool active = el < E;
+  const int64_t nel = a.nel;
+  const int64_t nelnp = nel * NP;
+  const int64_t ntiles = (nel + E - 1) / E;
+  const Real p0 = (Real)a.p0, p1 = (Real)a.p1, p2 = (Real)a.p2;
+  const Real half = (Real)0.5, two = (Real)2, zero = (Real)0;
+
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t e0 = tile * E;
+    const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
+
+    // {{{ 1. state and geometry -> shared memory (coalesced)
+    for (int idx = t; idx < NF * E * NP; idx += kBlock) {
+      const int k = idx / (E * NP);
+      const int rem = idx - k * (E * NP);
+      const double v =
+          rem < ecount * NP ? __ldg(a.q + k * nelnp + e0 * NP + rem) : 0.0;
+      sQ[idx] = v;
+      if constexpr (T::MIXED) sQr[idx] = (Real)v;
+    }
+    for (int idx = t; idx < 9 * E; idx += kBlock)
+      sG[idx] = idx < 9 * ecount ? (Real)__ldg(a.metric + e0 * 9 + idx) : zero;
+    for (int idx = t; idx < 16 * E; idx += kBlock)
+      sFG[idx] =
+          idx < 16 * ecount ? (Real)__ldg(a.face_geom + e0 * 16 + idx) : zero;
+    __syncthreads();
+    // }}}
+
+    // {{{ 2. pointwise pre-pass
+    if constexpr (EQ == DG_WAVE) {
+      if (active && el < ecount) {
+        const Real* G = sG + el * 9;
+        const Real v0 = sQr[(1 * E + el) * NP + i];
+        const Real v1 = sQr[(2 * E + el) * NP + i];
+        const Real v2 = sQr[(3 * E + el) * NP + i];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          sAux[(r * E + el) * NP + i] =
+              fma(G[r * 3 + 0], v0, fma(G[r * 3 + 1], v1, G[r * 3 + 2] * v2));
+      }
+    } else if constexpr (EQ == DG_EULER) {
+      if (active && el < ecount) {
+        const Real* G = sG + el * 9;
+        // pressure recovery from total energy in FP64
+        const double rho_d = sQ[(0 * E + el) * NP + i];
+        const double en_d = sQ[(1 * E + el) * NP + i];
+        const double md[3] = {sQ[(2 * E + el) * NP + i], sQ[(3 * E + el) * NP + i],
+                              sQ[(4 * E + el) * NP + i]};
+        const double rinv_d = 1.0 / rho_d;
+        const double p_d =
+            (a.p0 - 1.0) *
+            (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
+        const Real p = (Real)p_d, en = (Real)en_d;
+        const Real m[3] = {(Real)md[0], (Real)md[1], (Real)md[2]};
+        const Real rinv = (Real)rinv_d;
+        const Real u[3] = {m[0] * rinv, m[1] * rinv, m[2] * rinv};
+        Real F[5][3];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          F[0][x] = m[x];
+          F[1][x] = u[x] * (en + p);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) F[2 + c][x] = m[c] * u[x] + (c == x ? p : zero);
+        }
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            sAux[((k * 3 + r) * E + el) * NP + i] =
+                fma(G[r * 3 + 0], F[k][0],
+                    fma(G[r * 3 + 1], F[k][1], G[r * 3 + 2] * F[k][2]));
+      }
+    }
+    if constexpr (T::NAUX > 0) __syncthreads();
+    // }}}
+
+    // {{{ 3. volume term (registers)
+    Real vol[NF];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) vol[k] = zero;
+    if (active && el < ecount) {
+      const Real* G = sG + el * 9;
+      if constexpr (EQ == DG_WAVE) {
+        const Real c = p0;
+        const Real* u = sQr + el * NP;
+        Real ur0 = zero, ur1 = zero, ur2 = zero, dv = zero;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          const Real w0 = sW[(0 * NP + j) * NP + i];
+          const Real w1 = sW[(1 * NP + j) * NP + i];
+          const Real w2 = sW[(2 * NP + j) * NP + i];
+          const Real uj = u[j];
+          ur0 = fma(w0, uj, ur0);
+          ur1 = fma(w1, uj, ur1);
+          ur2 = fma(w2, uj, ur2);
+          dv = fma(w0, sAux[(0 * E + el) * NP + j],
+                   fma(w1, sAux[(1 * E + el) * NP + j],
+                       fma(w2, sAux[(2 * E + el) * NP + j], dv)));
+        }
+        vol[0] = -c * dv;
+#pragma unroll
+        for (int x = 0; x < 3; ++x)
+          vol[1 + x] = -c * fma(G[0 * 3 + x], ur0,
+                                fma(G[1 * 3 + x], ur1, G[2 * 3 + x] * ur2));
+      } else if constexpr (EQ == DG_EULER) {
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          const Real w0 = sW[(0 * NP + j) * NP + i];
+          const Real w1 = sW[(1 * NP + j) * NP + i];
+          const Real w2 = sW[(2 * NP + j) * NP + i];
+#pragma unroll
+          for (int k = 0; k < 5; ++k)
+            vol[k] = fma(w0, sAux[((k * 3 + 0) * E + el) * NP + j],
+                         fma(w1, sAux[((k * 3 + 1) * E + el) * NP + j],
+                             fma(w2, sAux[((k * 3 + 2) * E + el) * NP + j],
+                                 vol[k])));
+        }
+      } else {  // DG_MAXWELL: strong derivatives, curl
+        Real d[6][3];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) d[k][0] = d[k][1] = d[k][2] = zero;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+          const Real w0 = sW[(0 * NP + j) * NP + i];
+          const Real w1 = sW[(1 * NP + j) * NP + i];
+          const Real w2 = sW[(2 * NP + j) * NP + i];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            const Real qj = sQr[(k * E + el) * NP + j];
+            d[k][0] = fma(w0, qj, d[k][0]);
+            d[k][1] = fma(w1, qj, d[k][1]);
+            d[k][2] = fma(w2, qj, d[k][2]);
+          }
+        }
+        // dq_k/dx_x = sum_r G[r][x] d[k][r]
+        auto dx = [&](int k, int x) {
+          return fma(G[0 * 3 + x], d[k][0],
+                     fma(G[1 * 3 + x], d[k][1], G[2 * 3 + x] * d[k][2]));
+        };
+        // E_t = curl H, H_t = -curl E
+        vol[0] = dx(5, 1) - dx(4, 2);
+        vol[1] = dx(3, 2) - dx(5, 0);
+        vol[2] = dx(4, 0) - dx(3, 1);
+        vol[3] = -(dx(2, 1) - dx(1, 2));
+        vol[4] = -(dx(0, 2) - dx(2, 0));
+        vol[5] = -(dx(1, 0) - dx(0, 1));
+      }
+    }
+    // }}}
+
+    // {{{ 4. face gather + numerical flux
+    for (int pidx = t; pidx < ecount * NFPT; pidx += kBlock) {
+      const int elp = pidx / NFPT;
+      const int fj = pidx - elp * NFPT;
+      const int f = fj / Shape<N>::NFP;
+      const int node = sFN[fj];
+      uint32_t g = __ldg(a.gather + (e0 + elp) * NFPT + fj);
+      bool bdry = (g >> 31) != 0u;
+      int64_t gi = (int64_t)(g & 0x7fffffffu);
+      if (gi >= nelnp) {  // never read out of bounds
+        raise_status(a.status, DG_ERR_INDEX);
+        gi = (e0 + elp) * NP + node;
+      }
+      const Real* fg = sFG + (elp * 4 + f) * 4;
+      const Real nx = fg[0], ny = fg[1], nz = fg[2], scale = fg[3];
+      double qid[NF], qed[NF];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) qid[k] = sQ[(k * E + elp) * NP + node];
+      if (!bdry) {
+#pragma unroll
+        for (int k = 0; k < NF; ++k) qed[k] = __ldg(a.q + k * nelnp + gi);
+      }
+      Real* out = sFlux + elp * NFPT + fj;
+      constexpr int FS = E * NFPT;  // field stride in sFlux
+
+      if constexpr (EQ == DG_WAVE) {
+        Real qi[4], qe[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) qi[k] = (Real)qid[k];
+        if (bdry) {  // Dirichlet mirror: exterior (-u, v)
+          qe[0] = -qi[0];
+          qe[1] = qi[1];
+          qe[2] = qi[2];
+          qe[3] = qi[3];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) qe[k] = (Real)qed[k];
+        }
+        const Real c = p0;
+        const Real vavg_n = half * (qi[1] + qe[1]) * nx + half * (qi[2] + qe[2]) * ny +
+                            half * (qi[3] + qe[3]) * nz;
+        const Real uavg = half * (qi[0] + qe[0]);
+        const Real vjump = (qe[1] - qi[1]) * nx + (qe[2] - qi[2]) * ny +
+                           (qe[3] - qi[3]) * nz;
+        const Real fu = c * (vavg_n + half * (qe[0] - qi[0]));
+        const Real fv = c * (uavg + half * vjump);
+        out[0 * FS] = scale * fu;
+        out[1 * FS] = scale * (fv * nx);
+        out[2 * FS] = scale * (fv * ny);
+        out[3 * FS] = scale * (fv * nz);
+      } else if constexpr (EQ == DG_EULER) {
+        if (bdry) {  // InviscidWallBC: mirror the normal momentum (FP64 state)
+          const double ndx = a.face_geom[((e0 + elp) * 4 + f) * 4 + 0];
+          const double ndy = a.face_geom[((e0 + elp) * 4 + f) * 4 + 1];
+          const double ndz = a.face_geom[((e0 + elp) * 4 + f) * 4 + 2];
+          const double mn = qid[2] * ndx + qid[3] * ndy + qid[4] * ndz;
+          qed[0] = qid[0];
+          qed[1] = qid[1];
+          qed[2] = qid[2] - 2.0 * ndx * mn;
+          qed[3] = qid[3] - 2.0 * ndy * mn;
+          qed[4] = qid[4] - 2.0 * ndz * mn;
+        }
+        const Real gamma = p0;
+        Real fn_i[5], fn_e[5], lam_i, lam_e;
+        auto side = [&](const double* qd, Real* fn, Real& lam) {
+          const double rinv_d = 1.0 / qd[0];
+          const double p_d =  // pressure recovery from total energy in FP64
+              (a.p0 - 1.0) *
+              (qd[1] - 0.5 * (qd[2] * qd[2] + qd[3] * qd[3] + qd[4] * qd[4]) * rinv_d);
+          const Real p = (Real)p_d, rinv = (Real)rinv_d;
+          const Real q1 = (Real)qd[1], q2 = (Real)qd[2], q3 = (Real)qd[3],
+                     q4 = (Real)qd[4];
+          const Real ux = q2 * rinv, uy = q3 * rinv, uz = q4 * rinv;
+          const Real un = ux * nx + uy * ny + uz * nz;
+          fn[0] = q2 * nx + q3 * ny + q4 * nz;
+          fn[1] = un * (q1 + p);
+          fn[2] = q2 * un + p * nx;
+          fn[3] = q3 * un + p * ny;
+          fn[4] = q4 * un + p * nz;
+          lam = sqrt(ux * ux + uy * uy + uz * uz) + sqrt(gamma * (p * rinv));
+        };
+        side(qid, fn_i, lam_i);
+        side(qed, fn_e, lam_e);
+        const Real lam = fmax(lam_i, lam_e);
+        const Real nn = nx * nx + ny * ny + nz * nz;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          const Real dq = (Real)(qed[k] - qid[k]);
+          const Real fk = half * (fn_i[k] + fn_e[k]) - half * lam * dq * nn;
+          out[k * FS] = -scale * fk;
+        }
+      } else {  // DG_MAXWELL
+        Real qi[6], qe[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) qi[k] = (Real)qid[k];
+        if (bdry) {  // PEC: exterior (-E, H)
+          qe[0] = -qi[0];
+          qe[1] = -qi[1];
+          qe[2] = -qi[2];
+          qe[3] = qi[3];
+          qe[4] = qi[4];
+          qe[5] = qi[5];
+        } else {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) qe[k] = (Real)qed[k];
+        }
+        const Real alpha = p0, eps = p1, mu = p2;
+        const Real z = sqrt(mu / eps), y = (Real)1 / z;
+        const Real je[3] = {qe[0] - qi[0], qe[1] - qi[1], qe[2] - qi[2]};
+        const Real jh[3] = {qe[3] - qi[3], qe[4] - qi[4], qe[5] - qi[5]};
+        const Real n[3] = {nx, ny, nz};
+        auto cross = [](const Real* a_, const Real* b_, Real* c_) {
+          c_[0] = a_[1] * b_[2] - a_[2] * b_[1];
+          c_[1] = a_[2] * b_[0] - a_[0] * b_[2];
+          c_[2] = a_[0] * b_[1] - a_[1] * b_[0];
+        };
+        Real nxe[3], nxh[3], te[3], th[3], fe[3], fh[3];
+        cross(n, je, nxe);
+        cross(n, jh, nxh);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          te[x] = z * jh[x] - alpha * nxe[x];
+          th[x] = y * je[x] + alpha * nxh[x];
+        }
+        cross(n, te, fe);
+        cross(n, th, fh);
+        const Real ce = (Real)-1 / (z + z), ch = (Real)1 / (y + y);
+#pragma unroll
+        for (int x = 0; x < 3; ++x) {
+          out[x * FS] = -scale * (ce * fe[x]);
+          out[(3 + x) * FS] = -scale * (ch * fh[x]);
+        }
+      }
+    }
+    __syncthreads();
+    // }}}
+
+    // {{{ 5. LIFT, then store or fold into the RK stage
+    if (active && el < ecount) {
+      const Real* fl = sFlux + el * NFPT;
+      const int64_t node_idx = (e0 + el) * NP + i;
+#pragma unroll
+      for (int k = 0; k < NF; ++k) {
+        Real acc = vol[k];
+#pragma unroll 4
+        for (int fj = 0; fj < NFPT; ++fj)
+          acc = fma(sL[fj * NP + i], fl[k * E * NFPT + fj], acc);
+        if constexpr (EQ == DG_MAXWELL) acc = acc / (k < 3 ? p1 : p2);
+        const int64_t gidx = k * nelnp + node_idx;
+        if constexpr (MODE == MODE_RHS) {
+          a.rhs[gidx] = (double)acc;
+        } else {
+          const double r = (a.rk_a != 0.0 ? a.rk_a * a.res[gidx] : 0.0) +
+                           a.rk_dt * (double)acc;
+          a.res[gidx] = r;
+          a.q_out[gidx] = sQ[(k * E + el) * NP + i] + a.rk_b * r;
+        }
+      }
+    }
+    __syncthreads();
+    // }}}
+  }
+}
+
+}  // namespace dg

@@ -1,12 +1,13 @@
-// FP64 RHS kernels for the euler equation, orders 1..4.
+// RHS kernels for the euler equation: orders 1..4, FP64 and mixed
+// precision, plain RHS and fused RK stage.
 #include "rhs_instantiate.cuh"
 
 namespace dg {
-cudaError_t fp64_shape_euler(int order, LaunchShape* out) {
-  return shape_any<DG_EULER>(order, out);
+cudaError_t shape_euler(int order, int precision, int mode, LaunchShape* out) {
+  return shape_any<DG_EULER>(order, precision, mode, out);
 }
-cudaError_t fp64_launch_euler(int order, const RhsArgs& a, int grid,
-                               cudaStream_t s) {
-  return launch_any<DG_EULER>(order, a, grid, s);
+cudaError_t launch_euler(int order, int precision, int mode, const RhsArgs& a,
+                         int grid, cudaStream_t s) {
+  return launch_any<DG_EULER>(order, precision, mode, a, grid, s);
 }
 }  // namespace dg

@@ -1,12 +1,13 @@
-// FP64 RHS kernels for the maxwell equation, orders 1..4.
+// RHS kernels for the maxwell equation: orders 1..4, FP64 and mixed
+// precision, plain RHS and fused RK stage.
 #include "rhs_instantiate.cuh"
 
 namespace dg {
-cudaError_t fp64_shape_maxwell(int order, LaunchShape* out) {
-  return shape_any<DG_MAXWELL>(order, out);
+cudaError_t shape_maxwell(int order, int precision, int mode, LaunchShape* out) {
+  return shape_any<DG_MAXWELL>(order, precision, mode, out);
 }
-cudaError_t fp64_launch_maxwell(int order, const RhsArgs& a, int grid,
-                               cudaStream_t s) {
-  return launch_any<DG_MAXWELL>(order, a, grid, s);
+cudaError_t launch_maxwell(int order, int precision, int mode, const RhsArgs& a,
+                         int grid, cudaStream_t s) {
+  return launch_any<DG_MAXWELL>(order, precision, mode, a, grid, s);
 }
 }  // namespace dg

@@ -214,6 +214,43 @@ def affine_image(disc: DGDiscretization, scale: float,
         neighbor_face=disc.neighbor_face, ext_index=disc.ext_index)
 
 
+def union_discretization(discs: list[DGDiscretization]) -> tuple[DGDiscretization, np.ndarray]:
+    """One discretisation holding independent meshes side by side.
+
+    Elements, geometry and gather indices are concatenated; every member's
+    exterior indices are shifted by its element offset, so no face connects
+    two members.  Returns the union and the element offsets (len + 1)."""
+    if not discs:
+        raise ValueError("need at least one member")
+    order = discs[0].order
+    if any(d.order != order for d in discs):
+        raise ValueError("all members must have the same order")
+    npn = discs[0].np_
+    nels = np.array([d.nelements for d in discs], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(nels)])
+    voffs = np.concatenate([[0], np.cumsum([d.mesh.vertices.shape[0] for d in discs])])
+    mesh = TetMesh(vertices=np.concatenate([d.mesh.vertices for d in discs]),
+                   elements=np.concatenate([d.mesh.elements + voffs[k]
+                                            for k, d in enumerate(discs)]))
+
+    def shifted_neighbor(k, d):
+        nb = d.neighbor.copy()
+        nb[nb >= 0] += offs[k]
+        return nb
+
+    union = DGDiscretization(
+        order=order, ref=discs[0].ref, mesh=mesh,
+        jac=np.concatenate([d.jac for d in discs]),
+        metric=np.concatenate([d.metric for d in discs]),
+        normal=np.concatenate([d.normal for d in discs]),
+        face_jac=np.concatenate([d.face_jac for d in discs]),
+        neighbor=np.concatenate([shifted_neighbor(k, d) for k, d in enumerate(discs)]),
+        neighbor_face=np.concatenate([d.neighbor_face for d in discs]),
+        ext_index=np.concatenate([d.ext_index + offs[k] * npn
+                                  for k, d in enumerate(discs)]))
+    return union, offs
+
+
 _UNIT_BOX_CACHE: dict = {}
 
 

@@ -1,0 +1,75 @@
+"""Batched evaluation of many independent ensemble members.
+
+Members may live on meshes of different sizes.  Their discretisations are
+concatenated into one union (``discretization.union_discretization``), so one
+persistent launch of the RHS kernel covers every member: the kernel's tile
+loop balances uneven members automatically and no member-level control flow
+exists on the device.  The launch can be captured in a CUDA graph and
+replayed once per RHS.
+
+The reference has no ensemble path; this is the batched form asked of the
+GB300 build (64 Maxwell P3 members on boxes with n ~ U[12, 40]).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from actx_dgfem_suite_gb300.discretization import (DGDiscretization,
+                                                   union_discretization)
+from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+
+
+class Ensemble:
+    """``rhs(q)`` for all members at once; ``q`` is (nfields, sum Nel, Np)."""
+
+    def __init__(self, discs: list[DGDiscretization], equation: str, params,
+                 precision: str = "fp32-mixed", device=None):
+        self.union, self.offsets = union_discretization(discs)
+        self.nmembers = len(discs)
+        self.mesh = DeviceMesh(self.union, device)
+        self.plan = DevicePlan(self.mesh, equation, params, precision)
+        self._graph = None
+        self._gq = None
+        self._gout = None
+
+    @property
+    def shape(self):
+        return self.plan.shape
+
+    def member(self, x: torch.Tensor, k: int) -> torch.Tensor:
+        """View of member ``k`` in an ensemble-shaped tensor."""
+        return x[:, int(self.offsets[k]):int(self.offsets[k + 1]), :]
+
+    def stack_states(self, states: list[np.ndarray]) -> torch.Tensor:
+        if len(states) != self.nmembers:
+            raise ValueError("one state per member expected")
+        return torch.from_numpy(np.concatenate(states, axis=1)).to(self.mesh.device)
+
+    def rhs(self, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        return self.plan.rhs(q, out)
+
+    def capture(self, q: torch.Tensor, out: torch.Tensor) -> None:
+        """Capture ``out = L(q)`` as a CUDA graph bound to these tensors."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.plan.rhs(q, out)
+        torch.cuda.current_stream().wait_stream(s)
+        self._graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self._graph):
+            self.plan.rhs(q, out)
+        self._gq, self._gout = q, out
+
+    def replay(self) -> torch.Tensor:
+        if self._graph is None:
+            raise RuntimeError("capture() first")
+        self._graph.replay()
+        return self._gout
+
+
+def random_box_sizes(nmembers: int, lo: int, hi: int, seed: int = 0) -> list[int]:
+    """Elements per axis of each member, uniform in [lo, hi] from ``seed``."""
+    rng = np.random.default_rng(seed)
+    return [int(x) for x in rng.integers(lo, hi + 1, size=nmembers)]

@@ -58,6 +58,8 @@ class DGOperator:
         self.disc = problem.disc
         self.params = problem.params
         self.state_argnum = 0 if self.equation == "wave" else 1
+        #: arithmetic of the compiled plan: "fp64" or "fp32-mixed"
+        self.precision = "fp64"
         self._actx = actx
         self._plans: dict[int, object] = {}
         self._compiled = None
@@ -68,10 +70,11 @@ class DGOperator:
 
     def plan_for(self, actx):
         from actx_dgfem_suite_gb300.plan import DevicePlan
-        key = id(actx)
+        key = (id(actx), self.precision)
         if key not in self._plans:
             self._plans[key] = DevicePlan(actx.device_mesh(self.disc),
-                                          self.equation, self.params)
+                                          self.equation, self.params,
+                                          self.precision)
         return self._plans[key]
 
     def __call__(self, *args):

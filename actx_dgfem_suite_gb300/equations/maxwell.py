@@ -68,14 +68,14 @@ def plane_wave_mix(nodes: np.ndarray, seed: int = 0, nwaves: int = 8) -> np.ndar
 
 
 def maxwell_problem(order: int, nel_1d: int, definition: str = "reference",
-                    epsilon: float = 1.0, mu: float = 1.0) -> Problem:
+                    epsilon: float = 1.0, mu: float = 1.0, seed: int = 0) -> Problem:
     disc = make_box_discretization(order, nel_1d, 0.0, 1.0)
     nodes = disc.nodes()
     if definition == "reference":
         fields = np.real(rectangular_cavity_mode(nodes, 0.0)).copy()
         alpha = 0.5
     elif definition == "baseline":
-        fields = plane_wave_mix(nodes)
+        fields = plane_wave_mix(nodes, seed=seed)
         alpha = 1.0
     else:
         raise ValueError(f"unknown problem definition {definition!r}")

@@ -76,14 +76,25 @@ class DeviceMesh:
                    for t in (self.metric, self.face_geom, self.gather))
 
 
-class DevicePlan:
-    """One compiled RHS: ``rhs(q, out)`` with q, out of shape (nfields, Nel, Np)."""
+PRECISIONS = {"fp64": _lib.DG_FP64, "fp32-mixed": _lib.DG_FP32_MIXED}
 
-    def __init__(self, mesh: DeviceMesh, equation: str, params):
+
+class DevicePlan:
+    """One compiled RHS: ``rhs(q, out)`` with q, out of shape (nfields, Nel, Np).
+
+    ``precision``: ``"fp64"`` (plain path) or ``"fp32-mixed"`` (FP32
+    derivative/flux arithmetic, FP64 state, FP64 Euler pressure recovery and
+    FP64 RK accumulation)."""
+
+    def __init__(self, mesh: DeviceMesh, equation: str, params,
+                 precision: str = "fp64"):
         if equation not in EQUATIONS:
             raise ValueError(f"unknown equation {equation!r}")
+        if precision not in PRECISIONS:
+            raise ValueError(f"unknown precision {precision!r}")
         self.mesh = mesh
         self.equation = equation
+        self.precision = precision
         self.nfields = NFIELDS[equation]
         self.params = tuple(float(p) for p in params)
         L = _lib.lib()
@@ -91,6 +102,7 @@ class DevicePlan:
         parr = (ctypes.c_double * max(1, len(self.params)))(*self.params)
         with torch.cuda.device(mesh.device):
             _lib.check(L.dg_plan_create(ctypes.byref(handle), EQUATIONS[equation],
+                                        PRECISIONS[precision],
                                         ctypes.byref(mesh.desc()), parr,
                                         len(self.params)))
         self._handle = handle
@@ -127,6 +139,17 @@ class DevicePlan:
                                     ctypes.c_void_p(out.data_ptr()),
                                     _stream_handle(stream)))
         return out
+
+    def rk_stage(self, q_in: torch.Tensor, q_out: torch.Tensor,
+                 res: torch.Tensor, a: float, b: float, dt: float,
+                 stream=None) -> None:
+        """res = a res + dt L(q_in); q_out = q_in + b res (one fused launch)."""
+        for x, name in ((q_in, "q_in"), (q_out, "q_out"), (res, "res")):
+            self._check_tensor(x, name)
+        _lib.check(self._lib.dg_rk_stage(
+            self._handle, ctypes.c_void_p(q_in.data_ptr()),
+            ctypes.c_void_p(q_out.data_ptr()), ctypes.c_void_p(res.data_ptr()),
+            float(a), float(b), float(dt), _stream_handle(stream)))
 
     def finish(self, stream=None) -> None:
         _lib.check(self._lib.dg_finish(self._handle, _stream_handle(stream)))

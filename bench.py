@@ -272,6 +272,7 @@ def our_arm(args) -> None:
         n_eff = max(2, n // args.scale)
         rhs, call_args = get_rhs(eq, actx, 3, order, definition="baseline",
                                  nel_1d=n_eff)
+        rhs.dg_operator.precision = args.precision
         compiled = actx.compile(rhs)
         state = call_args[-1]
         q = compiled.stage(state)
@@ -420,8 +421,10 @@ def our_arm(args) -> None:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": K, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
+            "dtype": "f64" if args.precision == "fp64" else "f32 (f64 state)",
+            "data": "synthetic",
             "config": {"workload": WORKLOAD, "problem": "baseline definitions",
+                       "precision": args.precision,
                        "l2": "inputs larger than L2 (every case's state > 129 MB)",
                        "parallelism": f"replicas x{world}",
                        "scale_divisor": args.scale},
@@ -452,6 +455,8 @@ def main(argv=None):
                     help="CPU sample: every case at n // cpu-scale")
     ap.add_argument("--cases", default="", help="subset, e.g. wave3,euler4")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32-mixed"),
+                    help="arithmetic of the timed RHS (the benchmark metric is fp64)")
     args = ap.parse_args(argv)
     if args.impl == "reference":
         reference_arm(args)

@@ -42,6 +42,13 @@ enum dg_status {
 
 enum dg_equation { DG_WAVE = 0, DG_EULER = 1, DG_MAXWELL = 2 };
 
+/* Arithmetic of a plan.  DG_FP64: every operation in FP64 (the plain path).
+ * DG_FP32_MIXED: derivative, flux and LIFT arithmetic in FP32 with FP32
+ * operators and geometry, while the state stays FP64 in memory, the Euler
+ * pressure is recovered from total energy in FP64, and RK stage updates
+ * accumulate in FP64. */
+enum dg_precision { DG_FP64 = 0, DG_FP32_MIXED = 1 };
+
 typedef struct dg_plan dg_plan;
 
 typedef struct dg_mesh_desc {
@@ -57,20 +64,31 @@ typedef struct dg_mesh_desc {
 } dg_mesh_desc;
 
 /* Build a plan: validate the description, stage the reference operators in
- * device memory and size the persistent launch.
+ * device memory (in the plan's precision) and size the persistent launch.
  * params: wave {c}; euler {gamma}; maxwell {alpha, epsilon, mu}.
  * Replaces the compile step of the reference's array contexts:
  * actx.compile(rhs) (actx_dgfem_suite/run/__main__.py:74) and the DAG/loopy
  * pipeline behind it (actx_dgfem_suite/arraycontext/dgfem_optimizer.py:182-245). */
-int dg_plan_create(dg_plan** plan, int32_t equation, const dg_mesh_desc* mesh,
-                   const double* params, int32_t nparams);
+int dg_plan_create(dg_plan** plan, int32_t equation, int32_t precision,
+                   const dg_mesh_desc* mesh, const double* params,
+                   int32_t nparams);
 
-/* One RHS evaluation, FP64: rhs = L(q).  Enqueued on `stream` (a cudaStream_t,
+/* One RHS evaluation: rhs = L(q), state and result FP64.  Enqueued on `stream` (a cudaStream_t,
  * NULL = legacy default stream); returns without synchronising.
  * q and rhs are device arrays of nfields * Nel * Np doubles and must not overlap.
  * Replaces the call of the compiled RHS, compiled_rhs(*args)
  * (actx_dgfem_suite/run/__main__.py:76,109,126). */
 int dg_rhs(dg_plan* plan, const double* q, double* rhs, void* stream);
+
+/* One stage of a low-storage Runge-Kutta method fused into the RHS kernel:
+ *   res   = a * res + dt * L(q_in)      (res is not read when a == 0)
+ *   q_out = q_in + b * res
+ * All three arrays are device (nfields, Nel, Np) FP64 and must not overlap;
+ * q_out must differ from q_in because other elements still read q_in's face
+ * values during the stage.  The reference evaluates the RHS only; its RK hook
+ * is estimate_rk4_timestep (actx_dgfem_suite/equations/wave.py:206-213). */
+int dg_rk_stage(dg_plan* plan, const double* q_in, double* q_out, double* res,
+                double a, double b, double dt, void* stream);
 
 /* Block until `stream` has drained, then report any device-side error flag
  * the plan's kernels raised (DG_ERR_INDEX, DG_ERR_TIMEOUT) and clear it.

@@ -35,7 +35,7 @@ def test_library_exports_all_declared_symbols():
 
 def test_version_and_error_strings():
     L = _lib.lib()
-    assert L.dg_abi_version() == 1
+    assert L.dg_abi_version() == 2
     assert isinstance(L.dg_last_error(), bytes)
 
 
@@ -43,15 +43,19 @@ def test_argument_errors_without_device():
     L = _lib.lib()
     h = ctypes.c_void_p()
     # NULL mesh description -> DG_ERR_ARGUMENT, no CUDA call made
-    assert L.dg_plan_create(ctypes.byref(h), 0, None, None, 0) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_plan_create(ctypes.byref(h), 0, 0, None, None, 0) == _lib.DG_ERR_ARGUMENT
     assert b"NULL" in L.dg_last_error()
     d = _lib.MeshDesc()
     d.order = 7
     d.nelements = 10
-    assert L.dg_plan_create(ctypes.byref(h), 0, ctypes.byref(d), None, 0) \
+    assert L.dg_plan_create(ctypes.byref(h), 0, 0, ctypes.byref(d), None, 0) \
         == _lib.DG_ERR_UNSUPPORTED
+    assert L.dg_plan_create(ctypes.byref(h), 0, 7, ctypes.byref(d), None, 0) \
+        == _lib.DG_ERR_ARGUMENT
     d.order = 2
-    assert L.dg_plan_create(ctypes.byref(h), 9, ctypes.byref(d), None, 0) \
+    assert L.dg_plan_create(ctypes.byref(h), 9, 0, ctypes.byref(d), None, 0) \
+        == _lib.DG_ERR_ARGUMENT
+    assert L.dg_rk_stage(None, None, None, None, 0.0, 0.0, 0.0, None) \
         == _lib.DG_ERR_ARGUMENT
     assert L.dg_rhs(None, None, None, None) == _lib.DG_ERR_ARGUMENT
     assert L.dg_finish(None, None) == _lib.DG_ERR_ARGUMENT

@@ -86,3 +86,19 @@ def test_nonmanifold_mesh_rejected():
     m = TetMesh(v, el)
     with pytest.raises(ValueError):
         make_discretization(m, 1)
+
+
+def test_union_discretization_offsets():
+    from actx_dgfem_suite_gb300.discretization import union_discretization
+    a = make_box_discretization(2, 2)
+    b = make_box_discretization(2, 3, 0.0, 2.0)
+    u, offs = union_discretization([a, b])
+    assert list(offs) == [a.nelements, a.nelements + b.nelements][:0] + [0, a.nelements, a.nelements + b.nelements]
+    assert u.nelements == a.nelements + b.nelements
+    # member b's exterior indices point into member b only
+    eb = u.ext_index[a.nelements:]
+    assert eb.min() >= a.nelements * u.np_
+    assert np.array_equal(u.ext_index[:a.nelements], a.ext_index)
+    x = u.nodes().reshape(3, -1)
+    own = np.arange(u.nelements)[:, None, None] * u.np_ + u.ref.face_nodes[None]
+    assert np.abs(x[:, u.ext_index] - x[:, own]).max() < 1e-14
