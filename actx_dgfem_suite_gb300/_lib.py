@@ -28,7 +28,8 @@ DG_FP32_MIXED = 1
 
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
-                    "dg_plan_destroy",
+                    "dg_plan_destroy", "dg_plan_set_element_scale",
+                    "dg_rhs_adjoint",
                     "dg_plan_info", "dg_fp64_fma_probe", "dg_last_error",
                     "dg_abi_version")
 
@@ -50,6 +51,7 @@ class MeshDesc(ctypes.Structure):
         ("strong_diff", ctypes.c_void_p),
         ("lift", ctypes.c_void_p),
         ("face_nodes", ctypes.c_void_p),
+        ("face_partner", ctypes.c_void_p),
     ]
 
 
@@ -82,8 +84,12 @@ def lib() -> ctypes.CDLL:
     L.dg_rhs.argtypes = [vp, vp, vp, vp]
     L.dg_rhs.restype = ctypes.c_int
     dbl = ctypes.c_double
-    L.dg_rk_stage.argtypes = [vp, vp, vp, vp, dbl, dbl, dbl, vp]
+    L.dg_rk_stage.argtypes = [vp, vp, vp, vp, dbl, dbl, dbl, vp, vp]
     L.dg_rk_stage.restype = ctypes.c_int
+    L.dg_plan_set_element_scale.argtypes = [vp, vp]
+    L.dg_plan_set_element_scale.restype = ctypes.c_int
+    L.dg_rhs_adjoint.argtypes = [vp, vp, vp, vp, vp]
+    L.dg_rhs_adjoint.restype = ctypes.c_int
     L.dg_finish.argtypes = [vp, vp]
     L.dg_finish.restype = ctypes.c_int
     L.dg_plan_destroy.argtypes = [vp]

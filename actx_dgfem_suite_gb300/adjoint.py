@@ -1,0 +1,209 @@
+"""Gradients of a receiver misfit through the wave time integration.
+
+Forward model: the suite's wave operator (``actx_dgfem_suite/equations/wave.py:121-200``)
+with a per-element wave speed, ``dq/dt = diag(c_e) L q`` (the operator is linear
+in c, so a per-element speed is a per-element factor on the RHS), integrated
+with LSRK(5,4) in fused stage launches; receivers sample ``u`` after every
+step.  The gradient of any loss of the receiver traces with respect to the
+initial state and to ``c_e`` is the discrete adjoint of those steps:
+
+* the operator transpose ``L^T`` is the hand-written adjoint kernel
+  (``dg_rhs_adjoint``: transposed D and LIFT, face-gather transpose as a
+  deterministic gather over glued face points);
+* the reverse of one LSRK step needs only the stage residuals of the forward
+  step (the c-gradient term ``<rbar, L q>`` uses ``L q^{s-1} =
+  (r^s - a_s r^{s-1}) / (dt c_e)``), so the reverse sweep recomputes them
+  segment by segment from checkpoints.
+
+Checkpointing: states are stored every ``k`` steps in the forward sweep; the
+reverse sweep replays one segment at a time, keeping its 5 k residuals.
+Memory is ``N/k + 5k`` states, minimal at ``k = sqrt(N / 5)`` (square-root
+scaling); each forward step is recomputed exactly once.
+
+:class:`WaveMisfitFunction` wraps this as a ``torch.autograd.Function``.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from actx_dgfem_suite_gb300.discretization import DGDiscretization
+from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+from actx_dgfem_suite_gb300.refelem import BIUNIT_TET_VERTICES, pkdo_tet
+from actx_dgfem_suite_gb300.timestepping import RK4A, RK4B
+
+
+# {{{ receivers
+
+
+def locate_points(disc: DGDiscretization, points: np.ndarray, tol: float = 1e-10):
+    """Element index and reference coordinates of each point (brute force
+    over elements, vectorised; for test- and benchmark-sized point sets)."""
+    ev = disc.mesh.vertices[disc.mesh.elements]              # (Nel, 4, 3)
+    jm = np.stack([ev[:, 1] - ev[:, 0], ev[:, 2] - ev[:, 0], ev[:, 3] - ev[:, 0]],
+                  axis=2)                                    # (Nel, x, k)
+    jinv = np.linalg.inv(jm)
+    elems = np.empty(len(points), dtype=np.int64)
+    bary = np.empty((len(points), 4))
+    for p, x in enumerate(points):
+        lam = np.einsum("ekx,ex->ek", jinv, x[None, :] - ev[:, 0])  # (Nel, 3)
+        l0 = 1.0 - lam.sum(axis=1)
+        inside = np.all(lam >= -tol, axis=1) & (l0 >= -tol)
+        cand = np.nonzero(inside)[0]
+        if cand.size == 0:
+            raise ValueError(f"point {x} is outside the mesh")
+        e = cand[0]
+        elems[p] = e
+        bary[p] = np.concatenate([[l0[e]], lam[e]])
+    ref = bary @ BIUNIT_TET_VERTICES
+    return elems, ref
+
+
+class Receivers:
+    """Point samples of the first field: ``trace = sum_i w_i u[e, i]``."""
+
+    def __init__(self, disc: DGDiscretization, points: np.ndarray, device):
+        elems, ref = locate_points(disc, np.asarray(points, dtype=np.float64))
+        vinv = np.linalg.inv(disc.ref.vdm)
+        w = pkdo_tet(disc.order, ref) @ vinv                 # (R, Np)
+        self.npoints = len(points)
+        self.elems = torch.from_numpy(elems).to(device)
+        self.weights = torch.from_numpy(w).to(device)
+        # deterministic adjoint injection: one row per distinct element
+        uniq, inv = np.unique(elems, return_inverse=True)
+        self.uelems = torch.from_numpy(uniq).to(device)
+        inc = np.zeros((len(uniq), len(points)))
+        inc[inv, np.arange(len(points))] = 1.0
+        self.incidence = torch.from_numpy(inc).to(device)
+
+    def sample(self, q: torch.Tensor) -> torch.Tensor:
+        """(R,) values of field 0 of ``q`` (nfields, Nel, Np)."""
+        return (q[0, self.elems, :] * self.weights).sum(dim=1)
+
+    def inject(self, lam: torch.Tensor, g: torch.Tensor) -> None:
+        """``lam[0] += R^T g`` without atomics."""
+        contrib = self.incidence @ (g[:, None] * self.weights)   # (U, Np)
+        lam[0, self.uelems, :] += contrib
+
+
+def random_interior_points(n: int, lo, hi, margin: float, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    lo = np.asarray(lo, dtype=np.float64) + margin
+    hi = np.asarray(hi, dtype=np.float64) - margin
+    return lo + (hi - lo) * rng.random((n, 3))
+
+
+# }}}
+
+
+class WaveAdjointSolver:
+    """Forward traces and their adjoint for one mesh, time step and step count."""
+
+    def __init__(self, disc: DGDiscretization, dt: float, nsteps: int,
+                 receivers: Receivers, device=None, segment: int | None = None):
+        self.mesh = DeviceMesh(disc, device, with_partner=True)
+        self.device = self.mesh.device
+        self.plan = DevicePlan(self.mesh, "wave", (1.0,), "fp64")
+        self.dt = float(dt)
+        self.nsteps = int(nsteps)
+        self.rec = receivers
+        self.segment = segment or max(1, int(round(math.sqrt(self.nsteps / 5.0))))
+        shape = self.plan.shape
+        self._buf = torch.empty(shape, dtype=torch.float64, device=self.device)
+        self._res = torch.zeros(shape, dtype=torch.float64, device=self.device)
+        self.stats = {}
+
+    # {{{ forward
+
+    def _step(self, q: torch.Tensor, record: list | None = None) -> None:
+        src, dst = q, self._buf
+        for s in range(5):
+            self.plan.rk_stage(src, dst, self._res, RK4A[s], RK4B[s], self.dt)
+            if record is not None:
+                record.append(self._res.clone())
+            src, dst = dst, src
+        q.copy_(src)
+
+    def forward(self, q0: torch.Tensor, c: torch.Tensor):
+        """Traces (nsteps, R) and the checkpoints of the reverse sweep."""
+        self.plan.set_element_scale(c)
+        q = q0.clone()
+        ckpts = {0: q0.clone()}
+        traces = torch.empty((self.nsteps, self.rec.npoints), dtype=torch.float64,
+                             device=self.device)
+        for n in range(self.nsteps):
+            self._step(q)
+            traces[n] = self.rec.sample(q)
+            if (n + 1) % self.segment == 0 and n + 1 < self.nsteps:
+                ckpts[n + 1] = q.clone()
+        return traces, ckpts
+
+    # }}}
+
+    # {{{ reverse
+
+    def _adjoint_step(self, lam: torch.Tensor, residuals: list, c: torch.Tensor,
+                      cbar: torch.Tensor) -> None:
+        """lam <- Phi_q^T lam; cbar += Phi_c^T lam for one forward step whose
+        stage residuals r^1..r^5 are ``residuals``."""
+        dt = self.dt
+        rbar = torch.zeros_like(lam)
+        y = torch.empty_like(lam)
+        inv_dtc = (1.0 / (dt * c))[None, :, None]
+        for s in range(4, -1, -1):
+            rbar.add_(lam, alpha=RK4B[s])
+            self.plan.adjoint(rbar, y)
+            prev = residuals[s - 1] if s > 0 else None
+            lq = residuals[s] if prev is None else residuals[s] - RK4A[s] * prev
+            cbar.add_((rbar * lq * inv_dtc).sum(dim=(0, 2)), alpha=dt)
+            lam.add_(y, alpha=dt)
+            rbar.mul_(RK4A[s])
+
+    def backward(self, grad_traces: torch.Tensor, ckpts: dict, c: torch.Tensor):
+        """(dJ/dq0, dJ/dc) for dJ/dtraces = ``grad_traces``."""
+        self.plan.set_element_scale(c)
+        lam = torch.zeros(self.plan.shape, dtype=torch.float64, device=self.device)
+        cbar = torch.zeros_like(c)
+        starts = sorted(ckpts)
+        for seg_start in reversed(starts):
+            seg_end = min(self.nsteps, seg_start + self.segment)
+            q = ckpts[seg_start].clone()
+            records = []
+            for _ in range(seg_start, seg_end):
+                rec: list = []
+                self._step(q, rec)
+                records.append(rec)
+            for n in range(seg_end - 1, seg_start - 1, -1):
+                # trace n was sampled after step n, i.e. from q_{n+1}
+                self.rec.inject(lam, grad_traces[n])
+                self._adjoint_step(lam, records[n - seg_start], c, cbar)
+        return lam, cbar
+
+    # }}}
+
+
+class WaveMisfitFunction(torch.autograd.Function):
+    """``traces = F(q0, c)`` with the hand-written adjoint as its backward.
+
+    ``q0``: (4, Nel, Np) initial state; ``c``: (Nel,) element wave speeds; the
+    third argument is a :class:`WaveAdjointSolver`."""
+
+    @staticmethod
+    def forward(ctx, q0, c, solver: WaveAdjointSolver):
+        traces, ckpts = solver.forward(q0.detach().contiguous(),
+                                       c.detach().contiguous())
+        ctx.solver = solver
+        ctx.ckpts = ckpts
+        ctx.save_for_backward(c)
+        return traces
+
+    @staticmethod
+    def backward(ctx, grad_traces):
+        (c,) = ctx.saved_tensors
+        dq0, dc = ctx.solver.backward(grad_traces.contiguous(), ctx.ckpts,
+                                      c.contiguous())
+        ctx.ckpts = None
+        return dq0, dc, None

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/dgfem_gb300.h"
+#include "dg_adjoint.cuh"  // AdjArgs, AdjOpsLayout
 #include "dg_launch.h"
 #include "dg_rhs.cuh"  // RhsArgs, kBlock
 
@@ -94,6 +95,13 @@ struct dg_plan {
   int grid = 0;
   dg::LaunchShape shape;
   int device = 0;
+  int nsm = 0;
+  const double* elem_scale = nullptr;
+  // adjoint (wave, FP64, when the mesh carries face_partner)
+  const int32_t* face_partner = nullptr;
+  void* d_adj_ops = nullptr;
+  uint32_t adj_ops_bytes = 0;
+  int adj_grid = 0;
 };
 
 namespace {
@@ -111,7 +119,21 @@ dg::RhsArgs base_args(const dg_plan* p) {
   a.p0 = p->params[0];
   a.p1 = p->params[1];
   a.p2 = p->params[2];
+  a.elem_scale = p->elem_scale;
   return a;
+}
+
+// Adjoint operator block: W in [r][i][j] (the forward layout of W^T), LIFT in
+// [i][fj], face nodes.
+void pack_adj_ops(std::vector<unsigned char>& buf, int np, int nfp,
+                  const double* diff, const double* lift,
+                  const int32_t* face_nodes, int w_off, int l_off, int fn_off) {
+  double* w = reinterpret_cast<double*>(buf.data() + w_off);
+  double* l = reinterpret_cast<double*>(buf.data() + l_off);
+  int32_t* fn = reinterpret_cast<int32_t*>(buf.data() + fn_off);
+  for (int k = 0; k < 3 * np * np; ++k) w[k] = diff[k];
+  for (int k = 0; k < np * 4 * nfp; ++k) l[k] = lift[k];
+  for (int k = 0; k < 4 * nfp; ++k) fn[k] = face_nodes[k];
 }
 
 template <typename Real>
@@ -229,11 +251,99 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   }
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+  p->nsm = nsm;
   const int64_t ntiles =
       (p->nel + shape.elems_per_tile - 1) / shape.elems_per_tile;
   const int64_t full = (int64_t)nsm * shape.blocks_per_sm;
   p->grid = (int)(ntiles < full ? ntiles : full);
+
+  if (mesh->face_partner && equation == DG_WAVE && precision == DG_FP64) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, mesh->face_partner) != cudaSuccess ||
+        attr.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      dg_plan_destroy(p);
+      return fail(DG_ERR_ARGUMENT, "face_partner must be device memory");
+    }
+    dg::LaunchShape ashape;
+    err = dg::adjoint_shape_wave(N, &ashape);
+    if (err != cudaSuccess || ashape.blocks_per_sm < 1) {
+      dg_plan_destroy(p);
+      return err != cudaSuccess ? cuda_fail(err, "adjoint configuration")
+                                : fail(DG_ERR_UNSUPPORTED, "adjoint does not fit");
+    }
+    const int w_off = 0;
+    const int l_off = dg::pad16_host(3 * np * np * 8);
+    const int fn_off = l_off + dg::pad16_host(4 * nfp * np * 8);
+    const int size = fn_off + dg::pad16_host(4 * nfp * 4);
+    if (size != ashape.ops_bytes) {
+      dg_plan_destroy(p);
+      return fail(DG_ERR_CUDA, "adjoint operator layout mismatch");
+    }
+    std::vector<unsigned char> aops(size, 0);
+    pack_adj_ops(aops, np, nfp, diff, mesh->lift, mesh->face_nodes, w_off, l_off,
+                 fn_off);
+    err = cudaMalloc(&p->d_adj_ops, size);
+    if (err == cudaSuccess)
+      err = cudaMemcpy(p->d_adj_ops, aops.data(), size, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+      dg_plan_destroy(p);
+      return cuda_fail(err, "adjoint buffers");
+    }
+    p->face_partner = mesh->face_partner;
+    p->adj_ops_bytes = static_cast<uint32_t>(size);
+    const int64_t atiles = (p->nel + ashape.elems_per_tile - 1) / ashape.elems_per_tile;
+    const int64_t afull = (int64_t)nsm * ashape.blocks_per_sm;
+    p->adj_grid = (int)(atiles < afull ? atiles : afull);
+  }
   *plan_out = p;
+  return DG_OK;
+}
+
+int dg_plan_set_element_scale(dg_plan* p, const double* scale) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (scale) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, scale) != cudaSuccess ||
+        attr.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      return fail(DG_ERR_ARGUMENT, "element scale must be device memory");
+    }
+  }
+  p->elem_scale = scale;
+  return DG_OK;
+}
+
+int dg_rhs_adjoint(dg_plan* p, const double* x, double* y, double* face_scratch,
+                   void* stream) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!p->d_adj_ops)
+    return fail(DG_ERR_UNSUPPORTED,
+                "adjoint needs an FP64 wave plan built with face_partner");
+  if (!x || !y || !face_scratch)
+    return fail(DG_ERR_ARGUMENT, "x, y or face_scratch is NULL");
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  const int64_t sbytes = p->nel * 2 * 4 * (int64_t)p->nfp * 8;
+  if (overlap(x, y, bytes) || overlap(x, face_scratch, bytes > sbytes ? bytes : sbytes) ||
+      overlap(y, face_scratch, bytes > sbytes ? bytes : sbytes))
+    return fail(DG_ERR_ARGUMENT, "x, y and face_scratch must not overlap");
+  dg::AdjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.x = x;
+  a.y = y;
+  a.face_scratch = face_scratch;
+  a.elem_scale = p->elem_scale;
+  a.c = p->params[0];
+  a.metric = p->metric;
+  a.face_geom = p->face_geom;
+  a.face_partner = p->face_partner;
+  a.ops = p->d_adj_ops;
+  a.ops_bytes = p->adj_ops_bytes;
+  a.nel = p->nel;
+  a.status = p->d_status;
+  cudaError_t err = dg::adjoint_launch_wave(p->order, a, p->adj_grid, p->nsm,
+                                            reinterpret_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return cuda_fail(err, "adjoint launch");
   return DG_OK;
 }
 
@@ -252,7 +362,8 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
 }
 
 int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
-                double a_coef, double b_coef, double dt, void* stream) {
+                double a_coef, double b_coef, double dt, double* rhs_unscaled,
+                void* stream) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (!q_in || !q_out || !res)
     return fail(DG_ERR_ARGUMENT, "state, output or residual pointer is NULL");
@@ -267,6 +378,12 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
   a.rk_a = a_coef;
   a.rk_b = b_coef;
   a.rk_dt = dt;
+  if (rhs_unscaled) {
+    if (overlap(rhs_unscaled, q_in, bytes) || overlap(rhs_unscaled, q_out, bytes) ||
+        overlap(rhs_unscaled, res, bytes))
+      return fail(DG_ERR_ARGUMENT, "rhs_unscaled overlaps another array");
+    a.rhs_unscaled = rhs_unscaled;
+  }
   cudaError_t err = launch_of(p->equation, p->order, p->precision, 1, a, p->grid,
                               reinterpret_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
@@ -294,6 +411,7 @@ int dg_plan_destroy(dg_plan* p) {
   int code = DG_OK;
   if (p->d_ops && cudaFree(p->d_ops) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_status && cudaFree(p->d_status) != cudaSuccess) code = DG_ERR_CUDA;
+  if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
   return DG_OK;

@@ -9,6 +9,7 @@
 namespace dg {
 
 struct RhsArgs;
+struct AdjArgs;
 
 struct LaunchShape {
   int smem_bytes = 0;      // dynamic shared memory per CTA
@@ -46,5 +47,12 @@ DG_DECLARE_EQ(wave)
 DG_DECLARE_EQ(euler)
 DG_DECLARE_EQ(maxwell)
 #undef DG_DECLARE_EQ
+
+// Adjoint of the FP64 wave RHS: shape of the volume kernel, and the two
+// launches (volume transpose + lifted face adjoints, then the per-node
+// transposed flux/gather); `nsm` caps the second grid.
+cudaError_t adjoint_shape_wave(int order, LaunchShape* out);
+cudaError_t adjoint_launch_wave(int order, const AdjArgs& a, int grid, int nsm,
+                                cudaStream_t s);
 
 }  // namespace dg

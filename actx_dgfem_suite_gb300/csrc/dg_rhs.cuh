@@ -21,7 +21,8 @@
 //      actx_dgfem_suite/arraycontext/constants_folder.py:69-100);
 //   5. LIFT ``jfi,fe,fej->ei`` (mass_inverse_fuser.py:21-38 after the
 //      transpose of transpose_consts_in_einsums.py:5-35) added to the volume
-//      term, then either stored (MODE_RHS) or folded into a low-storage
+//      term, optionally multiplied by a per-element factor (variable wave
+//      speed), then either stored (MODE_RHS) or folded into a low-storage
 //      Runge-Kutta stage (MODE_STAGE): res = a res + dt L(q), q_out = q + b res.
 //
 // ``Real`` is the arithmetic type of steps 2-5.  double: the plain FP64 path.
@@ -49,6 +50,8 @@ struct RhsArgs {
   double* q_out;           // MODE_STAGE outputs
   double* res;
   double rk_a, rk_b, rk_dt;
+  const double* elem_scale;  // (Nel) per-element factor on the RHS, or NULL
+  double* rhs_unscaled;      // MODE_STAGE: L(q) before elem_scale, or NULL
   const double* metric;
   const double* face_geom;
   const uint32_t* gather;
@@ -447,11 +450,15 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           acc = fma(sL[fj * NP + i], fl[k * E * NFPT + fj], acc);
         if constexpr (EQ == DG_MAXWELL) acc = acc / (k < 3 ? p1 : p2);
         const int64_t gidx = k * nelnp + node_idx;
+        double val = (double)acc;
+        if constexpr (MODE == MODE_STAGE)
+          if (a.rhs_unscaled) a.rhs_unscaled[gidx] = val;
+        if (a.elem_scale) val *= __ldg(a.elem_scale + e0 + el);
         if constexpr (MODE == MODE_RHS) {
-          a.rhs[gidx] = (double)acc;
+          a.rhs[gidx] = val;
         } else {
-          const double r = (a.rk_a != 0.0 ? a.rk_a * a.res[gidx] : 0.0) +
-                           a.rk_dt * (double)acc;
+          const double r =
+              (a.rk_a != 0.0 ? a.rk_a * a.res[gidx] : 0.0) + a.rk_dt * val;
           a.res[gidx] = r;
           a.q_out[gidx] = sQ[(k * E + el) * NP + i] + a.rk_b * r;
         }

@@ -53,6 +53,7 @@ class DGDiscretization:
     neighbor: np.ndarray        # (Nel, 4) neighbour element, -1 on the boundary
     neighbor_face: np.ndarray   # (Nel, 4) neighbour's local face, -1 on the boundary
     ext_index: np.ndarray       # (Nel, 4, Nfp) int64 flat exterior node index
+    perm_id: np.ndarray | None = None  # (Nel, 4) gluing permutation id, -1 on the boundary
     _cache: dict = field(default_factory=dict, repr=False)
 
     @property
@@ -91,6 +92,25 @@ class DGDiscretization:
         out[:, :, :3] = self.normal
         out[:, :, 3] = self.face_jac / self.jac[:, None]
         return out
+
+    def face_partner(self) -> np.ndarray:
+        """(Nel, 4, Nfp) int32 flat face-point index (e' * 4 + f') * Nfp + j'
+        of the face point glued to each face point, -1 on the boundary.  The
+        adjoint uses it to turn the transpose of the face gather into a
+        gather (deterministic, no atomics)."""
+        if self.perm_id is None:
+            raise ValueError("discretisation was built without gluing permutations")
+        nfp = self.nfp
+        perm_maps = np.stack([self.ref.face_perm[p] for p in _PERMS])  # (6, Nfp)
+        out = np.full((self.nelements, NFACES, nfp), -1, dtype=np.int64)
+        inter = self.neighbor >= 0
+        nb = self.neighbor[inter]
+        nf = self.neighbor_face[inter]
+        pm = perm_maps[self.perm_id[inter]]
+        out[inter] = (nb * NFACES + nf)[:, None] * nfp + pm
+        if out.max() >= (1 << 31):
+            raise ValueError("mesh too large for 31-bit face-point indices")
+        return out.astype(np.int32)
 
     def gather_index(self) -> np.ndarray:
         """(Nel, 4, Nfp) uint32 flat exterior node index, bit 31 set on
@@ -195,7 +215,8 @@ def make_discretization(mesh: TetMesh, order: int) -> DGDiscretization:
         normal=normal, face_jac=face_jac,
         neighbor=neighbor.reshape(nel, NFACES),
         neighbor_face=neighbor_face.reshape(nel, NFACES),
-        ext_index=ext.reshape(nel, NFACES, nfp))
+        ext_index=ext.reshape(nel, NFACES, nfp),
+        perm_id=perm_id.reshape(nel, NFACES))
 
 
 def affine_image(disc: DGDiscretization, scale: float,
@@ -211,7 +232,8 @@ def affine_image(disc: DGDiscretization, scale: float,
         order=disc.order, ref=disc.ref, mesh=mesh, jac=disc.jac * scale**3,
         metric=disc.metric / scale, normal=disc.normal,
         face_jac=disc.face_jac * scale**2, neighbor=disc.neighbor,
-        neighbor_face=disc.neighbor_face, ext_index=disc.ext_index)
+        neighbor_face=disc.neighbor_face, ext_index=disc.ext_index,
+        perm_id=disc.perm_id)
 
 
 def union_discretization(discs: list[DGDiscretization]) -> tuple[DGDiscretization, np.ndarray]:
@@ -247,7 +269,9 @@ def union_discretization(discs: list[DGDiscretization]) -> tuple[DGDiscretizatio
         neighbor=np.concatenate([shifted_neighbor(k, d) for k, d in enumerate(discs)]),
         neighbor_face=np.concatenate([d.neighbor_face for d in discs]),
         ext_index=np.concatenate([d.ext_index + offs[k] * npn
-                                  for k, d in enumerate(discs)]))
+                                  for k, d in enumerate(discs)]),
+        perm_id=(None if any(d.perm_id is None for d in discs)
+                 else np.concatenate([d.perm_id for d in discs])))
     return union, offs
 
 

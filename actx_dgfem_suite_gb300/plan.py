@@ -31,7 +31,8 @@ class DeviceMesh:
     """Geometry, gather index and reference operators of one discretisation,
     uploaded once."""
 
-    def __init__(self, disc: DGDiscretization, device=None):
+    def __init__(self, disc: DGDiscretization, device=None,
+                 with_partner: bool = False):
         if not torch.cuda.is_available():
             raise RuntimeError("DeviceMesh needs a CUDA device")
         self.disc = disc
@@ -44,6 +45,9 @@ class DeviceMesh:
             np.ascontiguousarray(disc.face_geometry())).to(self.device)
         self.gather = torch.from_numpy(
             disc.gather_index().view(np.int32)).to(self.device)
+        # glued face-point index, needed only by the adjoint
+        self.partner = (torch.from_numpy(disc.face_partner()).to(self.device)
+                        if with_partner else None)
         ref = disc.ref
         self._weak = np.ascontiguousarray(ref.weak_diff, dtype=np.float64)
         self._strong = np.ascontiguousarray(ref.diff, dtype=np.float64)
@@ -69,6 +73,7 @@ class DeviceMesh:
         d.strong_diff = self._strong.ctypes.data
         d.lift = self._lift.ctypes.data
         d.face_nodes = self._fnodes.ctypes.data
+        d.face_partner = self.partner.data_ptr() if self.partner is not None else None
         return d
 
     def nbytes(self) -> int:
@@ -142,14 +147,52 @@ class DevicePlan:
 
     def rk_stage(self, q_in: torch.Tensor, q_out: torch.Tensor,
                  res: torch.Tensor, a: float, b: float, dt: float,
-                 stream=None) -> None:
-        """res = a res + dt L(q_in); q_out = q_in + b res (one fused launch)."""
+                 rhs_unscaled: torch.Tensor | None = None, stream=None) -> None:
+        """res = a res + dt L(q_in); q_out = q_in + b res (one fused launch).
+        ``rhs_unscaled`` optionally receives L(q_in) before the element scale."""
         for x, name in ((q_in, "q_in"), (q_out, "q_out"), (res, "res")):
             self._check_tensor(x, name)
+        rptr = None
+        if rhs_unscaled is not None:
+            self._check_tensor(rhs_unscaled, "rhs_unscaled")
+            rptr = ctypes.c_void_p(rhs_unscaled.data_ptr())
         _lib.check(self._lib.dg_rk_stage(
             self._handle, ctypes.c_void_p(q_in.data_ptr()),
             ctypes.c_void_p(q_out.data_ptr()), ctypes.c_void_p(res.data_ptr()),
-            float(a), float(b), float(dt), _stream_handle(stream)))
+            float(a), float(b), float(dt), rptr, _stream_handle(stream)))
+
+    def set_element_scale(self, scale: torch.Tensor | None) -> None:
+        """Multiply each element's RHS by ``scale[e]`` (kept referenced)."""
+        if scale is not None:
+            if (scale.dtype != torch.float64 or scale.device != self.mesh.device
+                    or tuple(scale.shape) != (self.mesh.nelements,)
+                    or not scale.is_contiguous()):
+                raise ValueError("scale must be a contiguous float64 (Nel,) "
+                                 "tensor on the plan's device")
+        self._scale = scale
+        _lib.check(self._lib.dg_plan_set_element_scale(
+            self._handle, None if scale is None else ctypes.c_void_p(scale.data_ptr())))
+
+    def adjoint(self, x: torch.Tensor, out: torch.Tensor | None = None,
+                scratch: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """``L^T x`` (FP64 wave plans on meshes uploaded with partners)."""
+        self._check_tensor(x, "x")
+        if out is None:
+            out = torch.empty_like(x)
+        else:
+            self._check_tensor(out, "out")
+        n = self.mesh.nelements * 2 * 4 * self.mesh.disc.nfp
+        if scratch is None:
+            scratch = getattr(self, "_adj_scratch", None)
+            if scratch is None or scratch.numel() != n:
+                scratch = torch.empty(n, dtype=torch.float64, device=self.mesh.device)
+                self._adj_scratch = scratch
+        elif scratch.numel() < n or scratch.dtype != torch.float64:
+            raise ValueError(f"scratch needs {n} float64 entries")
+        _lib.check(self._lib.dg_rhs_adjoint(
+            self._handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(scratch.data_ptr()), _stream_handle(stream)))
+        return out
 
     def finish(self, stream=None) -> None:
         _lib.check(self._lib.dg_finish(self._handle, _stream_handle(stream)))

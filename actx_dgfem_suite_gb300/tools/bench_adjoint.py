@@ -1,0 +1,119 @@
+"""Adjoint benchmark: gradient of a receiver misfit through the wave solve.
+
+Default configuration: wave P3 on [-1, 1]^3 with 6 * 40^3 tetrahedra,
+per-element wave speed c_e ~ U[0.8, 1.2] (seed 0), Gaussian-pulse initial
+pressure, 300 LSRK45 steps, 256 receivers at random interior points (seed 1),
+loss = 1/2 sum (traces - observations)^2 with observations computed from a
+perturbed speed c_e (1 + 0.05 xi_e), xi_e ~ U[-1, 1] (seed 2).
+
+Reports the forward and adjoint cost per step, the checkpoint memory, and
+central finite-difference checks of the gradient with respect to c_e and the
+initial state along random directions (FP64).
+
+``python -m actx_dgfem_suite_gb300.tools.bench_adjoint [--n 40 --steps 300]``
+prints one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+
+
+def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
+        cfl: float = 0.5, fd_eps: float = 1e-5) -> dict:
+    import time
+
+    import numpy as np
+    import torch
+
+    from actx_dgfem_suite_gb300.adjoint import (Receivers, WaveAdjointSolver,
+                                                WaveMisfitFunction,
+                                                random_interior_points)
+    from actx_dgfem_suite_gb300.equations.wave import wave_problem
+    from actx_dgfem_suite_gb300.perf_model import RhsCost
+    from actx_dgfem_suite_gb300.timestepping import estimate_rk4_timestep
+
+    t0 = time.perf_counter()
+    prob = wave_problem(order, n, "baseline")
+    d = prob.disc
+    pts = random_interior_points(nrec, (-1, -1, -1), (1, 1, 1), 0.05, seed=1)
+    rec = Receivers(d, pts, "cuda")
+    dt = estimate_rk4_timestep(d, 1.2, cfl)
+    solver = WaveAdjointSolver(d, dt, nsteps, rec)
+    q0 = torch.from_numpy(prob.fields).to(solver.device)
+    rng = np.random.default_rng(0)
+    c = torch.from_numpy(rng.uniform(0.8, 1.2, d.nelements)).to(solver.device)
+    xi = np.random.default_rng(2).uniform(-1, 1, d.nelements)
+    c_obs = c * torch.from_numpy(1 + 0.05 * xi).to(solver.device)
+    setup_s = time.perf_counter() - t0
+
+    with torch.no_grad():
+        obs = WaveMisfitFunction.apply(q0, c_obs, solver)
+
+    def loss(qq, cc):
+        t = WaveMisfitFunction.apply(qq, cc, solver)
+        return 0.5 * torch.sum((t - obs) ** 2)
+
+    qv = q0.clone().requires_grad_(True)
+    cv = c.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    s = time.perf_counter()
+    J = loss(qv, cv)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - s
+    s = time.perf_counter()
+    J.backward()
+    torch.cuda.synchronize()
+    t_bwd = time.perf_counter() - s
+    gq, gc = qv.grad, cv.grad
+
+    checks = {}
+    r2 = np.random.default_rng(7)
+    dirs = {"c": (None, torch.from_numpy(r2.standard_normal(d.nelements)).to(solver.device)),
+            "q0": (torch.from_numpy(r2.standard_normal(tuple(q0.shape))).to(solver.device), None)}
+    for name, (dq, dc) in dirs.items():
+        with torch.no_grad():
+            qp = q0 + fd_eps * dq if dq is not None else q0
+            qm = q0 - fd_eps * dq if dq is not None else q0
+            cp = c + fd_eps * dc if dc is not None else c
+            cm = c - fd_eps * dc if dc is not None else c
+            fd = (float(loss(qp, cp)) - float(loss(qm, cm))) / (2 * fd_eps)
+        an = float(torch.sum(gq * dq)) if dq is not None else float(torch.sum(gc * dc))
+        checks[name] = {"adjoint": an, "finite_difference": fd,
+                        "rel_diff": abs(an - fd) / max(abs(fd), 1e-300)}
+
+    cost = RhsCost("wave", order, d.nelements)
+    state_bytes = 4 * d.nelements * d.np_ * 8
+    nck = (nsteps - 1) // solver.segment + 1
+    return {
+        "workload": (f"wave P{order}, 6*{n}^3 tets, {nsteps} LSRK45 steps, "
+                     f"{nrec} receivers, c_e ~ U[0.8,1.2]"),
+        "nelements": d.nelements,
+        "dt": dt,
+        "loss": float(J),
+        "forward_ms_per_step": 1e3 * t_fwd / nsteps,
+        "adjoint_ms_per_step": 1e3 * t_bwd / nsteps,
+        "adjoint_over_forward": t_bwd / t_fwd,
+        "forward_dof_updates_per_s": 5 * nsteps * cost.dofs / t_fwd,
+        "checkpoint_segment": solver.segment,
+        "checkpoint_states": nck,
+        "peak_extra_states": nck + 5 * solver.segment,
+        "state_mb": state_bytes / 1e6,
+        "fd_checks": checks,
+        "setup_s": setup_s,
+    }
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m actx_dgfem_suite_gb300.tools.bench_adjoint")
+    ap.add_argument("--n", type=int, default=40)
+    ap.add_argument("--order", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--receivers", type=int, default=256)
+    a = ap.parse_args(argv)
+    print(json.dumps(run(a.n, a.order, a.steps, a.receivers)))
+
+
+if __name__ == "__main__":
+    main()

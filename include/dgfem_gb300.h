@@ -61,6 +61,10 @@ typedef struct dg_mesh_desc {
   const double* strong_diff; /* host, (3, Np, Np): D_r (maxwell) */
   const double* lift;        /* host, (Np, 4, Nfp): M^-1 E */
   const int32_t* face_nodes; /* host, (4, Nfp): volume node of each face node */
+  const int32_t* face_partner; /* device, (Nel, 4, Nfp): flat face-point index
+                                  (e'*4 + f')*Nfp + j' of the glued face point,
+                                  -1 on the boundary; optional, needed only by
+                                  dg_rhs_adjoint */
 } dg_mesh_desc;
 
 /* Build a plan: validate the description, stage the reference operators in
@@ -83,12 +87,32 @@ int dg_rhs(dg_plan* plan, const double* q, double* rhs, void* stream);
 /* One stage of a low-storage Runge-Kutta method fused into the RHS kernel:
  *   res   = a * res + dt * L(q_in)      (res is not read when a == 0)
  *   q_out = q_in + b * res
- * All three arrays are device (nfields, Nel, Np) FP64 and must not overlap;
- * q_out must differ from q_in because other elements still read q_in's face
- * values during the stage.  The reference evaluates the RHS only; its RK hook
+ * All arrays are device (nfields, Nel, Np) FP64 and must not overlap; q_out
+ * must differ from q_in because other elements still read q_in's face values
+ * during the stage.  rhs_unscaled (optional, NULL to skip) receives L(q_in)
+ * before the per-element scale (what an adjoint needs for the gradient with
+ * respect to that scale).  The reference evaluates the RHS only; its RK hook
  * is estimate_rk4_timestep (actx_dgfem_suite/equations/wave.py:206-213). */
 int dg_rk_stage(dg_plan* plan, const double* q_in, double* q_out, double* res,
-                double a, double b, double dt, void* stream);
+                double a, double b, double dt, double* rhs_unscaled,
+                void* stream);
+
+/* Multiply the RHS of every element e by scale[e] in dg_rhs / dg_rk_stage /
+ * dg_rhs_adjoint (a variable wave speed c_e for the wave operator, whose RHS
+ * is linear in c).  scale: device array of Nel doubles kept alive by the
+ * caller, or NULL to clear.  No counterpart in the reference (its wave speed
+ * is a scalar, actx_dgfem_suite/equations/wave.py:279). */
+int dg_plan_set_element_scale(dg_plan* plan, const double* scale);
+
+/* Transpose of the plan's operator: y = L^T x (Euclidean inner product over
+ * all DOFs), for FP64 wave plans built with mesh->face_partner.  The face
+ * gather's transpose is computed as a gather over glued face points, so the
+ * result is deterministic.  face_scratch: device buffer of Nel * 2 * 4 * Nfp
+ * doubles.  x, y, face_scratch must not overlap.  No counterpart in the
+ * reference (which has no adjoint); it is the building block of the
+ * gradient of a misfit with respect to the initial state and wave speed. */
+int dg_rhs_adjoint(dg_plan* plan, const double* x, double* y,
+                   double* face_scratch, void* stream);
 
 /* Block until `stream` has drained, then report any device-side error flag
  * the plan's kernels raised (DG_ERR_INDEX, DG_ERR_TIMEOUT) and clear it.

@@ -55,11 +55,13 @@ def test_argument_errors_without_device():
     d.order = 2
     assert L.dg_plan_create(ctypes.byref(h), 9, 0, ctypes.byref(d), None, 0) \
         == _lib.DG_ERR_ARGUMENT
-    assert L.dg_rk_stage(None, None, None, None, 0.0, 0.0, 0.0, None) \
+    assert L.dg_rk_stage(None, None, None, None, 0.0, 0.0, 0.0, None, None) \
         == _lib.DG_ERR_ARGUMENT
     assert L.dg_rhs(None, None, None, None) == _lib.DG_ERR_ARGUMENT
     assert L.dg_finish(None, None) == _lib.DG_ERR_ARGUMENT
     assert L.dg_plan_destroy(None) == _lib.DG_OK
     assert L.dg_fp64_fma_probe(None, 1, 1, 1, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_plan_set_element_scale(None, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_rhs_adjoint(None, None, None, None, None) == _lib.DG_ERR_ARGUMENT
     with pytest.raises(_lib.DGError):
         _lib.check(L.dg_rhs(None, None, None, None))

@@ -102,3 +102,19 @@ def test_union_discretization_offsets():
     x = u.nodes().reshape(3, -1)
     own = np.arange(u.nelements)[:, None, None] * u.np_ + u.ref.face_nodes[None]
     assert np.abs(x[:, u.ext_index] - x[:, own]).max() < 1e-14
+
+
+@pytest.mark.parametrize("order", [1, 2, 4])
+def test_face_partner_is_an_involution(order):
+    from tests._helpers import jittered_box_mesh
+    d = make_discretization(jittered_box_mesh(3), order)
+    p = d.face_partner().reshape(-1).astype(np.int64)
+    inter = p >= 0
+    idx = np.arange(p.size)
+    assert np.array_equal(p[p[inter]], idx[inter])
+    # partner face points sit at the same physical node as the exterior index
+    nfpt = 4 * d.nfp
+    fn = d.ref.face_nodes.reshape(-1)
+    node_of_fp = (idx // nfpt) * d.np_ + fn[idx % nfpt]
+    assert np.array_equal(node_of_fp[p[inter]], d.ext_index.reshape(-1)[inter])
+    assert np.array_equal(~inter.reshape(d.nelements, 4, -1).all(axis=2), d.is_boundary)
