@@ -152,13 +152,16 @@ class WaveAdjointSolver:
         dt = self.dt
         rbar = torch.zeros_like(lam)
         y = torch.empty_like(lam)
-        inv_dtc = (1.0 / (dt * c))[None, :, None]
+        inv_c = 1.0 / c
         for s in range(4, -1, -1):
             rbar.add_(lam, alpha=RK4B[s])
             self.plan.adjoint(rbar, y)
-            prev = residuals[s - 1] if s > 0 else None
-            lq = residuals[s] if prev is None else residuals[s] - RK4A[s] * prev
-            cbar.add_((rbar * lq * inv_dtc).sum(dim=(0, 2)), alpha=dt)
+            # dt <rbar, L q^{s-1}>_e with L q^{s-1} = (r^s - a_s r^{s-1}) / (dt c_e)
+            g = torch.einsum("fen,fen->e", rbar, residuals[s])
+            if s > 0:
+                g.sub_(torch.einsum("fen,fen->e", rbar, residuals[s - 1]),
+                       alpha=RK4A[s])
+            cbar.addcmul_(g, inv_c)
             lam.add_(y, alpha=dt)
             rbar.mul_(RK4A[s])
 

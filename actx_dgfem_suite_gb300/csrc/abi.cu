@@ -61,6 +61,13 @@ bool overlap(const void* a, const void* b, int64_t bytes) {
   return x < y + bytes && y < x + bytes;
 }
 
+// [a, a + na) and [b, b + nb) intersect
+bool overlap2(const void* a, int64_t na, const void* b, int64_t nb) {
+  const char* x = static_cast<const char*>(a);
+  const char* y = static_cast<const char*>(b);
+  return x < y + nb && y < x + na;
+}
+
 __global__ void fp64_fma_probe_kernel(double* out, int64_t iters) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double v[8];
@@ -324,8 +331,8 @@ int dg_rhs_adjoint(dg_plan* p, const double* x, double* y, double* face_scratch,
     return fail(DG_ERR_ARGUMENT, "x, y or face_scratch is NULL");
   const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
   const int64_t sbytes = p->nel * 2 * 4 * (int64_t)p->nfp * 8;
-  if (overlap(x, y, bytes) || overlap(x, face_scratch, bytes > sbytes ? bytes : sbytes) ||
-      overlap(y, face_scratch, bytes > sbytes ? bytes : sbytes))
+  if (overlap(x, y, bytes) || overlap2(x, bytes, face_scratch, sbytes) ||
+      overlap2(y, bytes, face_scratch, sbytes))
     return fail(DG_ERR_ARGUMENT, "x, y and face_scratch must not overlap");
   dg::AdjArgs a;
   std::memset(&a, 0, sizeof(a));

@@ -61,7 +61,8 @@ struct AdjTile {
   static constexpr int AUX = X + pad16(4 * E * NP * 8);
   static constexpr int GEO = AUX + pad16(3 * E * NP * 8);
   static constexpr int FGEO = GEO + pad16(9 * E * 8);
-  static constexpr int SMEM_BYTES = FGEO + pad16(16 * E * 8);
+  static constexpr int VN = FGEO + pad16(16 * E * 8);  // n_f . x_v per face, node
+  static constexpr int SMEM_BYTES = VN + pad16(4 * E * NP * 8);
 };
 
 template <int N>
@@ -78,6 +79,7 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
   double* sAux = reinterpret_cast<double*>(smem + T::AUX);
   double* sG = reinterpret_cast<double*>(smem + T::GEO);
   double* sFG = reinterpret_cast<double*>(smem + T::FGEO);
+  double* sVN = reinterpret_cast<double*>(smem + T::VN);
 
   const int t = threadIdx.x;
   if (t == 0) {
@@ -129,6 +131,11 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
       for (int r = 0; r < 3; ++r)
         sAux[(r * E + el) * NP + i] =
             fma(G[r * 3 + 0], v0, fma(G[r * 3 + 1], v1, G[r * 3 + 2] * v2));
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const double* fg = sFG + (el * 4 + f) * 4;
+        sVN[(el * 4 + f) * NP + i] = fma(fg[0], v0, fma(fg[1], v1, fg[2] * v2));
+      }
     }
     __syncthreads();
 
@@ -163,18 +170,15 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
       const int elp = pidx / NFPT;
       const int fj = pidx - elp * NFPT;
       const int f = fj / Shape<N>::NFP;
-      const double* fg = sFG + (elp * 4 + f) * 4;
-      const double nx = fg[0], ny = fg[1], nz = fg[2], s = fg[3];
+      const double s = sFG[(elp * 4 + f) * 4 + 3];
       double au = 0.0, av = 0.0;
       const double* xu = sX + (0 * E + elp) * NP;
-      const double* xv0 = sX + (1 * E + elp) * NP;
-      const double* xv1 = sX + (2 * E + elp) * NP;
-      const double* xv2 = sX + (3 * E + elp) * NP;
+      const double* vn = sVN + (elp * 4 + f) * NP;
 #pragma unroll 4
       for (int ii = 0; ii < NP; ++ii) {
         const double l = sL[ii * NFPT + fj];
         au = fma(l, xu[ii], au);
-        av = fma(l, fma(nx, xv0[ii], fma(ny, xv1[ii], nz * xv2[ii])), av);
+        av = fma(l, vn[ii], av);
       }
       double* sc = a.face_scratch + (e0 + elp) * 2 * NFPT;
       sc[fj] = s * au;

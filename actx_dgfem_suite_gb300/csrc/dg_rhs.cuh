@@ -111,8 +111,21 @@ struct Tile {
   static constexpr int FLUX = AUX + pad16(NAUX * E * NP * RS);
   static constexpr int GEO = FLUX + pad16(NF * E * NFPT * RS);
   static constexpr int FGEO = GEO + pad16(9 * E * RS);
-  static constexpr int SMEM_BYTES = FGEO + pad16(16 * E * RS);
+  // mixed-precision Euler: FP64 pressure of every node of the tile
+  static constexpr int PRES = FGEO + pad16(16 * E * RS);
+  static constexpr int SMEM_BYTES =
+      PRES + ((MIXED && EQ == DG_EULER) ? pad16(E * NP * 8) : 0);
 };
+
+// FP64 reciprocal from the FP32 estimate refined by one Newton step
+// (relative error below 2^-45).  The mixed-precision path uses it for the
+// FP64 pressure recovery, where a correctly rounded FP64 division would
+// dominate the cost on GB300's narrow FP64 pipe.
+__device__ __forceinline__ double rcp64_fast(double x) {
+  const double r0 = (double)__frcp_rn((float)x);
+  const double e = fma(-x, r0, 1.0);
+  return fma(r0, e, r0);
+}
 
 template <int N, int EQ, typename Real, int MODE>
 __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
@@ -133,6 +146,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   Real* sFlux = reinterpret_cast<Real*>(smem + T::FLUX);
   Real* sG = reinterpret_cast<Real*>(smem + T::GEO);
   Real* sFG = reinterpret_cast<Real*>(smem + T::FGEO);
+  double* sP = reinterpret_cast<double*>(smem + T::PRES);
 
   const int t = threadIdx.x;
   if (t == 0) {
@@ -199,10 +213,13 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         const double en_d = sQ[(1 * E + el) * NP + i];
         const double md[3] = {sQ[(2 * E + el) * NP + i], sQ[(3 * E + el) * NP + i],
                               sQ[(4 * E + el) * NP + i]};
-        const double rinv_d = 1.0 / rho_d;
+        double rinv_d;
+        if constexpr (T::MIXED) rinv_d = rcp64_fast(rho_d);
+        else rinv_d = 1.0 / rho_d;
         const double p_d =
             (a.p0 - 1.0) *
             (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
+        if constexpr (T::MIXED) sP[el * NP + i] = p_d;
         const Real p = (Real)p_d, en = (Real)en_d;
         const Real m[3] = {(Real)md[0], (Real)md[1], (Real)md[2]};
         const Real rinv = (Real)rinv_d;
@@ -316,28 +333,28 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       }
       const Real* fg = sFG + (elp * 4 + f) * 4;
       const Real nx = fg[0], ny = fg[1], nz = fg[2], scale = fg[3];
-      double qid[NF], qed[NF];
+      // interior trace from shared memory (already in the arithmetic type),
+      // exterior trace from HBM through the gather index (FP64 state)
+      Real qi[NF], qe[NF];
+      double qed[NF];
 #pragma unroll
-      for (int k = 0; k < NF; ++k) qid[k] = sQ[(k * E + elp) * NP + node];
+      for (int k = 0; k < NF; ++k) qi[k] = sQr[(k * E + elp) * NP + node];
       if (!bdry) {
 #pragma unroll
-        for (int k = 0; k < NF; ++k) qed[k] = __ldg(a.q + k * nelnp + gi);
+        for (int k = 0; k < NF; ++k) {
+          qed[k] = __ldg(a.q + k * nelnp + gi);
+          qe[k] = (Real)qed[k];
+        }
       }
       Real* out = sFlux + elp * NFPT + fj;
       constexpr int FS = E * NFPT;  // field stride in sFlux
 
       if constexpr (EQ == DG_WAVE) {
-        Real qi[4], qe[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) qi[k] = (Real)qid[k];
         if (bdry) {  // Dirichlet mirror: exterior (-u, v)
           qe[0] = -qi[0];
           qe[1] = qi[1];
           qe[2] = qi[2];
           qe[3] = qi[3];
-        } else {
-#pragma unroll
-          for (int k = 0; k < 4; ++k) qe[k] = (Real)qed[k];
         }
         const Real c = p0;
         const Real vavg_n = half * (qi[1] + qe[1]) * nx + half * (qi[2] + qe[2]) * ny +
@@ -352,50 +369,72 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         out[2 * FS] = scale * (fv * ny);
         out[3 * FS] = scale * (fv * nz);
       } else if constexpr (EQ == DG_EULER) {
-        if (bdry) {  // InviscidWallBC: mirror the normal momentum (FP64 state)
-          const double ndx = a.face_geom[((e0 + elp) * 4 + f) * 4 + 0];
-          const double ndy = a.face_geom[((e0 + elp) * 4 + f) * 4 + 1];
-          const double ndz = a.face_geom[((e0 + elp) * 4 + f) * 4 + 2];
-          const double mn = qid[2] * ndx + qid[3] * ndy + qid[4] * ndz;
-          qed[0] = qid[0];
-          qed[1] = qid[1];
-          qed[2] = qid[2] - 2.0 * ndx * mn;
-          qed[3] = qid[3] - 2.0 * ndy * mn;
-          qed[4] = qid[4] - 2.0 * ndz * mn;
-        }
         const Real gamma = p0;
+        double pi_d = 0.0, pe_d = 0.0;
+        if constexpr (T::MIXED) {
+          // FP64 pressures: interior from the pre-pass, exterior recovered here
+          pi_d = sP[elp * NP + node];
+          if (bdry) {
+            pe_d = pi_d;  // the wall mirror keeps rho, |m| and E
+          } else {
+            const double rinv_e = rcp64_fast(qed[0]);
+            pe_d = (a.p0 - 1.0) *
+                   (qed[1] - 0.5 * (qed[2] * qed[2] + qed[3] * qed[3] + qed[4] * qed[4]) *
+                                 rinv_e);
+          }
+        }
+        if (bdry) {  // InviscidWallBC: mirror the normal momentum
+          if constexpr (T::MIXED) {
+            const Real mn = qi[2] * nx + qi[3] * ny + qi[4] * nz;
+            qe[0] = qi[0];
+            qe[1] = qi[1];
+            qe[2] = qi[2] - two * nx * mn;
+            qe[3] = qi[3] - two * ny * mn;
+            qe[4] = qi[4] - two * nz * mn;
+          } else {  // FP64: the normal in FP64 from HBM
+            const double ndx = a.face_geom[((e0 + elp) * 4 + f) * 4 + 0];
+            const double ndy = a.face_geom[((e0 + elp) * 4 + f) * 4 + 1];
+            const double ndz = a.face_geom[((e0 + elp) * 4 + f) * 4 + 2];
+            const double mn = qi[2] * ndx + qi[3] * ndy + qi[4] * ndz;
+            qe[0] = qi[0];
+            qe[1] = qi[1];
+            qe[2] = qi[2] - 2.0 * ndx * mn;
+            qe[3] = qi[3] - 2.0 * ndy * mn;
+            qe[4] = qi[4] - 2.0 * ndz * mn;
+          }
+        }
         Real fn_i[5], fn_e[5], lam_i, lam_e;
-        auto side = [&](const double* qd, Real* fn, Real& lam) {
-          const double rinv_d = 1.0 / qd[0];
-          const double p_d =  // pressure recovery from total energy in FP64
-              (a.p0 - 1.0) *
-              (qd[1] - 0.5 * (qd[2] * qd[2] + qd[3] * qd[3] + qd[4] * qd[4]) * rinv_d);
-          const Real p = (Real)p_d, rinv = (Real)rinv_d;
-          const Real q1 = (Real)qd[1], q2 = (Real)qd[2], q3 = (Real)qd[3],
-                     q4 = (Real)qd[4];
-          const Real ux = q2 * rinv, uy = q3 * rinv, uz = q4 * rinv;
+        auto side = [&](const Real* q, double p_mixed, Real* fn, Real& lam) {
+          Real p, rinv;
+          if constexpr (T::MIXED) {
+            p = (Real)p_mixed;
+            rinv = (Real)1 / q[0];
+          } else {
+            const double rinv_d = 1.0 / q[0];
+            p = (a.p0 - 1.0) *
+                (q[1] - 0.5 * (q[2] * q[2] + q[3] * q[3] + q[4] * q[4]) * rinv_d);
+            rinv = rinv_d;
+          }
+          const Real ux = q[2] * rinv, uy = q[3] * rinv, uz = q[4] * rinv;
           const Real un = ux * nx + uy * ny + uz * nz;
-          fn[0] = q2 * nx + q3 * ny + q4 * nz;
-          fn[1] = un * (q1 + p);
-          fn[2] = q2 * un + p * nx;
-          fn[3] = q3 * un + p * ny;
-          fn[4] = q4 * un + p * nz;
+          fn[0] = q[2] * nx + q[3] * ny + q[4] * nz;
+          fn[1] = un * (q[1] + p);
+          fn[2] = q[2] * un + p * nx;
+          fn[3] = q[3] * un + p * ny;
+          fn[4] = q[4] * un + p * nz;
           lam = sqrt(ux * ux + uy * uy + uz * uz) + sqrt(gamma * (p * rinv));
         };
-        side(qid, fn_i, lam_i);
-        side(qed, fn_e, lam_e);
+        side(qi, pi_d, fn_i, lam_i);
+        side(qe, pe_d, fn_e, lam_e);
         const Real lam = fmax(lam_i, lam_e);
         const Real nn = nx * nx + ny * ny + nz * nz;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-          const Real dq = (Real)(qed[k] - qid[k]);
+          const Real dq = qe[k] - qi[k];
           const Real fk = half * (fn_i[k] + fn_e[k]) - half * lam * dq * nn;
           out[k * FS] = -scale * fk;
         }
       } else {  // DG_MAXWELL
-        Real qi[6], qe[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) qi[k] = (Real)qid[k];
         if (bdry) {  // PEC: exterior (-E, H)
           qe[0] = -qi[0];
           qe[1] = -qi[1];
@@ -403,9 +442,6 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           qe[3] = qi[3];
           qe[4] = qi[4];
           qe[5] = qi[5];
-        } else {
-#pragma unroll
-          for (int k = 0; k < 6; ++k) qe[k] = (Real)qed[k];
         }
         const Real alpha = p0, eps = p1, mu = p2;
         const Real z = sqrt(mu / eps), y = (Real)1 / z;
