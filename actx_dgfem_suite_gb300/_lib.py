@@ -29,7 +29,7 @@ DG_FP32_MIXED = 1
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
-                    "dg_rhs_adjoint",
+                    "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
                     "dg_plan_info", "dg_fp64_fma_probe", "dg_last_error",
                     "dg_abi_version")
 
@@ -90,6 +90,8 @@ def lib() -> ctypes.CDLL:
     L.dg_plan_set_element_scale.restype = ctypes.c_int
     L.dg_rhs_adjoint.argtypes = [vp, vp, vp, vp, vp]
     L.dg_rhs_adjoint.restype = ctypes.c_int
+    L.dg_rhs_adjoint_noalloc.argtypes = [vp, vp, vp, vp]
+    L.dg_rhs_adjoint_noalloc.restype = ctypes.c_int
     L.dg_finish.argtypes = [vp, vp]
     L.dg_finish.restype = ctypes.c_int
     L.dg_plan_destroy.argtypes = [vp]

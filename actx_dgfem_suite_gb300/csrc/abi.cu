@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -395,6 +396,65 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
                               reinterpret_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
   return DG_OK;
+}
+
+}  // extern "C"
+
+// Face-point scratch of dg_rhs_adjoint_noalloc, one per device that loads the
+// library.  In host code this name is only a stand-in for the device array:
+// its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) double
+    g_noalloc_scratch[DG_NOALLOC_SCRATCH_BYTES / sizeof(double)];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the static scratch on `device` (which must be current),
+// looked up on the first call for that device and cached.
+int noalloc_scratch(int device, double** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[device]) {
+    void* ptr = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "looking up the static adjoint scratch");
+    g_noalloc_addr[device] = static_cast<double*>(ptr);
+  }
+  *out = g_noalloc_addr[device];
+  return DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_rhs_adjoint_noalloc(dg_plan* p, const double* x, double* y,
+                           void* stream) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!p->d_adj_ops)
+    return fail(DG_ERR_UNSUPPORTED,
+                "adjoint needs an FP64 wave plan built with face_partner");
+  if (!x || !y) return fail(DG_ERR_ARGUMENT, "x or y is NULL");
+  const int64_t need = p->nel * 2 * 4 * (int64_t)p->nfp * 8;
+  if (need > (int64_t)DG_NOALLOC_SCRATCH_BYTES)
+    return fail(DG_ERR_ARGUMENT,
+                "mesh too large for the static adjoint scratch: needs " +
+                    std::to_string(need) + " bytes, the buffer holds " +
+                    std::to_string(DG_NOALLOC_SCRATCH_BYTES));
+  int dev = -1;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return cuda_fail(err, "cudaGetDevice");
+  if (dev != p->device)
+    return fail(DG_ERR_ARGUMENT, "the plan's device must be current");
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(DG_ERR_UNSUPPORTED, "device ordinal out of range");
+  double* scratch = nullptr;
+  const int code = noalloc_scratch(dev, &scratch);
+  if (code != DG_OK) return code;
+  return dg_rhs_adjoint(p, x, y, scratch, stream);
 }
 
 int dg_finish(dg_plan* p, void* stream) {

@@ -114,6 +114,32 @@ int dg_plan_set_element_scale(dg_plan* plan, const double* scale);
 int dg_rhs_adjoint(dg_plan* plan, const double* x, double* y,
                    double* face_scratch, void* stream);
 
+/* Size of the device buffer that dg_rhs_adjoint_noalloc works in. */
+#define DG_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+
+/* dg_rhs_adjoint without a caller-supplied scratch buffer and without any
+ * allocation.  It has no counterpart in the reference.
+ *
+ * Who needs it: callers that are not allowed to call cudaMalloc while they
+ * run -- for example a host application that reserves the whole device
+ * memory budget for its own pool at start-up and forbids allocations behind
+ * its back, or code on a latency-critical path where cudaMalloc could
+ * synchronise the device and stall work on other streams.
+ *
+ * How it works: the face-point scratch lives in one file-scope __device__
+ * array of DG_NOALLOC_SCRATCH_BYTES (64 MiB) that every GPU loading this
+ * library holds until the process exits.  The plan's mesh must fit:
+ * Nel * 2 * 4 * Nfp * 8 bytes <= 64 MiB, i.e. at most 349,525 / 174,762 /
+ * 104,857 / 69,905 elements at P1 / P2 / P3 / P4; larger meshes are
+ * rejected with DG_ERR_ARGUMENT.  The plan's device must be current.
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Nothing in the array needs to start at zero: each call writes every entry
+ * it later reads.  All calls share the one array, so calls that overlap on
+ * the GPU (concurrent streams) race and must be serialised by the caller. */
+int dg_rhs_adjoint_noalloc(dg_plan* plan, const double* x, double* y,
+                           void* stream);
+
 /* Block until `stream` has drained, then report any device-side error flag
  * the plan's kernels raised (DG_ERR_INDEX, DG_ERR_TIMEOUT) and clear it.
  * Replaces finish_command_queue(actx) (actx_dgfem_suite/measure.py:48-55). */
