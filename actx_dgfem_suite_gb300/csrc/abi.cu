@@ -266,6 +266,10 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   p->grid = (int)(ntiles < full ? ntiles : full);
 
   if (mesh->face_partner && equation == DG_WAVE && precision == DG_FP64) {
+    if (p->nel * 8 * (int64_t)nfp >= (int64_t(1) << 32)) {
+      dg_plan_destroy(p);
+      return fail(DG_ERR_ARGUMENT, "mesh too large for the adjoint's 32-bit face indices");
+    }
     cudaPointerAttributes attr;
     if (cudaPointerGetAttributes(&attr, mesh->face_partner) != cudaSuccess ||
         attr.type != cudaMemoryTypeDevice) {

@@ -106,20 +106,27 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t e0 = tile * E;
     const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
-    for (int idx = t; idx < 4 * E * NP; idx += kBlock) {
-      const int k = idx / (E * NP);
-      const int rem = idx - k * (E * NP);
-      double v = 0.0;
-      if (rem < ecount * NP) {
-        v = a.c * __ldg(a.x + k * nelnp + e0 * NP + rem);
-        if (a.elem_scale) v *= __ldg(a.elem_scale + e0 + rem / NP);
+    {
+      const double* xk = a.x + e0 * NP;
+      const double* sc_t = a.elem_scale ? a.elem_scale + e0 : nullptr;
+#pragma unroll
+      for (int k = 0; k < 4; ++k, xk += nelnp) {
+        for (int rem = t; rem < E * NP; rem += kBlock) {
+          double v = 0.0;
+          if (rem < ecount * NP) {
+            v = a.c * __ldg(xk + rem);
+            if (sc_t) v *= __ldg(sc_t + rem / NP);
+          }
+          sX[k * (E * NP) + rem] = v;
+        }
       }
-      sX[idx] = v;
+      const double* mt = a.metric + e0 * 9;
+      const double* ft = a.face_geom + e0 * 16;
+      for (int idx = t; idx < 9 * E; idx += kBlock)
+        sG[idx] = idx < 9 * ecount ? __ldg(mt + idx) : 0.0;
+      for (int idx = t; idx < 16 * E; idx += kBlock)
+        sFG[idx] = idx < 16 * ecount ? __ldg(ft + idx) : 0.0;
     }
-    for (int idx = t; idx < 9 * E; idx += kBlock)
-      sG[idx] = idx < 9 * ecount ? __ldg(a.metric + e0 * 9 + idx) : 0.0;
-    for (int idx = t; idx < 16 * E; idx += kBlock)
-      sFG[idx] = idx < 16 * ecount ? __ldg(a.face_geom + e0 * 16 + idx) : 0.0;
     __syncthreads();
 
     if (active && el < ecount) {
@@ -157,12 +164,13 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
                  fma(w1, sAux[(1 * E + el) * NP + j],
                      fma(w2, sAux[(2 * E + el) * NP + j], dv)));
       }
-      const int64_t g = (e0 + el) * NP + i;
-      a.y[0 * nelnp + g] = -dv;
+      double* yk = a.y + e0 * NP + (el * NP + i);
+      *yk = -dv;
 #pragma unroll
-      for (int x = 0; x < 3; ++x)
-        a.y[(1 + x) * nelnp + g] =
-            -fma(G[0 * 3 + x], ur0, fma(G[1 * 3 + x], ur1, G[2 * 3 + x] * ur2));
+      for (int x = 0; x < 3; ++x) {
+        yk += nelnp;
+        *yk = -fma(G[0 * 3 + x], ur0, fma(G[1 * 3 + x], ur1, G[2 * 3 + x] * ur2));
+      }
     }
 
     // lifted face adjoints
@@ -180,7 +188,7 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
         au = fma(l, xu[ii], au);
         av = fma(l, vn[ii], av);
       }
-      double* sc = a.face_scratch + (e0 + elp) * 2 * NFPT;
+      double* sc = a.face_scratch + e0 * (2 * NFPT) + elp * (2 * NFPT);
       sc[fj] = s * au;
       sc[NFPT + fj] = s * av;
     }
@@ -189,64 +197,76 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
 }
 
 // One thread per node: add the transposed flux and face-gather contributions.
+// Index arithmetic stays in 32 bits (Nel * 4 Nfp < 2^31 is checked on the
+// host): on GB300 wide integer multiplies compete with FP64 for a narrow pipe.
 template <int N>
 __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_surface(const AdjArgs a) {
   using Ops = AdjOpsLayout<N>;
   constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
-  __shared__ int sFN[NFPT];
-  const int* gFN = reinterpret_cast<const int*>(
-      static_cast<const unsigned char*>(a.ops) + Ops::FN);
-  for (int k = threadIdx.x; k < NFPT; k += blockDim.x) sFN[k] = gFN[k];
+  // face points of every volume node (a node lies on at most 3 faces)
+  __shared__ int sNodeFP[NP][3];
+  if (threadIdx.x < NP) {
+    const int* gFN = reinterpret_cast<const int*>(
+        static_cast<const unsigned char*>(a.ops) + Ops::FN);
+    int cnt = 0;
+    for (int fj = 0; fj < NFPT; ++fj)
+      if (gFN[fj] == (int)threadIdx.x && cnt < 3) sNodeFP[threadIdx.x][cnt++] = fj;
+    for (; cnt < 3; ++cnt) sNodeFP[threadIdx.x][cnt] = -1;
+  }
   __syncthreads();
-  const int64_t nelnp = a.nel * NP;
-  const int64_t nfpt_total = a.nel * NFPT;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nelnp;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = g / NP;
+  const uint32_t nelnp = (uint32_t)(a.nel * NP);
+  const uint32_t nfpt_total = (uint32_t)(a.nel * NFPT);
+  double* yu_p = a.y;
+  double* y0_p = a.y + nelnp;
+  double* y1_p = y0_p + nelnp;
+  double* y2_p = y1_p + nelnp;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < nelnp;
+       g += gridDim.x * blockDim.x) {
+    const uint32_t e = g / NP;
     const int i = (int)(g - e * NP);
-    double yu = a.y[g], y0 = a.y[nelnp + g], y1 = a.y[2 * nelnp + g],
-           y2 = a.y[3 * nelnp + g];
-    const double* sc = a.face_scratch + e * 2 * NFPT;
-    for (int fj = 0; fj < NFPT; ++fj) {
-      if (sFN[fj] != i) continue;
-      const int f = fj / NFP;
-      const double* fg = a.face_geom + (e * 4 + f) * 4;
-      const double nx = fg[0], ny = fg[1], nz = fg[2];
+    if (sNodeFP[i][0] < 0) continue;  // interior node: volume part only
+    double yu = yu_p[g], y0 = y0_p[g], y1 = y1_p[g], y2 = y2_p[g];
+    const double* sc = a.face_scratch + e * (2 * NFPT);
+    const double* fge = a.face_geom + e * 16;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int fj = sNodeFP[i][m];
+      if (fj < 0) break;
+      const double* fg = fge + (fj / NFP) * 4;
       const double au = sc[fj], av = sc[NFPT + fj];
-      // own face point, interior-trace derivatives
-      yu += -0.5 * au + 0.5 * av;
-      const double cv = 0.5 * au - 0.5 * av;
-      y0 += nx * cv;
-      y1 += ny * cv;
-      y2 += nz * cv;
       const int32_t p = a.face_partner[e * NFPT + fj];
       if (p < 0) {
-        // boundary mirror: u+ = -u-, v+ = v-
-        yu += -(0.5 * au + 0.5 * av);
-        const double cb = 0.5 * au + 0.5 * av;
-        y0 += nx * cb;
-        y1 += ny * cb;
-        y2 += nz * cb;
-      } else if ((int64_t)p < nfpt_total) {
-        // the partner's flux depends on this node as its exterior trace
-        const int64_t pe = p / NFPT;
-        const int pfj = p - (int)(pe * NFPT);
-        const double* psc = a.face_scratch + pe * 2 * NFPT;
-        const double pu = psc[pfj], pv = psc[NFPT + pfj];
-        const double* pg = a.face_geom + (pe * 4 + pfj / NFP) * 4;
-        yu += 0.5 * pu + 0.5 * pv;
-        const double cp = 0.5 * pu + 0.5 * pv;
-        y0 += pg[0] * cp;
-        y1 += pg[1] * cp;
-        y2 += pg[2] * cp;
+        // own flux with the boundary mirror u+ = -u-, v+ = v- folded in:
+        // d/du- = -abar_u, d/dv- = n abar_u
+        yu -= au;
+        y0 = fma(fg[0], au, y0);
+        y1 = fma(fg[1], au, y1);
+        y2 = fma(fg[2], au, y2);
+      } else if ((uint32_t)p < nfpt_total) {
+        // own flux, interior-trace derivatives
+        const double d = 0.5 * (av - au);
+        yu += d;
+        y0 = fma(-fg[0], d, y0);
+        y1 = fma(-fg[1], d, y1);
+        y2 = fma(-fg[2], d, y2);
+        // the glued partner's flux depends on this node as its exterior trace
+        const uint32_t pe = (uint32_t)p / NFPT;
+        const int pfj = p - (int32_t)(pe * NFPT);
+        const double* psc = a.face_scratch + pe * (2 * NFPT);
+        const double sp = 0.5 * (psc[pfj] + psc[NFPT + pfj]);
+        const double* pg = a.face_geom + pe * 16 + (pfj / NFP) * 4;
+        yu += sp;
+        y0 = fma(pg[0], sp, y0);
+        y1 = fma(pg[1], sp, y1);
+        y2 = fma(pg[2], sp, y2);
       } else {
         raise_status(a.status, DG_ERR_INDEX);
       }
     }
-    a.y[g] = yu;
-    a.y[nelnp + g] = y0;
-    a.y[2 * nelnp + g] = y1;
-    a.y[3 * nelnp + g] = y2;
+    yu_p[g] = yu;
+    y0_p[g] = y0;
+    y1_p[g] = y1;
+    y2_p[g] = y2;
   }
 }
 

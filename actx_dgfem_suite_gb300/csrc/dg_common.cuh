@@ -76,4 +76,38 @@ __device__ __forceinline__ void raise_status(int* status, int code) {
   if (status) atomicMax(status, code);
 }
 
+// FP64 <-> FP32 conversions done with integer ALU instructions.  On GB300 the
+// FP64 pipe issues a small fraction of the FP32/INT rate, and conversion
+// instructions that touch FP64 compete for it; in the mixed-precision kernels
+// the state is converted once per load, so these bit manipulations keep that
+// traffic off the FP64 pipe.  Round to nearest even; results below the
+// smallest normal float flush to zero, values beyond the float range become
+// infinity (the DG states are O(1)).
+__device__ __forceinline__ float d2f_alu(double x) {
+  const uint32_t lo = (uint32_t)__double2loint(x);
+  const uint32_t hi = (uint32_t)__double2hiint(x);
+  const uint32_t sign = hi & 0x80000000u;
+  const int32_t e = (int32_t)((hi >> 20) & 0x7ffu) - 896;  // float biased exponent
+  const uint32_t mant = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const uint32_t rest = lo & 0x1fffffffu;
+  uint32_t bits = ((uint32_t)e << 23) + mant;
+  bits += (uint32_t)((rest > 0x10000000u) | ((rest == 0x10000000u) & (mant & 1u)));
+  bits = e <= 0 ? 0u : bits;
+  bits = e >= 255 ? 0x7f800000u : bits;
+  return __uint_as_float(sign | bits);
+}
+
+__device__ __forceinline__ double f2d_alu(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t sign = b & 0x80000000u;
+  const uint32_t e = (b >> 23) & 0xffu;
+  const uint32_t m = b & 0x7fffffu;
+  uint32_t hi = sign | ((e + 896u) << 20) | (m >> 3);
+  uint32_t lo = m << 29;
+  hi = e == 0u ? sign : hi;
+  lo = e == 0u ? 0u : lo;
+  hi = e == 255u ? (sign | 0x7ff00000u | (m >> 3)) : hi;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 }  // namespace dg

@@ -127,6 +127,13 @@ __device__ __forceinline__ double rcp64_fast(double x) {
   return fma(r0, e, r0);
 }
 
+// double -> arithmetic type; the mixed path converts on the integer ALU
+template <typename Real>
+__device__ __forceinline__ Real to_real(double v) {
+  if constexpr (std::is_same<Real, double>::value) return v;
+  else return d2f_alu(v);
+}
+
 template <int N, int EQ, typename Real, int MODE>
 __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   using T = Tile<N, EQ, Real>;
@@ -176,20 +183,27 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     const int64_t e0 = tile * E;
     const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
 
-    // {{{ 1. state and geometry -> shared memory (coalesced)
-    for (int idx = t; idx < NF * E * NP; idx += kBlock) {
-      const int k = idx / (E * NP);
-      const int rem = idx - k * (E * NP);
-      const double v =
-          rem < ecount * NP ? __ldg(a.q + k * nelnp + e0 * NP + rem) : 0.0;
-      sQ[idx] = v;
-      if constexpr (T::MIXED) sQr[idx] = (Real)v;
+    // {{{ 1. state and geometry -> shared memory (coalesced; 64-bit address
+    //         arithmetic once per tile and field, 32-bit offsets inside)
+    {
+      const double* qk = a.q + e0 * NP;
+#pragma unroll
+      for (int k = 0; k < NF; ++k, qk += nelnp) {
+        for (int rem = t; rem < E * NP; rem += kBlock) {
+          const double v = rem < ecount * NP ? __ldg(qk + rem) : 0.0;
+          sQ[k * (E * NP) + rem] = v;
+          if constexpr (T::MIXED) sQr[k * (E * NP) + rem] = to_real<Real>(v);
+        }
+      }
     }
-    for (int idx = t; idx < 9 * E; idx += kBlock)
-      sG[idx] = idx < 9 * ecount ? (Real)__ldg(a.metric + e0 * 9 + idx) : zero;
-    for (int idx = t; idx < 16 * E; idx += kBlock)
-      sFG[idx] =
-          idx < 16 * ecount ? (Real)__ldg(a.face_geom + e0 * 16 + idx) : zero;
+    {
+      const double* mt = a.metric + e0 * 9;
+      const double* ft = a.face_geom + e0 * 16;
+      for (int idx = t; idx < 9 * E; idx += kBlock)
+        sG[idx] = idx < 9 * ecount ? to_real<Real>(__ldg(mt + idx)) : zero;
+      for (int idx = t; idx < 16 * E; idx += kBlock)
+        sFG[idx] = idx < 16 * ecount ? to_real<Real>(__ldg(ft + idx)) : zero;
+    }
     __syncthreads();
     // }}}
 
@@ -220,9 +234,10 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
             (a.p0 - 1.0) *
             (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
         if constexpr (T::MIXED) sP[el * NP + i] = p_d;
-        const Real p = (Real)p_d, en = (Real)en_d;
-        const Real m[3] = {(Real)md[0], (Real)md[1], (Real)md[2]};
-        const Real rinv = (Real)rinv_d;
+        const Real p = to_real<Real>(p_d), en = to_real<Real>(en_d);
+        const Real m[3] = {to_real<Real>(md[0]), to_real<Real>(md[1]),
+                           to_real<Real>(md[2])};
+        const Real rinv = to_real<Real>(rinv_d);
         const Real u[3] = {m[0] * rinv, m[1] * rinv, m[2] * rinv};
         Real F[5][3];
 #pragma unroll
@@ -319,17 +334,19 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     // }}}
 
     // {{{ 4. face gather + numerical flux
+    const uint32_t* gt = a.gather + e0 * NFPT;
+    const uint32_t tile_node0 = (uint32_t)(e0 * NP);
     for (int pidx = t; pidx < ecount * NFPT; pidx += kBlock) {
       const int elp = pidx / NFPT;
       const int fj = pidx - elp * NFPT;
       const int f = fj / Shape<N>::NFP;
       const int node = sFN[fj];
-      uint32_t g = __ldg(a.gather + (e0 + elp) * NFPT + fj);
-      bool bdry = (g >> 31) != 0u;
-      int64_t gi = (int64_t)(g & 0x7fffffffu);
-      if (gi >= nelnp) {  // never read out of bounds
+      const uint32_t g = __ldg(gt + pidx);
+      const bool bdry = (g >> 31) != 0u;
+      uint32_t gi = g & 0x7fffffffu;
+      if (gi >= (uint32_t)nelnp) {  // never read out of bounds
         raise_status(a.status, DG_ERR_INDEX);
-        gi = (e0 + elp) * NP + node;
+        gi = tile_node0 + (uint32_t)(elp * NP + node);
       }
       const Real* fg = sFG + (elp * 4 + f) * 4;
       const Real nx = fg[0], ny = fg[1], nz = fg[2], scale = fg[3];
@@ -340,10 +357,11 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
 #pragma unroll
       for (int k = 0; k < NF; ++k) qi[k] = sQr[(k * E + elp) * NP + node];
       if (!bdry) {
+        const double* qk = a.q + gi;
 #pragma unroll
-        for (int k = 0; k < NF; ++k) {
-          qed[k] = __ldg(a.q + k * nelnp + gi);
-          qe[k] = (Real)qed[k];
+        for (int k = 0; k < NF; ++k, qk += nelnp) {
+          qed[k] = __ldg(qk);
+          qe[k] = to_real<Real>(qed[k]);
         }
       }
       Real* out = sFlux + elp * NFPT + fj;
@@ -392,9 +410,8 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
             qe[3] = qi[3] - two * ny * mn;
             qe[4] = qi[4] - two * nz * mn;
           } else {  // FP64: the normal in FP64 from HBM
-            const double ndx = a.face_geom[((e0 + elp) * 4 + f) * 4 + 0];
-            const double ndy = a.face_geom[((e0 + elp) * 4 + f) * 4 + 1];
-            const double ndz = a.face_geom[((e0 + elp) * 4 + f) * 4 + 2];
+            const double* fgd = a.face_geom + e0 * 16 + (elp * 4 + f) * 4;
+            const double ndx = fgd[0], ndy = fgd[1], ndz = fgd[2];
             const double mn = qi[2] * ndx + qi[3] * ndy + qi[4] * ndz;
             qe[0] = qi[0];
             qe[1] = qi[1];
@@ -407,7 +424,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         auto side = [&](const Real* q, double p_mixed, Real* fn, Real& lam) {
           Real p, rinv;
           if constexpr (T::MIXED) {
-            p = (Real)p_mixed;
+            p = to_real<Real>(p_mixed);
             rinv = (Real)1 / q[0];
           } else {
             const double rinv_d = 1.0 / q[0];
@@ -477,16 +494,17 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     // {{{ 5. LIFT, then store or fold into the RK stage
     if (active && el < ecount) {
       const Real* fl = sFlux + el * NFPT;
-      const int64_t node_idx = (e0 + el) * NP + i;
+      int64_t gidx = e0 * NP + (el * NP + i);  // advanced by nelnp per field
 #pragma unroll
-      for (int k = 0; k < NF; ++k) {
+      for (int k = 0; k < NF; ++k, gidx += nelnp) {
         Real acc = vol[k];
 #pragma unroll 4
         for (int fj = 0; fj < NFPT; ++fj)
           acc = fma(sL[fj * NP + i], fl[k * E * NFPT + fj], acc);
         if constexpr (EQ == DG_MAXWELL) acc = acc / (k < 3 ? p1 : p2);
-        const int64_t gidx = k * nelnp + node_idx;
-        double val = (double)acc;
+        double val;
+        if constexpr (T::MIXED) val = f2d_alu(acc);
+        else val = acc;
         if constexpr (MODE == MODE_STAGE)
           if (a.rhs_unscaled) a.rhs_unscaled[gidx] = val;
         if (a.elem_scale) val *= __ldg(a.elem_scale + e0 + el);
