@@ -144,20 +144,39 @@ void pack_adj_ops(std::vector<unsigned char>& buf, int np, int nfp,
   for (int k = 0; k < 4 * nfp; ++k) fn[k] = face_nodes[k];
 }
 
-template <typename Real>
-void pack_ops(std::vector<unsigned char>& buf, const dg::OpsOffsets& off,
-              int np, int nfp, const double* diff, const double* lift,
-              const int32_t* face_nodes) {
-  Real* w = reinterpret_cast<Real*>(buf.data() + off.w);
-  Real* l = reinterpret_cast<Real*>(buf.data() + off.l);
+// FP64: Wt[r][j][i] and Lt[fj][i] (one scalar per thread and step).
+void pack_ops_fp64(std::vector<unsigned char>& buf, const dg::OpsOffsets& off,
+                   int np, int nfp, const double* diff, const double* lift,
+                   const int32_t* face_nodes) {
+  double* w = reinterpret_cast<double*>(buf.data() + off.w);
+  double* l = reinterpret_cast<double*>(buf.data() + off.l);
   int32_t* fn = reinterpret_cast<int32_t*>(buf.data() + off.fn);
   for (int r = 0; r < 3; ++r)
     for (int i = 0; i < np; ++i)
       for (int j = 0; j < np; ++j)
-        w[(r * np + j) * np + i] = (Real)diff[(r * np + i) * np + j];
+        w[(r * np + j) * np + i] = diff[(r * np + i) * np + j];
   for (int i = 0; i < np; ++i)
     for (int fj = 0; fj < 4 * nfp; ++fj)
-      l[fj * np + i] = (Real)lift[i * 4 * nfp + fj];
+      l[fj * np + i] = lift[i * 4 * nfp + fj];
+  for (int k = 0; k < 4 * nfp; ++k) fn[k] = face_nodes[k];
+}
+
+// Mixed: FP32 W[r][i][j] and L[i][fj] with zero-padded rows of pitch
+// pitch_host(np) and pitch_host(4 nfp) (four entries per shared load).
+void pack_ops_fp32(std::vector<unsigned char>& buf, const dg::OpsOffsets& off,
+                   int np, int nfp, const double* diff, const double* lift,
+                   const int32_t* face_nodes) {
+  float* w = reinterpret_cast<float*>(buf.data() + off.w);
+  float* l = reinterpret_cast<float*>(buf.data() + off.l);
+  int32_t* fn = reinterpret_cast<int32_t*>(buf.data() + off.fn);
+  const int rp = dg::pitch_host(np), fp = dg::pitch_host(4 * nfp);
+  for (int r = 0; r < 3; ++r)
+    for (int i = 0; i < np; ++i)
+      for (int j = 0; j < np; ++j)
+        w[(r * np + i) * rp + j] = (float)diff[(r * np + i) * np + j];
+  for (int i = 0; i < np; ++i)
+    for (int fj = 0; fj < 4 * nfp; ++fj)
+      l[i * fp + fj] = (float)lift[i * 4 * nfp + fj];
   for (int k = 0; k < 4 * nfp; ++k) fn[k] = face_nodes[k];
 }
 
@@ -228,9 +247,9 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
 
   std::vector<unsigned char> ops(off.size, 0);
   if (precision == DG_FP64)
-    pack_ops<double>(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
+    pack_ops_fp64(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
   else
-    pack_ops<float>(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
+    pack_ops_fp32(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
 
   dg_plan* p = new dg_plan;
   p->equation = equation;

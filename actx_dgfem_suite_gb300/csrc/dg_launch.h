@@ -25,11 +25,19 @@ struct OpsOffsets {
   int w, l, fn, size;
 };
 inline int pad16_host(int n) { return (n + 15) & ~15; }
+// same rule as the kernels' odd4(): multiple of 4 with an odd quotient
+inline int pitch_host(int n) {
+  const int m = (n + 3) & ~3;
+  return (m / 4) % 2 == 0 ? m + 4 : m;
+}
+// rs = 8: FP64 layout Wt[r][j][i], Lt[fj][i]; rs = 4: mixed layout
+// W[r][i][j] with pitch pitch_host(np), L[i][fj] with pitch pitch_host(4 nfp)
 inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
   OpsOffsets o;
+  const bool mixed = rs == 4;
   o.w = 0;
-  o.l = o.w + pad16_host(3 * np * np * rs);
-  o.fn = o.l + pad16_host(4 * nfp * np * rs);
+  o.l = o.w + pad16_host((mixed ? 3 * np * pitch_host(np) : 3 * np * np) * rs);
+  o.fn = o.l + pad16_host((mixed ? np * pitch_host(4 * nfp) : 4 * nfp * np) * rs);
   o.size = o.fn + pad16_host(4 * nfp * 4);
   return o;
 }

@@ -86,13 +86,35 @@ struct EqInfo<DG_MAXWELL> {
 
 constexpr int pad16(int bytes) { return (bytes + 15) & ~15; }
 
+// Row pitch (in floats) for rows read with 16-byte shared-memory loads: a
+// multiple of 4 whose quotient by 4 is odd, so 8 consecutive rows map to 8
+// distinct 16-byte bank groups (conflict-free LDS.128 across a quarter warp).
+constexpr int odd4(int n) {
+  return (((n + 3) & ~3) / 4) % 2 == 0 ? ((n + 3) & ~3) + 4 : ((n + 3) & ~3);
+}
+
+// Shared-memory row pitches.  FP64: the unpadded scalar layout.  Mixed:
+// padded rows read four entries at a time (float4).
+template <int N, typename Real>
+struct Pitch {
+  static constexpr bool MIXED = !std::is_same<Real, double>::value;
+  static constexpr int ROW = MIXED ? odd4(Shape<N>::NP) : Shape<N>::NP;
+  static constexpr int FROW = MIXED ? odd4(Shape<N>::NFPT) : Shape<N>::NFPT;
+};
+
 // Layout of the operator block in bytes, identical in global and shared memory.
+//   FP64:  W^T as Wt[r][j][i] (i fastest) | LIFT^T as Lt[fj][i]   (scalar reads)
+//   mixed: W as W[r][i][j] (j fastest, pitch ROW) | LIFT as L[i][fj] (pitch FROW)
 template <int N, typename Real>
 struct OpsLayout {
   static constexpr int NP = Shape<N>::NP, NFPT = Shape<N>::NFPT;
-  static constexpr int W = 0;                                      // Wt[r][j][i]
-  static constexpr int L = W + pad16(3 * NP * NP * (int)sizeof(Real));  // Lt[fj][i]
-  static constexpr int FN = L + pad16(NFPT * NP * (int)sizeof(Real));   // int32[fj]
+  static constexpr int RS = (int)sizeof(Real);
+  static constexpr bool MIXED = Pitch<N, Real>::MIXED;
+  static constexpr int W = 0;
+  static constexpr int L =
+      W + pad16((MIXED ? 3 * NP * Pitch<N, Real>::ROW : 3 * NP * NP) * RS);
+  static constexpr int FN =
+      L + pad16((MIXED ? NP * Pitch<N, Real>::FROW : NFPT * NP) * RS);
   static constexpr int SIZE = FN + pad16(NFPT * 4);
 };
 
@@ -105,11 +127,12 @@ struct Tile {
   static constexpr int E = kBlock / NP;
   static constexpr bool MIXED = !std::is_same<Real, double>::value;
   static constexpr int RS = (int)sizeof(Real);
+  static constexpr int ROW = Pitch<N, Real>::ROW, FROW = Pitch<N, Real>::FROW;
   static constexpr int Q = OpsLayout<N, Real>::SIZE;              // double
   static constexpr int QR = Q + pad16(NF * E * NP * 8);           // Real copy
-  static constexpr int AUX = QR + (MIXED ? pad16(NF * E * NP * RS) : 0);
-  static constexpr int FLUX = AUX + pad16(NAUX * E * NP * RS);
-  static constexpr int GEO = FLUX + pad16(NF * E * NFPT * RS);
+  static constexpr int AUX = QR + (MIXED ? pad16(NF * E * ROW * RS) : 0);
+  static constexpr int FLUX = AUX + pad16(NAUX * E * ROW * RS);
+  static constexpr int GEO = FLUX + pad16(NF * E * FROW * RS);
   static constexpr int FGEO = GEO + pad16(9 * E * RS);
   // mixed-precision Euler: FP64 pressure of every node of the tile
   static constexpr int PRES = FGEO + pad16(16 * E * RS);
@@ -127,6 +150,10 @@ __device__ __forceinline__ double rcp64_fast(double x) {
   return fma(r0, e, r0);
 }
 
+__device__ __forceinline__ float dot4(const float4 w, const float4 x, float acc) {
+  return fmaf(w.x, x.x, fmaf(w.y, x.y, fmaf(w.z, x.z, fmaf(w.w, x.w, acc))));
+}
+
 // double -> arithmetic type; the mixed path converts on the integer ALU
 template <typename Real>
 __device__ __forceinline__ Real to_real(double v) {
@@ -139,6 +166,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   using T = Tile<N, EQ, Real>;
   using Ops = OpsLayout<N, Real>;
   constexpr int NP = T::NP, NFPT = T::NFPT, NF = T::NF, E = T::E;
+  constexpr int ROW = T::ROW, FROW = T::FROW;  // shared-memory row pitches
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   __shared__ int ops_ok;
@@ -167,6 +195,12 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     }
     ops_ok = ok ? 1 : 0;
   }
+  if constexpr (T::MIXED) {
+    // padded rows are read by the vector loads: give the pads a value once
+    float* z = reinterpret_cast<float*>(smem + T::QR);
+    const int nz = (T::GEO - T::QR) / 4;
+    for (int idx = t; idx < nz; idx += kBlock) z[idx] = 0.0f;
+  }
   __syncthreads();
   if (!ops_ok) return;
 
@@ -192,7 +226,10 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         for (int rem = t; rem < E * NP; rem += kBlock) {
           const double v = rem < ecount * NP ? __ldg(qk + rem) : 0.0;
           sQ[k * (E * NP) + rem] = v;
-          if constexpr (T::MIXED) sQr[k * (E * NP) + rem] = to_real<Real>(v);
+          if constexpr (T::MIXED) {
+            const int le = rem / NP;
+            sQr[(k * E + le) * ROW + (rem - le * NP)] = to_real<Real>(v);
+          }
         }
       }
     }
@@ -211,12 +248,12 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     if constexpr (EQ == DG_WAVE) {
       if (active && el < ecount) {
         const Real* G = sG + el * 9;
-        const Real v0 = sQr[(1 * E + el) * NP + i];
-        const Real v1 = sQr[(2 * E + el) * NP + i];
-        const Real v2 = sQr[(3 * E + el) * NP + i];
+        const Real v0 = sQr[(1 * E + el) * ROW + i];
+        const Real v1 = sQr[(2 * E + el) * ROW + i];
+        const Real v2 = sQr[(3 * E + el) * ROW + i];
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-          sAux[(r * E + el) * NP + i] =
+          sAux[(r * E + el) * ROW + i] =
               fma(G[r * 3 + 0], v0, fma(G[r * 3 + 1], v1, G[r * 3 + 2] * v2));
       }
     } else if constexpr (EQ == DG_EULER) {
@@ -251,7 +288,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         for (int k = 0; k < 5; ++k)
 #pragma unroll
           for (int r = 0; r < 3; ++r)
-            sAux[((k * 3 + r) * E + el) * NP + i] =
+            sAux[((k * 3 + r) * E + el) * ROW + i] =
                 fma(G[r * 3 + 0], F[k][0],
                     fma(G[r * 3 + 1], F[k][1], G[r * 3 + 2] * F[k][2]));
       }
@@ -265,7 +302,69 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     for (int k = 0; k < NF; ++k) vol[k] = zero;
     if (active && el < ecount) {
       const Real* G = sG + el * 9;
-      if constexpr (EQ == DG_WAVE) {
+      if constexpr (T::MIXED) {
+        // float4 operands: four matrix entries per 16-byte shared load
+        const float4* w0v = reinterpret_cast<const float4*>(sW + (0 * NP + i) * ROW);
+        const float4* w1v = reinterpret_cast<const float4*>(sW + (1 * NP + i) * ROW);
+        const float4* w2v = reinterpret_cast<const float4*>(sW + (2 * NP + i) * ROW);
+        auto row = [&](const Real* base, int r) {
+          return reinterpret_cast<const float4*>(base + (r * E + el) * ROW);
+        };
+        if constexpr (EQ == DG_WAVE) {
+          const float4* uv = row(sQr, 0);
+          const float4 *a0 = row(sAux, 0), *a1 = row(sAux, 1), *a2 = row(sAux, 2);
+          float ur0 = 0.f, ur1 = 0.f, ur2 = 0.f, dv = 0.f;
+#pragma unroll
+          for (int jj = 0; jj < ROW / 4; ++jj) {
+            const float4 w0 = w0v[jj], w1 = w1v[jj], w2 = w2v[jj], u = uv[jj];
+            ur0 = dot4(w0, u, ur0);
+            ur1 = dot4(w1, u, ur1);
+            ur2 = dot4(w2, u, ur2);
+            dv = dot4(w0, a0[jj], dot4(w1, a1[jj], dot4(w2, a2[jj], dv)));
+          }
+          const Real c = p0;
+          vol[0] = -c * dv;
+#pragma unroll
+          for (int x = 0; x < 3; ++x)
+            vol[1 + x] = -c * fma(G[0 * 3 + x], ur0,
+                                  fma(G[1 * 3 + x], ur1, G[2 * 3 + x] * ur2));
+        } else if constexpr (EQ == DG_EULER) {
+#pragma unroll
+          for (int jj = 0; jj < ROW / 4; ++jj) {
+            const float4 w0 = w0v[jj], w1 = w1v[jj], w2 = w2v[jj];
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+              vol[k] = dot4(w0, row(sAux, k * 3 + 0)[jj],
+                            dot4(w1, row(sAux, k * 3 + 1)[jj],
+                                 dot4(w2, row(sAux, k * 3 + 2)[jj], vol[k])));
+          }
+        } else {  // DG_MAXWELL
+          float d[6][3];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) d[k][0] = d[k][1] = d[k][2] = 0.f;
+#pragma unroll
+          for (int jj = 0; jj < ROW / 4; ++jj) {
+            const float4 w0 = w0v[jj], w1 = w1v[jj], w2 = w2v[jj];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+              const float4 qv = row(sQr, k)[jj];
+              d[k][0] = dot4(w0, qv, d[k][0]);
+              d[k][1] = dot4(w1, qv, d[k][1]);
+              d[k][2] = dot4(w2, qv, d[k][2]);
+            }
+          }
+          auto dx = [&](int k, int x) {
+            return fma(G[0 * 3 + x], d[k][0],
+                       fma(G[1 * 3 + x], d[k][1], G[2 * 3 + x] * d[k][2]));
+          };
+          vol[0] = dx(5, 1) - dx(4, 2);
+          vol[1] = dx(3, 2) - dx(5, 0);
+          vol[2] = dx(4, 0) - dx(3, 1);
+          vol[3] = -(dx(2, 1) - dx(1, 2));
+          vol[4] = -(dx(0, 2) - dx(2, 0));
+          vol[5] = -(dx(1, 0) - dx(0, 1));
+        }
+      } else if constexpr (EQ == DG_WAVE) {
         const Real c = p0;
         const Real* u = sQr + el * NP;
         Real ur0 = zero, ur1 = zero, ur2 = zero, dv = zero;
@@ -355,7 +454,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       Real qi[NF], qe[NF];
       double qed[NF];
 #pragma unroll
-      for (int k = 0; k < NF; ++k) qi[k] = sQr[(k * E + elp) * NP + node];
+      for (int k = 0; k < NF; ++k) qi[k] = sQr[(k * E + elp) * ROW + node];
       if (!bdry) {
         const double* qk = a.q + gi;
 #pragma unroll
@@ -364,8 +463,8 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           qe[k] = to_real<Real>(qed[k]);
         }
       }
-      Real* out = sFlux + elp * NFPT + fj;
-      constexpr int FS = E * NFPT;  // field stride in sFlux
+      Real* out = sFlux + elp * FROW + fj;
+      constexpr int FS = E * FROW;  // field stride in sFlux
 
       if constexpr (EQ == DG_WAVE) {
         if (bdry) {  // Dirichlet mirror: exterior (-u, v)
@@ -493,14 +592,21 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
 
     // {{{ 5. LIFT, then store or fold into the RK stage
     if (active && el < ecount) {
-      const Real* fl = sFlux + el * NFPT;
+      const Real* fl = sFlux + el * FROW;
       int64_t gidx = e0 * NP + (el * NP + i);  // advanced by nelnp per field
 #pragma unroll
       for (int k = 0; k < NF; ++k, gidx += nelnp) {
         Real acc = vol[k];
+        if constexpr (T::MIXED) {
+          const float4* lv = reinterpret_cast<const float4*>(sL + i * FROW);
+          const float4* fv = reinterpret_cast<const float4*>(fl + k * E * FROW);
+#pragma unroll
+          for (int jj = 0; jj < FROW / 4; ++jj) acc = dot4(lv[jj], fv[jj], acc);
+        } else {
 #pragma unroll 4
-        for (int fj = 0; fj < NFPT; ++fj)
-          acc = fma(sL[fj * NP + i], fl[k * E * NFPT + fj], acc);
+          for (int fj = 0; fj < NFPT; ++fj)
+            acc = fma(sL[fj * NP + i], fl[k * E * NFPT + fj], acc);
+        }
         if constexpr (EQ == DG_MAXWELL) acc = acc / (k < 3 ? p1 : p2);
         double val;
         if constexpr (T::MIXED) val = f2d_alu(acc);

@@ -389,7 +389,7 @@ def our_arm(args) -> None:
         "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
         "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
         "traffic": traffic,
-        "kernel": f"dg_rhs_fp64_kernel<{rd['order']},{rd['eq']}>",
+        "kernel": f"dg_rhs_kernel<{rd['order']}, {rd['eq']}, {'double' if args.precision == 'fp64' else 'float'}, RHS>",
         "peak_source": peaks["source"],
         "fp64_pipe": {"achieved_tflops": fp64_achieved,
                       "peak_tflops": fp64_peak,
