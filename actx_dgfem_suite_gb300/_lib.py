@@ -30,6 +30,7 @@ DG_FP32_MIXED = 1
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
+                    "dg_box_mesh_build",
                     "dg_plan_info", "dg_fp64_fma_probe", "dg_last_error",
                     "dg_abi_version")
 
@@ -52,6 +53,27 @@ class MeshDesc(ctypes.Structure):
         ("lift", ctypes.c_void_p),
         ("face_nodes", ctypes.c_void_p),
         ("face_partner", ctypes.c_void_p),
+    ]
+
+
+class BoxDesc(ctypes.Structure):
+    _fields_ = [
+        ("order", ctypes.c_int32),
+        ("n", ctypes.c_int64 * 3),
+        ("a", ctypes.c_double * 3),
+        ("b", ctypes.c_double * 3),
+        ("corner", ctypes.c_void_p),
+        ("nbr", ctypes.c_void_p),
+        ("face_vert", ctypes.c_void_p),
+        ("face_opp", ctypes.c_void_p),
+        ("face_nodes", ctypes.c_void_p),
+        ("perm", ctypes.c_void_p),
+        ("bary", ctypes.c_void_p),
+        ("metric", ctypes.c_void_p),
+        ("face_geom", ctypes.c_void_p),
+        ("gather", ctypes.c_void_p),
+        ("face_partner", ctypes.c_void_p),
+        ("nodes", ctypes.c_void_p),
     ]
 
 
@@ -92,6 +114,8 @@ def lib() -> ctypes.CDLL:
     L.dg_rhs_adjoint.restype = ctypes.c_int
     L.dg_rhs_adjoint_noalloc.argtypes = [vp, vp, vp, vp]
     L.dg_rhs_adjoint_noalloc.restype = ctypes.c_int
+    L.dg_box_mesh_build.argtypes = [ctypes.POINTER(BoxDesc), vp]
+    L.dg_box_mesh_build.restype = ctypes.c_int
     L.dg_finish.argtypes = [vp, vp]
     L.dg_finish.restype = ctypes.c_int
     L.dg_plan_destroy.argtypes = [vp]

@@ -193,9 +193,11 @@ class GB300DGArrayContext:
         return f"GB300DGArrayContext(device={self.device})"
 
 
-def stacked_state(actx: GB300DGArrayContext, template: Any,
-                  fields: np.ndarray):
-    """Upload host fields (nfields, Nel, Np) as one device tensor and return
-    a container of views shaped like ``template``."""
-    dev = torch.from_numpy(np.ascontiguousarray(fields, dtype=np.float64)).to(actx.device)
+def stacked_state(actx: GB300DGArrayContext, template: Any, fields):
+    """Fields (nfields, Nel, Np) as one device tensor -- uploaded when given
+    on the host -- and a container of views shaped like ``template``."""
+    if isinstance(fields, torch.Tensor):
+        dev = fields.to(device=actx.device, dtype=torch.float64).contiguous()
+    else:
+        dev = torch.from_numpy(np.ascontiguousarray(fields, dtype=np.float64)).to(actx.device)
     return from_stacked(actx, template, dev)

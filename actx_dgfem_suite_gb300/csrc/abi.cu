@@ -21,6 +21,17 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+}  // namespace
+
+namespace dg {
+int set_error(int code, const char* msg) {
+  g_last_error = msg;
+  return code;
+}
+}  // namespace dg
+
+namespace {
+
 int cuda_fail(cudaError_t err, const char* what) {
   return fail(DG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(err));
 }

@@ -56,6 +56,10 @@ DG_DECLARE_EQ(euler)
 DG_DECLARE_EQ(maxwell)
 #undef DG_DECLARE_EQ
 
+// Record `msg` as the calling thread's last error (dg_last_error) and
+// return `code`; shared by the translation units behind the C ABI.
+int set_error(int code, const char* msg);
+
 // Adjoint of the FP64 wave RHS: shape of the volume kernel, and the two
 // launches (volume transpose + lifted face adjoints, then the per-node
 // transposed flux/gather); `nsm` caps the second grid.

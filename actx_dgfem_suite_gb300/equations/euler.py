@@ -20,46 +20,56 @@ import numpy as np
 from actx_dgfem_suite_gb300.discretization import make_box_discretization
 from actx_dgfem_suite_gb300.equations.common import Problem, make_rhs_and_args
 from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
+from actx_dgfem_suite_gb300.xp import array_module, r2, zeros
 
 GAMMA = 1.4
+#: box corners of each problem definition
+BOXES = {"reference": (-0.5, 0.5), "baseline": (-0.5, 0.5)}
 
 
-def acoustic_pulse_condition(nodes: np.ndarray, gamma: float = GAMMA) -> np.ndarray:
+def acoustic_pulse_condition(nodes, gamma: float = GAMMA):
     """``euler.py:119-137`` (gaussian_profile with rhoamp = 0 plus make_pulse
-    with width 0.1 at the origin); returns (5, Nel, Np)."""
-    r2 = (nodes**2).sum(axis=0)
-    mass = 0.0 * np.exp(1 - r2) + 1.0
+    with width 0.1 at the origin); returns (5, Nel, Np).  ``nodes``: (3, ...)
+    NumPy array or torch tensor."""
+    xp = array_module(nodes)
+    rr = r2(nodes)
+    mass = 0.0 * xp.exp(1 - rr) + 1.0
     energy = 1.0 / (gamma - 1.0) + 0.0 / (2.0 * mass)
-    pulse = np.exp(-0.5 * r2 / 0.1**2)
-    out = np.zeros((5,) + r2.shape)
+    pulse = xp.exp(-0.5 * rr / 0.1**2)
+    out = zeros(rr, (5,) + tuple(rr.shape))
     out[0] = mass
     out[1] = energy + pulse
     return out
 
 
-def density_pulse_condition(nodes: np.ndarray, gamma: float = GAMMA) -> np.ndarray:
-    r2 = (nodes**2).sum(axis=0)
-    rho = 1.0 + 0.1 * np.exp(-r2 / 0.2**2)
-    u = np.array([0.1, 0.0, 0.0])
+def density_pulse_condition(nodes, gamma: float = GAMMA):
+    xp = array_module(nodes)
+    rr = r2(nodes)
+    rho = 1.0 + 0.1 * xp.exp(-rr / 0.2**2)
+    u = (0.1, 0.0, 0.0)
     p = 1.0
-    out = np.zeros((5,) + r2.shape)
+    out = zeros(rr, (5,) + tuple(rr.shape))
     out[0] = rho
-    out[1] = p / (gamma - 1.0) + 0.5 * rho * (u**2).sum()
+    out[1] = p / (gamma - 1.0) + 0.5 * rho * sum(c * c for c in u)
     for i in range(3):
         out[2 + i] = rho * u[i]
     return out
 
 
+def initial_state(nodes, definition: str, gamma: float = GAMMA):
+    if definition == "reference":
+        return acoustic_pulse_condition(nodes, gamma)
+    if definition == "baseline":
+        return density_pulse_condition(nodes, gamma)
+    raise ValueError(f"unknown problem definition {definition!r}")
+
+
 def euler_problem(order: int, nel_1d: int, definition: str = "reference",
                   gamma: float = GAMMA) -> Problem:
-    disc = make_box_discretization(order, nel_1d, -0.5, 0.5)
-    nodes = disc.nodes()
-    if definition == "reference":
-        fields = acoustic_pulse_condition(nodes, gamma)
-    elif definition == "baseline":
-        fields = density_pulse_condition(nodes, gamma)
-    else:
+    if definition not in BOXES:
         raise ValueError(f"unknown problem definition {definition!r}")
+    disc = make_box_discretization(order, nel_1d, *BOXES[definition])
+    fields = initial_state(disc.nodes(), definition, gamma)
     return Problem("euler", disc, fields, (float(gamma),), 0.5, definition)
 
 

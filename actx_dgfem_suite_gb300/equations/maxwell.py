@@ -21,6 +21,11 @@ import numpy as np
 from actx_dgfem_suite_gb300.discretization import make_box_discretization
 from actx_dgfem_suite_gb300.equations.common import Problem, make_rhs_and_args
 from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
+from actx_dgfem_suite_gb300.xp import array_module, zeros
+
+#: flux parameter alpha of each problem definition, box [0, 1]^3 for both
+ALPHA = {"reference": 0.5, "baseline": 1.0}
+BOXES = {"reference": (0.0, 1.0), "baseline": (0.0, 1.0)}
 
 
 def rectangular_cavity_mode(nodes: np.ndarray, t: float = 0.0,
@@ -45,11 +50,30 @@ def rectangular_cavity_mode(nodes: np.ndarray, t: float = 0.0,
     ])
 
 
-def plane_wave_mix(nodes: np.ndarray, seed: int = 0, nwaves: int = 8) -> np.ndarray:
+def cavity_mode_real_t0(nodes, mode=(1, 2, 2)):
+    """Real part of :func:`rectangular_cavity_mode` at t = 0: (E, 0), for
+    NumPy arrays or torch tensors."""
+    xp = array_module(nodes)
+    kx, ky, kz = (m * np.pi for m in mode)
+    x, y, z = nodes[0], nodes[1], nodes[2]
+    sx, cx = xp.sin(kx * x), xp.cos(kx * x)
+    sy, cy = xp.sin(ky * y), xp.cos(ky * y)
+    sz, cz = xp.sin(kz * z), xp.cos(kz * z)
+    g2 = kx**2 + ky**2
+    out = zeros(x, (6,) + tuple(x.shape))
+    out[0] = -kx * kz * cx * sy * sz / g2
+    out[1] = -ky * kz * sx * cy * sz / g2
+    out[2] = sx * sy * cz
+    return out
+
+
+def plane_wave_mix(nodes, seed: int = 0, nwaves: int = 8):
     """Sum of vacuum plane waves E = a e cos(k.x + phi), H = a (k^ x e)
-    cos(k.x + phi), |k| in 2 pi [1, 3], from a fixed seed."""
+    cos(k.x + phi), |k| in 2 pi [1, 3], from a fixed seed (parameters drawn
+    on the host; ``nodes`` may be a NumPy array or a torch tensor)."""
+    xp = array_module(nodes)
     rng = np.random.default_rng(seed)
-    out = np.zeros((6,) + nodes.shape[1:])
+    out = zeros(nodes, (6,) + tuple(nodes.shape[1:]))
     for _ in range(nwaves):
         khat = rng.normal(size=3)
         khat /= np.linalg.norm(khat)
@@ -59,8 +83,9 @@ def plane_wave_mix(nodes: np.ndarray, seed: int = 0, nwaves: int = 8) -> np.ndar
         kmag = 2 * np.pi * rng.uniform(1.0, 3.0)
         amp = rng.uniform(0.5, 1.0)
         phase = rng.uniform(0.0, 2 * np.pi)
-        arg = kmag * np.tensordot(khat, nodes, axes=(0, 0)) + phase
-        c = amp * np.cos(arg)
+        arg = kmag * (khat[0] * nodes[0] + khat[1] * nodes[1]
+                      + khat[2] * nodes[2]) + phase
+        c = amp * xp.cos(arg)
         for i in range(3):
             out[i] += e[i] * c
             out[3 + i] += h[i] * c
@@ -69,18 +94,20 @@ def plane_wave_mix(nodes: np.ndarray, seed: int = 0, nwaves: int = 8) -> np.ndar
 
 def maxwell_problem(order: int, nel_1d: int, definition: str = "reference",
                     epsilon: float = 1.0, mu: float = 1.0, seed: int = 0) -> Problem:
-    disc = make_box_discretization(order, nel_1d, 0.0, 1.0)
-    nodes = disc.nodes()
-    if definition == "reference":
-        fields = np.real(rectangular_cavity_mode(nodes, 0.0)).copy()
-        alpha = 0.5
-    elif definition == "baseline":
-        fields = plane_wave_mix(nodes, seed=seed)
-        alpha = 1.0
-    else:
+    if definition not in ALPHA:
         raise ValueError(f"unknown problem definition {definition!r}")
-    return Problem("maxwell", disc, fields, (alpha, float(epsilon), float(mu)),
-                   0.5, definition)
+    disc = make_box_discretization(order, nel_1d, 0.0, 1.0)
+    fields = initial_state(disc.nodes(), definition, seed)
+    return Problem("maxwell", disc, fields,
+                   (ALPHA[definition], float(epsilon), float(mu)), 0.5, definition)
+
+
+def initial_state(nodes, definition: str, seed: int = 0):
+    if definition == "reference":
+        return cavity_mode_real_t0(nodes)
+    if definition == "baseline":
+        return plane_wave_mix(nodes, seed=seed)
+    raise ValueError(f"unknown problem definition {definition!r}")
 
 
 def get_maxwell_rhs(*, actx, dim: int, order: int, ndofs: int,

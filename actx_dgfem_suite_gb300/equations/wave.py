@@ -16,38 +16,52 @@ Problem definitions:
 
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from actx_dgfem_suite_gb300.discretization import make_box_discretization
 from actx_dgfem_suite_gb300.equations.common import Problem, make_rhs_and_args
 from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
+from actx_dgfem_suite_gb300.xp import array_module, r2, zeros
 
 DEFINITIONS = ("reference", "baseline")
+#: box corners of each problem definition
+BOXES = {"reference": (-0.5, 0.5), "baseline": (-1.0, 1.0)}
 
 
-def bump(nodes: np.ndarray, t: float = 0.0) -> np.ndarray:
-    """``wave.py:216-236``: cos(3 t) exp(-|x - c|^2 / w^2)."""
-    center = np.array([0.2, 0.35, 0.1])
+def bump(nodes, t: float = 0.0):
+    """``wave.py:216-236``: cos(3 t) exp(-|x - c|^2 / w^2).  ``nodes``: (3, ...)
+    NumPy array or torch tensor."""
+    center = (0.2, 0.35, 0.1)
     width = 0.05
     omega = 3.0
-    d2 = sum((nodes[i] - center[i]) ** 2 for i in range(3))
-    return np.cos(omega * t) * np.exp(-d2 / width**2)
+    return math.cos(omega * t) * array_module(nodes).exp(-r2(nodes, center) / width**2)
+
+
+def gaussian_pulse(nodes, width: float = 0.1):
+    """exp(-|x|^2 / width^2), the benchmark pressure pulse."""
+    return array_module(nodes).exp(-r2(nodes) / width**2)
+
+
+def initial_state(nodes, definition: str):
+    """(4, Nel, Np) wave state of a problem definition at the given nodes."""
+    if definition == "reference":
+        u = bump(nodes)
+    elif definition == "baseline":
+        u = gaussian_pulse(nodes)
+    else:
+        raise ValueError(f"unknown problem definition {definition!r}")
+    fields = zeros(u, (4,) + tuple(u.shape))
+    fields[0] = u
+    return fields
 
 
 def wave_problem(order: int, nel_1d: int, definition: str = "reference",
                  c: float = 1.0) -> Problem:
-    if definition == "reference":
-        disc = make_box_discretization(order, nel_1d, -0.5, 0.5)
-        nodes = disc.nodes()
-        u = bump(nodes)
-    elif definition == "baseline":
-        disc = make_box_discretization(order, nel_1d, -1.0, 1.0)
-        nodes = disc.nodes()
-        u = np.exp(-(nodes**2).sum(axis=0) / 0.1**2)
-    else:
-        raise ValueError(f"unknown problem definition {definition!r}")
-    fields = np.zeros((4,) + u.shape)
-    fields[0] = u
+    a, b = BOXES[definition]
+    disc = make_box_discretization(order, nel_1d, a, b)
+    fields = initial_state(disc.nodes(), definition)
     return Problem("wave", disc, fields, (float(c),), None, definition)
 
 

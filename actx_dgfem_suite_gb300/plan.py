@@ -40,14 +40,24 @@ class DeviceMesh:
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
         self.device = dev
-        self.metric = torch.from_numpy(disc.metric_flat()).to(self.device)
-        self.face_geom = torch.from_numpy(
-            np.ascontiguousarray(disc.face_geometry())).to(self.device)
-        self.gather = torch.from_numpy(
-            disc.gather_index().view(np.int32)).to(self.device)
-        # glued face-point index, needed only by the adjoint
-        self.partner = (torch.from_numpy(disc.face_partner()).to(self.device)
-                        if with_partner else None)
+        if isinstance(getattr(disc, "metric", None), torch.Tensor):
+            # built on the device (device_setup.DeviceBoxDiscretization)
+            if disc.metric.device != dev:
+                raise ValueError("device-built mesh lives on another device")
+            self.metric, self.face_geom, self.gather = (
+                disc.metric, disc.face_geom, disc.gather)
+            self.partner = disc.partner
+            if with_partner and self.partner is None:
+                raise ValueError("device mesh was built without face partners")
+        else:
+            self.metric = torch.from_numpy(disc.metric_flat()).to(self.device)
+            self.face_geom = torch.from_numpy(
+                np.ascontiguousarray(disc.face_geometry())).to(self.device)
+            self.gather = torch.from_numpy(
+                disc.gather_index().view(np.int32)).to(self.device)
+            # glued face-point index, needed only by the adjoint
+            self.partner = (torch.from_numpy(disc.face_partner()).to(self.device)
+                            if with_partner else None)
         ref = disc.ref
         self._weak = np.ascontiguousarray(ref.weak_diff, dtype=np.float64)
         self._strong = np.ascontiguousarray(ref.diff, dtype=np.float64)

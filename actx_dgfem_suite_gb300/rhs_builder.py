@@ -25,10 +25,24 @@ def split_equation_name(equation: str) -> tuple[str, int]:
 
 
 def get_rhs(equation: str, actx, dim: int, degree: int, *,
-            definition: str = "reference",
-            nel_1d: int | None = None) -> tuple[Any, tuple[Any, ...]]:
-    """Return ``(rhs_callable, call_args)`` for ``equation``."""
+            definition: str = "reference", nel_1d: int | None = None,
+            device_setup: bool = False) -> tuple[Any, tuple[Any, ...]]:
+    """Return ``(rhs_callable, call_args)`` for ``equation``.
+
+    ``device_setup=True`` builds the box mesh, geometry, connectivity and
+    initial state on the array context's GPU instead of on the host."""
     base, ndofs = split_equation_name(equation)
+    if device_setup:
+        from actx_dgfem_suite_gb300.device_setup import device_problem
+        from actx_dgfem_suite_gb300.equations.common import make_rhs_and_args
+        from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
+        if dim != 3:
+            raise NotImplementedError("only 3D tetrahedral meshes are implemented")
+        if base not in ("wave", "euler", "maxwell"):
+            raise NotImplementedError(f"equation '{equation}' not supported")
+        n = nel_1d or get_nel_1d_for_regular_rect_mesh(dim, degree, ndofs)
+        return make_rhs_and_args(device_problem(base, degree, n, definition,
+                                                actx.device), actx)
     kw = dict(actx=actx, dim=dim, order=degree, ndofs=ndofs,
               definition=definition, nel_1d=nel_1d)
     if base == "wave":

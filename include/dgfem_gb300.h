@@ -145,6 +145,33 @@ int dg_rhs_adjoint_noalloc(dg_plan* plan, const double* x, double* y,
  * Replaces finish_command_queue(actx) (actx_dgfem_suite/measure.py:48-55). */
 int dg_finish(dg_plan* plan, void* stream);
 
+/* Box mesh built on the device: the 6 n[0] n[1] n[2] tetrahedra of the box
+ * [a, b] (hexahedra in C order, six tetrahedra each), written straight into
+ * the plan's input arrays.  Replaces the host-side mesh generation and
+ * connectivity of the suite's builders (generate_regular_rect_mesh and
+ * DiscretizationCollection, actx_dgfem_suite/equations/wave.py:250-270).
+ * The small tables describe the hexahedron split and the reference element;
+ * the host derives them once (see actx_dgfem_suite_gb300/device_setup.py). */
+typedef struct dg_box_desc {
+  int32_t order;                /* 1..4 */
+  int64_t n[3];                 /* hexahedra per axis */
+  double a[3], b[3];            /* box corners, b > a */
+  const int32_t* corner;        /* host (6, 4, 3): corner offsets of each tet */
+  const int32_t* nbr;           /* host (6, 4, 6): di, dj, dk, tet', face', perm */
+  const int32_t* face_vert;     /* host (4, 3) */
+  const int32_t* face_opp;      /* host (4) */
+  const int32_t* face_nodes;    /* host (4, Nfp) */
+  const int32_t* perm;          /* host (6, Nfp) */
+  const double* bary;           /* host (Np, 4) */
+  double* metric;               /* device out (Nel, 3, 3) */
+  double* face_geom;            /* device out (Nel, 4, 4) */
+  uint32_t* gather;             /* device out (Nel, 4, Nfp) */
+  int32_t* face_partner;        /* device out (Nel, 4, Nfp), optional */
+  double* nodes;                /* device out (3, Nel, Np), optional */
+} dg_box_desc;
+
+int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
+
 /* Release the plan's device buffers.  Replaces dropping the compiled program
  * and freeing the memory pool (actx_dgfem_suite/tools/wave_dof_scaling.py:108-126). */
 int dg_plan_destroy(dg_plan* plan);
