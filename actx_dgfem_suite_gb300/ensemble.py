@@ -24,9 +24,13 @@ from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
 class Ensemble:
     """``rhs(q)`` for all members at once; ``q`` is (nfields, sum Nel, Np)."""
 
-    def __init__(self, discs: list[DGDiscretization], equation: str, params,
+    def __init__(self, discs: list, equation: str, params,
                  precision: str = "fp32-mixed", device=None):
-        self.union, self.offsets = union_discretization(discs)
+        if isinstance(getattr(discs[0], "metric", None), torch.Tensor):
+            from actx_dgfem_suite_gb300.device_setup import device_union
+            self.union, self.offsets = device_union(discs)   # built on the GPU
+        else:
+            self.union, self.offsets = union_discretization(discs)
         self.nmembers = len(discs)
         self.mesh = DeviceMesh(self.union, device)
         self.plan = DevicePlan(self.mesh, equation, params, precision)
@@ -42,9 +46,11 @@ class Ensemble:
         """View of member ``k`` in an ensemble-shaped tensor."""
         return x[:, int(self.offsets[k]):int(self.offsets[k + 1]), :]
 
-    def stack_states(self, states: list[np.ndarray]) -> torch.Tensor:
+    def stack_states(self, states: list) -> torch.Tensor:
         if len(states) != self.nmembers:
             raise ValueError("one state per member expected")
+        if isinstance(states[0], torch.Tensor):
+            return torch.cat([s.to(self.mesh.device) for s in states], dim=1).contiguous()
         return torch.from_numpy(np.concatenate(states, axis=1)).to(self.mesh.device)
 
     def rhs(self, q: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:

@@ -19,7 +19,8 @@ import json
 
 
 def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
-        reps: int = 10, seed: int = 0, precision: str = "fp32-mixed") -> dict:
+        reps: int = 10, seed: int = 0, precision: str = "fp32-mixed",
+        device_setup: bool = True) -> dict:
     import time
 
     import numpy as np
@@ -35,8 +36,14 @@ def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
     sizes = random_box_sizes(members, lo, hi, seed)
     order_of_build = sorted(range(members), key=lambda k: sizes[k])
     probs = [None] * members
-    for k in order_of_build:          # equal sizes consecutively: mesh cache hits
-        probs[k] = maxwell_problem(order, sizes[k], "baseline", seed=seed + 1 + k)
+    if device_setup:
+        from actx_dgfem_suite_gb300.device_setup import device_problem
+        for k in range(members):
+            probs[k] = device_problem("maxwell", order, sizes[k], "baseline",
+                                      seed=seed + 1 + k)
+    else:
+        for k in order_of_build:      # equal sizes consecutively: mesh cache hits
+            probs[k] = maxwell_problem(order, sizes[k], "baseline", seed=seed + 1 + k)
     clear_box_cache()
     ens = Ensemble([p.disc for p in probs], "maxwell", probs[0].params, precision)
     q = ens.stack_states([p.fields for p in probs])
@@ -45,11 +52,13 @@ def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
     for p in probs:
         plan = DevicePlan(DeviceMesh(p.disc), "maxwell", p.params, "fp64")
         member_plans.append(plan)
-        qq = torch.from_numpy(p.fields).cuda()
+        qq = (p.fields if isinstance(p.fields, torch.Tensor)
+              else torch.from_numpy(p.fields)).cuda()
         member_q.append(qq)
         member_out.append(torch.empty_like(qq))
     for p in probs:
-        p.disc._cache.clear()
+        if hasattr(p.disc, "_cache"):
+            p.disc._cache.clear()
     setup_s = time.perf_counter() - t0
 
     ens.capture(q, out)

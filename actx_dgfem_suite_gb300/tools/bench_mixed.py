@@ -28,14 +28,19 @@ def run(n: int = 56, order: int = 3, nsteps: int = 100, cfl: float = 0.5,
     from actx_dgfem_suite_gb300.timestepping import LSRK45, estimate_rk4_timestep
 
     if problem is None:
-        problem = get_problem("euler", 3, order, definition="baseline", nel_1d=n)
+        try:
+            from actx_dgfem_suite_gb300.device_setup import device_problem
+            problem = device_problem("euler", order, n, "baseline", device)
+        except Exception:
+            problem = get_problem("euler", 3, order, definition="baseline", nel_1d=n)
     disc = problem.disc
     mesh = DeviceMesh(disc, device)
     plans = {p: DevicePlan(mesh, "euler", problem.params, p)
              for p in ("fp64", "fp32-mixed")}
     # max wave speed of the benchmark state ~ |u| + c = 0.1 + sqrt(1.4) < 1.3
     dt = estimate_rk4_timestep(disc, 1.3, cfl)
-    q0 = torch.from_numpy(problem.fields).to(mesh.device)
+    q0 = (problem.fields if isinstance(problem.fields, torch.Tensor)
+          else torch.from_numpy(problem.fields)).to(mesh.device)
     qs = {p: q0.clone() for p in plans}
     integ = {p: LSRK45(plans[p], dt) for p in plans}
     # warm-up: one stage each, on scratch copies

@@ -245,6 +245,70 @@ def reference_arm(args) -> None:
 # }}}
 
 
+def run_extras(args, runs, actx, K, fp64_ms_per_step) -> dict:
+    """The three forms built beside the plain FP64 path, each measured on its
+    own benchmark configuration: mixed precision (the same 12-case sweep with
+    FP32 arithmetic, and Euler P3 n=56 over 100 LSRK45 steps), the 64-member
+    Maxwell ensemble, and the wave adjoint (gradient checked by finite
+    differences).  Each entry reports its error against FP64."""
+    import torch
+
+    out = {}
+    # {{{ mixed-precision sweep on the resident states
+    try:
+        stream = torch.cuda.current_stream()
+        plans = []
+        for r in runs:
+            op = r["compiled"].op
+            op.precision = "fp32-mixed"
+            plans.append(op.plan_for(actx))
+            op.precision = "fp64"
+        outs = [torch.empty_like(r["q"]) for r in runs]
+        for _ in range(2):
+            for p, r, o in zip(plans, runs, outs):
+                p.rhs(r["q"], o)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(True), torch.cuda.Event(True)) for _ in runs]
+        times = [0.0] * len(runs)
+        for _ in range(K):
+            for k, (p, r, o) in enumerate(zip(plans, runs, outs)):
+                ev[k][0].record(stream)
+                p.rhs(r["q"], o)
+                ev[k][1].record(stream)
+            torch.cuda.synchronize()
+            for k in range(len(runs)):
+                times[k] += ev[k][0].elapsed_time(ev[k][1]) / K
+        errs = [float(torch.linalg.norm(o - r["out"]) / torch.linalg.norm(r["out"]))
+                for o, r in zip(outs, runs)]
+        dofs = sum(r["cost"].dofs for r in runs)
+        out["mixed_precision_sweep"] = {
+            "value": dofs / (sum(times) * 1e-3), "unit": UNIT,
+            "ms_per_step": sum(times),
+            "speedup_vs_fp64": fp64_ms_per_step / sum(times),
+            "max_rel_l2_err_vs_fp64": max(errs),
+            "cases_ms": {f"{r['eq']}{r['order']}": t for r, t in zip(runs, times)},
+        }
+        del outs
+    except Exception as exc:  # report, keep the main line
+        out["mixed_precision_sweep"] = {"error": repr(exc)}
+    # }}}
+    for name, mod, kw in (
+            ("mixed_precision_euler_p3_lsrk45", "bench_mixed", {}),
+            ("ensemble_maxwell_p3_64", "bench_ensemble", {"reps": 5}),
+            ("adjoint_wave_p3", "bench_adjoint", {})):
+        try:
+            import importlib
+            m = importlib.import_module(f"actx_dgfem_suite_gb300.tools.{mod}")
+            res = m.run(**kw)
+            res.pop("err_per_step", None)
+            res.pop("member_sizes", None)
+            out[name] = res
+        except Exception as exc:
+            out[name] = {"error": repr(exc)}
+        torch.cuda.empty_cache()
+    return out
+
+
 def our_arm(args) -> None:
     import numpy as np
     import torch
@@ -410,6 +474,10 @@ def our_arm(args) -> None:
                "sample": (f"CPU FP64 oracle, every case at n // {args.cpu_scale}, "
                           f"one process per case")}
 
+    extras = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras = run_extras(args, runs, actx, K, ms_step)
+
     per_case = [{"case": f"{r['eq']} P{r['order']} n={r['n']}",
                  "nel": r["cost"].nelements, "ms": case_ms[k],
                  "gdof_s": r["cost"].dofs / case_ms[k] / 1e6,
@@ -438,6 +506,7 @@ def our_arm(args) -> None:
             "gpu_launches": len(runs) * K,
             "setup_s": setup_s,
             "cases": per_case,
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -456,6 +525,8 @@ def main(argv=None):
                     help="CPU sample: every case at n // cpu-scale")
     ap.add_argument("--cases", default="", help="subset, e.g. wave3,euler4")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the mixed-precision, ensemble and adjoint extras")
     ap.add_argument("--host-setup", action="store_true",
                     help="build meshes on the host (NumPy) instead of on the GPU")
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32-mixed"),
