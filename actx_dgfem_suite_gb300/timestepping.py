@@ -42,15 +42,19 @@ def estimate_rk4_timestep(disc: DGDiscretization, c: float = 1.0,
     the wave speed ``c``.  Plays the role of grudge's
     ``characteristic_lengthscales`` / ``nodal_min`` used by
     ``actx_dgfem_suite/equations/wave.py:206-213`` (the constants differ)."""
-    ev = disc.mesh.vertices[disc.mesh.elements]
-    vol = disc.jac * (4.0 / 3.0)
-    area = 2.0 * disc.face_jac.sum(axis=1)
-    inradius = 3.0 * vol / area
+    # inradius = 3 vol / area = 2 / sum_f (sJ_f / J) on the biunit tetrahedron
+    # (reference volume 4/3, reference face area 2); works for host meshes
+    # and for device-built ones, whose face geometry holds sJ/J directly
+    fg = getattr(disc, "face_geom", None)
+    if isinstance(fg, torch.Tensor):
+        ratio_sum = float(fg[:, :, 3].sum(dim=1).max())
+    else:
+        ratio_sum = float((disc.face_jac / disc.jac[:, None]).sum(axis=1).max())
+    inradius_min = 2.0 / ratio_sum
     x = disc.ref.nodes
     d = np.linalg.norm(x[:, None, :] - x[None, :, :], axis=2)
     dmin = d[d > 0].min() / 2.0       # biunit element: edge length 2
-    del ev
-    return float(cfl * inradius.min() * dmin / c)
+    return float(cfl * inradius_min * dmin / c)
 
 
 class LSRK45:

@@ -91,7 +91,7 @@ def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
                      f"{nrec} receivers, c_e ~ U[0.8,1.2]"),
         "nelements": d.nelements,
         "dt": dt,
-        "loss": float(J),
+        "loss": float(J.detach()),
         "forward_ms_per_step": 1e3 * t_fwd / nsteps,
         "adjoint_ms_per_step": 1e3 * t_bwd / nsteps,
         "adjoint_over_forward": t_bwd / t_fwd,

@@ -70,3 +70,16 @@ def test_get_rhs_device_setup_through_actx(actx):
     o1 = np.stack([d[0] for d in leaves(actx.to_numpy(actx.compile(r1)(*a1)))])
     o2 = np.stack([d[0] for d in leaves(actx.to_numpy(actx.compile(r2)(*a2)))])
     assert np.linalg.norm(o1 - o2) <= 1e-13 * np.linalg.norm(o1)
+
+
+def test_timestep_estimate_device_mesh_matches_host():
+    from actx_dgfem_suite_gb300.device_setup import DeviceBoxDiscretization
+    from actx_dgfem_suite_gb300.discretization import make_discretization
+    from actx_dgfem_suite_gb300.mesh import generate_box_tet_mesh
+    from actx_dgfem_suite_gb300.timestepping import estimate_rk4_timestep
+    n, a, b = (3, 2, 4), (-1.0, 0.0, 0.5), (1.0, 0.5, 2.0)
+    host = make_discretization(generate_box_tet_mesh(a, b, n), 3)
+    dev = DeviceBoxDiscretization(3, n, a, b, "cuda:0")
+    dt_h = estimate_rk4_timestep(host, 1.3, 0.5)
+    dt_d = estimate_rk4_timestep(dev, 1.3, 0.5)
+    assert abs(dt_d - dt_h) <= 1e-13 * dt_h
