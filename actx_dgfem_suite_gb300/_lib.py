@@ -31,7 +31,8 @@ EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
                     "dg_box_mesh_build",
-                    "dg_plan_info", "dg_fp64_fma_probe", "dg_last_error",
+                    "dg_plan_path", "dg_plan_info", "dg_fp64_fma_probe",
+                    "dg_last_error",
                     "dg_abi_version")
 
 
@@ -124,6 +125,8 @@ def lib() -> ctypes.CDLL:
     L.dg_plan_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), i32p, i32p,
                                i32p, i32p, i32p]
     L.dg_plan_info.restype = ctypes.c_int
+    L.dg_plan_path.argtypes = [vp, i32p, i32p, ctypes.POINTER(ctypes.c_int64)]
+    L.dg_plan_path.restype = ctypes.c_int
     L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, vp]
     L.dg_fp64_fma_probe.restype = ctypes.c_int

@@ -1,6 +1,7 @@
 // C ABI of the DG-FEM RHS evaluator (declared in include/dgfem_gb300.h).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -9,6 +10,7 @@
 
 #include "../../include/dgfem_gb300.h"
 #include "dg_adjoint.cuh"  // AdjArgs, AdjOpsLayout
+#include "dg_face.cuh"     // FaceArgs
 #include "dg_launch.h"
 #include "dg_rhs.cuh"  // RhsArgs, kBlock
 
@@ -57,6 +59,25 @@ cudaError_t shape_of(int eq, int order, int precision, int mode,
   }
 }
 
+cudaError_t face_blocks_of(int eq, int order, int* blocks_per_sm) {
+  switch (eq) {
+    case DG_WAVE: return dg::face_blocks_wave(order, blocks_per_sm);
+    case DG_EULER: return dg::face_blocks_euler(order, blocks_per_sm);
+    case DG_MAXWELL: return dg::face_blocks_maxwell(order, blocks_per_sm);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t face_launch_of(int eq, int order, const dg::FaceArgs& a, int grid,
+                           int aux_grid, cudaStream_t s) {
+  switch (eq) {
+    case DG_WAVE: return dg::face_launch_wave(order, a, grid, aux_grid, s);
+    case DG_EULER: return dg::face_launch_euler(order, a, grid, aux_grid, s);
+    case DG_MAXWELL: return dg::face_launch_maxwell(order, a, grid, aux_grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_of(int eq, int order, int precision, int mode,
                       const dg::RhsArgs& a, int grid, cudaStream_t s) {
   switch (eq) {
@@ -80,13 +101,15 @@ bool overlap2(const void* a, int64_t na, const void* b, int64_t nb) {
   return x < y + nb && y < x + na;
 }
 
-__global__ void fp64_fma_probe_kernel(double* out, int64_t iters) {
+__global__ void fp64_fma_probe_kernel(double* out, int iters) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double v[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = 1.0 + 1e-9 * (double)(tid + k);
   const double b = 0.9999999, c = 1e-7;
-  for (int64_t it = 0; it < iters; ++it) {
+  // 32-bit trip count, unrolled: the loop overhead stays off the timed pipe
+#pragma unroll 4
+  for (int it = 0; it < iters; ++it) {
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = fma(v[k], b, c);
   }
@@ -116,7 +139,16 @@ struct dg_plan {
   int device = 0;
   int nsm = 0;
   const double* elem_scale = nullptr;
-  // adjoint (wave, FP64, when the mesh carries face_partner)
+  double k[6] = {0, 0, 0, 0, 0, 0};  // derived constants (see RhsArgs::k)
+  // face-shared path (FP64, when the mesh carries face_partner)
+  bool split = false;
+  int32_t* d_owned = nullptr;  // owned faces e * 4 + f
+  int64_t nowned = 0;
+  double* d_flux = nullptr;    // (NF, Nel, 4 Nfp)
+  double* d_aux = nullptr;     // euler: (3, Nel, Np)
+  int face_grid = 0, aux_grid = 0;
+  const int32_t* d_face_nodes = nullptr;  // inside d_ops
+  // face-shared path and adjoint (wave, FP64): the mesh's face_partner
   const int32_t* face_partner = nullptr;
   void* d_adj_ops = nullptr;
   uint32_t adj_ops_bytes = 0;
@@ -138,8 +170,130 @@ dg::RhsArgs base_args(const dg_plan* p) {
   a.p0 = p->params[0];
   a.p1 = p->params[1];
   a.p2 = p->params[2];
+  for (int k = 0; k < 6; ++k) a.k[k] = p->k[k];
   a.elem_scale = p->elem_scale;
+  a.flux_in = p->split ? p->d_flux : nullptr;
+  a.aux = p->split ? p->d_aux : nullptr;
   return a;
+}
+
+// Ownership of every face for the face-shared path, with a consistency
+// check of face_partner: owned[face] = 1 for a boundary face and for the
+// lower-numbered face of a glued pair.  *bad is set unless every interior
+// face point's partner lies on one other face, maps back to it, and is the
+// face point whose volume node the gather index names.
+__global__ void face_owner_kernel(const uint32_t* gather, const int32_t* partner,
+                                  const int32_t* face_nodes, int np, int nfp,
+                                  int64_t nel, uint8_t* owned, int* bad) {
+  const int64_t nfaces = nel * 4;
+  const int64_t nfp_all = nfaces * nfp;
+  for (int64_t face = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; face < nfaces;
+       face += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t fp0 = face * nfp;
+    const bool bdry = (gather[fp0] >> 31) != 0u;
+    int64_t pface = -1;
+    bool ok = true;
+    for (int j = 0; j < nfp && ok; ++j) {
+      const uint32_t g = gather[fp0 + j];
+      const int32_t pp = partner[fp0 + j];
+      if (((g >> 31) != 0u) != bdry) {
+        ok = false;
+      } else if (bdry) {
+        ok = pp == -1;
+      } else if (pp < 0 || pp >= nfp_all) {
+        ok = false;
+      } else {
+        const int64_t pf = pp / nfp;
+        if (j == 0) pface = pf;
+        const int64_t e2 = pp / (4 * nfp);
+        const int fj2 = (int)(pp - e2 * 4 * nfp);
+        ok = pf == pface && pf != face && partner[pp] == fp0 + j &&
+             (int64_t)(g & 0x7fffffffu) == e2 * np + face_nodes[fj2];
+      }
+    }
+    if (!ok) atomicExch(bad, 1);
+    owned[face] = (ok && (bdry || face < pface)) ? 1 : 0;
+  }
+}
+
+// Build the owned-face list and the buffers of the face-shared path.
+int setup_split(dg_plan* p, const int32_t* partner, const int32_t* d_face_nodes) {
+  const int64_t nfaces = p->nel * 4;
+  uint8_t* d_mask = nullptr;
+  int* d_bad = nullptr;
+  cudaError_t err = cudaMalloc(&d_mask, nfaces);
+  if (err == cudaSuccess) err = cudaMalloc(&d_bad, sizeof(int));
+  if (err == cudaSuccess) err = cudaMemset(d_bad, 0, sizeof(int));
+  if (err == cudaSuccess) {
+    const int64_t blocks = (nfaces + 255) / 256;
+    const int grid = (int)(blocks < (int64_t)p->nsm * 16 ? blocks : (int64_t)p->nsm * 16);
+    face_owner_kernel<<<grid, 256>>>(p->gather, partner, d_face_nodes, p->np, p->nfp,
+                                     p->nel, d_mask, d_bad);
+    err = cudaGetLastError();
+  }
+  std::vector<uint8_t> mask;
+  int bad = 0;
+  if (err == cudaSuccess) {
+    mask.resize(nfaces);
+    err = cudaMemcpy(mask.data(), d_mask, nfaces, cudaMemcpyDeviceToHost);
+  }
+  if (err == cudaSuccess) err = cudaMemcpy(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost);
+  if (d_mask) cudaFree(d_mask);
+  if (d_bad) cudaFree(d_bad);
+  if (err != cudaSuccess) return cuda_fail(err, "face ownership");
+  if (bad)
+    return fail(DG_ERR_ARGUMENT,
+                "face_partner is not a pairing of whole faces consistent with gather");
+  std::vector<int32_t> owned;
+  owned.reserve(nfaces / 2 + 1024);
+  for (int64_t f = 0; f < nfaces; ++f)
+    if (mask[f]) owned.push_back((int32_t)f);
+  p->nowned = (int64_t)owned.size();
+  const int nfpt = 4 * p->nfp;
+  err = cudaMalloc(&p->d_owned, (owned.empty() ? 1 : owned.size()) * sizeof(int32_t));
+  if (err == cudaSuccess && !owned.empty())
+    err = cudaMemcpy(p->d_owned, owned.data(), owned.size() * sizeof(int32_t),
+                     cudaMemcpyHostToDevice);
+  if (err == cudaSuccess)
+    err = cudaMalloc(&p->d_flux, (size_t)p->nfields * p->nel * nfpt * sizeof(double));
+  if (err == cudaSuccess && p->equation == DG_EULER)
+    err = cudaMalloc(&p->d_aux, (size_t)3 * p->nel * p->np * sizeof(double));
+  if (err != cudaSuccess) return cuda_fail(err, "face-shared buffers");
+  int fb = 0;
+  err = face_blocks_of(p->equation, p->order, &fb);
+  if (err != cudaSuccess) return cuda_fail(err, "face kernel configuration");
+  if (fb < 1) return fail(DG_ERR_UNSUPPORTED, "face kernel does not fit on an SM");
+  const int64_t fthreads = p->nowned * p->nfp;
+  const int64_t fblocks = (fthreads + dg::kFaceBlock - 1) / dg::kFaceBlock;
+  const int64_t ffull = (int64_t)p->nsm * fb;
+  p->face_grid = (int)(fblocks < ffull ? (fblocks > 0 ? fblocks : 1) : ffull);
+  const int64_t ablocks = (p->nel * p->np + dg::kFaceBlock - 1) / dg::kFaceBlock;
+  const int64_t afull = (int64_t)p->nsm * 8;
+  p->aux_grid = (int)(ablocks < afull ? ablocks : afull);
+  p->split = true;
+  return DG_OK;
+}
+
+// The face-shared path's first launches (Euler table, face kernel) for state q.
+cudaError_t launch_faces(const dg_plan* p, const double* q, cudaStream_t s) {
+  dg::FaceArgs f;
+  std::memset(&f, 0, sizeof(f));
+  f.q = q;
+  f.aux = p->d_aux;
+  f.face_geom = p->face_geom;
+  f.gather = p->gather;
+  f.partner = p->face_partner;
+  f.owned = p->d_owned;
+  f.face_nodes = p->d_face_nodes;
+  f.flux = p->d_flux;
+  f.nel = p->nel;
+  f.nowned = p->nowned;
+  f.status = p->d_status;
+  f.p0 = p->params[0];
+  f.p1 = p->params[1];
+  f.p2 = p->params[2];
+  for (int k = 0; k < 6; ++k) f.k[k] = p->k[k];
+  return face_launch_of(p->equation, p->order, f, p->face_grid, p->aux_grid, s);
 }
 
 // Adjoint operator block: W in [r][i][j] (the forward layout of W^T), LIFT in
@@ -243,12 +397,28 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     }
   }
 
-  dg::LaunchShape shape, shape_stage;
+  // face-shared path: FP64 plans on meshes that carry face_partner and whose
+  // face points fit 31-bit indices; the fused kernel serves all others
+  const bool split = mesh->face_partner && precision == DG_FP64 &&
+                     mesh->nelements * 4 * (int64_t)nfp < (int64_t(1) << 31);
+  if (mesh->face_partner) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, mesh->face_partner) != cudaSuccess ||
+        attr.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      return fail(DG_ERR_ARGUMENT, "face_partner must be device memory");
+    }
+  }
+
+  dg::LaunchShape shape;
   cudaError_t err = shape_of(equation, N, precision, 0, &shape);
-  if (err == cudaSuccess) err = shape_of(equation, N, precision, 1, &shape_stage);
+  for (int mode = 1; mode < (split ? 4 : 2) && err == cudaSuccess; ++mode) {
+    dg::LaunchShape other;
+    err = shape_of(equation, N, precision, mode, &other);
+    if (other.blocks_per_sm < shape.blocks_per_sm)
+      shape.blocks_per_sm = other.blocks_per_sm;
+  }
   if (err != cudaSuccess) return cuda_fail(err, "kernel configuration");
-  if (shape_stage.blocks_per_sm < shape.blocks_per_sm)
-    shape.blocks_per_sm = shape_stage.blocks_per_sm;
   if (shape.blocks_per_sm < 1)
     return fail(DG_ERR_UNSUPPORTED, "kernel does not fit on an SM");
   const int rs = precision == DG_FP64 ? 8 : 4;
@@ -276,6 +446,15 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   p->shape = shape;
   p->ops_bytes = static_cast<uint32_t>(off.size);
   for (int k = 0; k < nparams; ++k) p->params[k] = params[k];
+  if (equation == DG_MAXWELL) {  // flux and mass constants, once per plan
+    const double z = std::sqrt(params[2] / params[1]), y = 1.0 / z;
+    p->k[0] = z;
+    p->k[1] = y;
+    p->k[2] = -1.0 / (z + z);
+    p->k[3] = 1.0 / (y + y);
+    p->k[4] = 1.0 / params[1];
+    p->k[5] = 1.0 / params[2];
+  }
   cudaGetDevice(&p->device);
 
   err = cudaMalloc(&p->d_ops, p->ops_bytes);
@@ -294,18 +473,22 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
       (p->nel + shape.elems_per_tile - 1) / shape.elems_per_tile;
   const int64_t full = (int64_t)nsm * shape.blocks_per_sm;
   p->grid = (int)(ntiles < full ? ntiles : full);
+  p->face_partner = mesh->face_partner;
+
+  if (split) {
+    p->d_face_nodes = reinterpret_cast<const int32_t*>(
+        static_cast<const unsigned char*>(p->d_ops) + off.fn);
+    const int code = setup_split(p, mesh->face_partner, p->d_face_nodes);
+    if (code != DG_OK) {
+      dg_plan_destroy(p);
+      return code;
+    }
+  }
 
   if (mesh->face_partner && equation == DG_WAVE && precision == DG_FP64) {
     if (p->nel * 8 * (int64_t)nfp >= (int64_t(1) << 32)) {
       dg_plan_destroy(p);
       return fail(DG_ERR_ARGUMENT, "mesh too large for the adjoint's 32-bit face indices");
-    }
-    cudaPointerAttributes attr;
-    if (cudaPointerGetAttributes(&attr, mesh->face_partner) != cudaSuccess ||
-        attr.type != cudaMemoryTypeDevice) {
-      cudaGetLastError();
-      dg_plan_destroy(p);
-      return fail(DG_ERR_ARGUMENT, "face_partner must be device memory");
     }
     dg::LaunchShape ashape;
     err = dg::adjoint_shape_wave(N, &ashape);
@@ -332,7 +515,6 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
       dg_plan_destroy(p);
       return cuda_fail(err, "adjoint buffers");
     }
-    p->face_partner = mesh->face_partner;
     p->adj_ops_bytes = static_cast<uint32_t>(size);
     const int64_t atiles = (p->nel + ashape.elems_per_tile - 1) / ashape.elems_per_tile;
     const int64_t afull = (int64_t)nsm * ashape.blocks_per_sm;
@@ -397,8 +579,13 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
   dg::RhsArgs a = base_args(p);
   a.q = q;
   a.rhs = rhs;
-  cudaError_t err = launch_of(p->equation, p->order, p->precision, 0, a, p->grid,
-                              reinterpret_cast<cudaStream_t>(stream));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (p->split) {
+    cudaError_t err = launch_faces(p, q, s);
+    if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
+  }
+  cudaError_t err = launch_of(p->equation, p->order, p->precision,
+                              p->split ? dg::MODE_SPLIT : dg::MODE_RHS, a, p->grid, s);
   if (err != cudaSuccess) return cuda_fail(err, "rhs launch");
   return DG_OK;
 }
@@ -426,8 +613,14 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
       return fail(DG_ERR_ARGUMENT, "rhs_unscaled overlaps another array");
     a.rhs_unscaled = rhs_unscaled;
   }
-  cudaError_t err = launch_of(p->equation, p->order, p->precision, 1, a, p->grid,
-                              reinterpret_cast<cudaStream_t>(stream));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (p->split) {
+    cudaError_t err = launch_faces(p, q_in, s);
+    if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
+  }
+  cudaError_t err = launch_of(p->equation, p->order, p->precision,
+                              dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0), a,
+                              p->grid, s);
   if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
   return DG_OK;
 }
@@ -513,6 +706,8 @@ int dg_plan_destroy(dg_plan* p) {
   if (p->d_ops && cudaFree(p->d_ops) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_status && cudaFree(p->d_status) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
+  for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux})
+    if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
   return DG_OK;
@@ -520,12 +715,22 @@ int dg_plan_destroy(dg_plan* p) {
 
 int dg_fp64_fma_probe(double* out, int64_t iters, int32_t grid, int32_t block,
                       void* stream) {
-  if (!out || iters < 1 || grid < 1 || block < 1 || block > 1024)
+  if (!out || iters < 1 || iters > INT32_MAX || grid < 1 || block < 1 || block > 1024)
     return fail(DG_ERR_ARGUMENT, "bad probe arguments");
   fp64_fma_probe_kernel<<<grid, block, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      out, iters);
+      out, (int)iters);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return cuda_fail(err, "probe launch");
+  return DG_OK;
+}
+
+int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* launches_per_rhs,
+                 int64_t* owned_faces) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (face_shared) *face_shared = p->split ? 1 : 0;
+  if (launches_per_rhs)
+    *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : 1;
+  if (owned_faces) *owned_faces = p->split ? p->nowned : 0;
   return DG_OK;
 }
 

@@ -10,6 +10,7 @@ namespace dg {
 
 struct RhsArgs;
 struct AdjArgs;
+struct FaceArgs;
 
 struct LaunchShape {
   int smem_bytes = 0;      // dynamic shared memory per CTA
@@ -44,13 +45,19 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
 
 // Per equation: shape query (also raises the kernel's shared-memory limit on
 // the current device) and launch, for precision 0 (FP64) or 1 (FP32
-// arithmetic, FP64 state) and mode 0 (RHS) or 1 (fused RK stage).  Return
+// arithmetic, FP64 state) and mode bits MODE_STAGE (fused RK stage) and
+// MODE_SPLIT (face values from the face-shared kernels, FP64 only).  Return
 // cudaErrorInvalidValue for a combination that is not compiled in.
+// face_blocks_*: resident CTAs per SM of the face kernel; face_launch_*:
+// (Euler: the per-node table, then) the face kernel of the face-shared path.
 #define DG_DECLARE_EQ(name)                                                   \
   cudaError_t shape_##name(int order, int precision, int mode,               \
                            LaunchShape* out);                                \
   cudaError_t launch_##name(int order, int precision, int mode,              \
-                            const RhsArgs& a, int grid, cudaStream_t s);
+                            const RhsArgs& a, int grid, cudaStream_t s);     \
+  cudaError_t face_blocks_##name(int order, int* blocks_per_sm);             \
+  cudaError_t face_launch_##name(int order, const FaceArgs& a, int grid,     \
+                                 int aux_grid, cudaStream_t s);
 DG_DECLARE_EQ(wave)
 DG_DECLARE_EQ(euler)
 DG_DECLARE_EQ(maxwell)

@@ -25,6 +25,11 @@
 //      speed), then either stored (MODE_RHS) or folded into a low-storage
 //      Runge-Kutta stage (MODE_STAGE): res = a res + dt L(q), q_out = q + b res.
 //
+// With MODE_SPLIT (FP64 only) step 4 is replaced by a coalesced load of face
+// values that dg_face_flux_kernel (dg_face.cuh) evaluated once per glued pair
+// of face points, and the Euler pre-pass reads pressure and 1/rho from the
+// per-node table of dg_euler_aux_kernel instead of dividing.
+//
 // ``Real`` is the arithmetic type of steps 2-5.  double: the plain FP64 path.
 // float: the mixed-precision path -- derivative, flux and LIFT arithmetic in
 // FP32 while the state, the RK accumulation and the Euler pressure recovery
@@ -42,7 +47,8 @@
 
 namespace dg {
 
-enum { MODE_RHS = 0, MODE_STAGE = 1 };
+// bit 0: RK stage epilogue; bit 1: face values from the face-shared kernels
+enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_SPLIT = 2 };
 
 struct RhsArgs {
   const double* q;
@@ -60,6 +66,9 @@ struct RhsArgs {
   int64_t nel;
   int* status;
   double p0, p1, p2;       // equation parameters
+  double k[6];             // maxwell: z, 1/z, -1/(2z), 1/(2/z), 1/eps, 1/mu
+  const double* flux_in;   // MODE_SPLIT: (NF, Nel, 4 Nfp) face values
+  const double* aux;       // MODE_SPLIT euler: (3, Nel, Np) p, 1/rho, |u| + c
 };
 
 template <int N>
@@ -165,6 +174,9 @@ template <int N, int EQ, typename Real, int MODE>
 __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   using T = Tile<N, EQ, Real>;
   using Ops = OpsLayout<N, Real>;
+  constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
+  constexpr bool SPLIT = (MODE & MODE_SPLIT) != 0;
+  static_assert(!(SPLIT && T::MIXED), "the face-shared path is FP64 only");
   constexpr int NP = T::NP, NFPT = T::NFPT, NF = T::NF, E = T::E;
   constexpr int ROW = T::ROW, FROW = T::FROW;  // shared-memory row pitches
   extern __shared__ __align__(128) unsigned char smem[];
@@ -210,8 +222,9 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   const int64_t nel = a.nel;
   const int64_t nelnp = nel * NP;
   const int64_t ntiles = (nel + E - 1) / E;
-  const Real p0 = (Real)a.p0, p1 = (Real)a.p1, p2 = (Real)a.p2;
+  const Real p0 = (Real)a.p0;
   const Real half = (Real)0.5, two = (Real)2, zero = (Real)0;
+  const Real inv_eps = (Real)a.k[4], inv_mu = (Real)a.k[5];
 
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t e0 = tile * E;
@@ -241,6 +254,14 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       for (int idx = t; idx < 16 * E; idx += kBlock)
         sFG[idx] = idx < 16 * ecount ? to_real<Real>(__ldg(ft + idx)) : zero;
     }
+    if constexpr (SPLIT) {  // face values of the tile: contiguous per field
+      const int64_t nfpt_all = nel * NFPT;
+      const double* fk = a.flux_in + e0 * NFPT;
+#pragma unroll
+      for (int k = 0; k < NF; ++k, fk += nfpt_all)
+        for (int rem = t; rem < E * NFPT; rem += kBlock)
+          sFlux[k * (E * FROW) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : zero;
+    }
     __syncthreads();
     // }}}
 
@@ -264,12 +285,17 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         const double en_d = sQ[(1 * E + el) * NP + i];
         const double md[3] = {sQ[(2 * E + el) * NP + i], sQ[(3 * E + el) * NP + i],
                               sQ[(4 * E + el) * NP + i]};
-        double rinv_d;
-        if constexpr (T::MIXED) rinv_d = rcp64_fast(rho_d);
-        else rinv_d = 1.0 / rho_d;
-        const double p_d =
-            (a.p0 - 1.0) *
-            (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
+        double rinv_d, p_d;
+        if constexpr (SPLIT) {
+          const int64_t gidx = e0 * NP + (el * NP + i);
+          p_d = __ldg(a.aux + gidx);
+          rinv_d = __ldg(a.aux + nelnp + gidx);
+        } else {
+          if constexpr (T::MIXED) rinv_d = rcp64_fast(rho_d);
+          else rinv_d = 1.0 / rho_d;
+          p_d = (a.p0 - 1.0) *
+                (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
+        }
         if constexpr (T::MIXED) sP[el * NP + i] = p_d;
         const Real p = to_real<Real>(p_d), en = to_real<Real>(en_d);
         const Real m[3] = {to_real<Real>(md[0]), to_real<Real>(md[1]),
@@ -432,10 +458,10 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     }
     // }}}
 
-    // {{{ 4. face gather + numerical flux
+    // {{{ 4. face gather + numerical flux (fused path only)
     const uint32_t* gt = a.gather + e0 * NFPT;
     const uint32_t tile_node0 = (uint32_t)(e0 * NP);
-    for (int pidx = t; pidx < ecount * NFPT; pidx += kBlock) {
+    for (int pidx = t; pidx < (SPLIT ? 0 : ecount * NFPT); pidx += kBlock) {
       const int elp = pidx / NFPT;
       const int fj = pidx - elp * NFPT;
       const int f = fj / Shape<N>::NFP;
@@ -559,8 +585,8 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           qe[4] = qi[4];
           qe[5] = qi[5];
         }
-        const Real alpha = p0, eps = p1, mu = p2;
-        const Real z = sqrt(mu / eps), y = (Real)1 / z;
+        const Real alpha = p0;
+        const Real z = (Real)a.k[0], y = (Real)a.k[1];
         const Real je[3] = {qe[0] - qi[0], qe[1] - qi[1], qe[2] - qi[2]};
         const Real jh[3] = {qe[3] - qi[3], qe[4] - qi[4], qe[5] - qi[5]};
         const Real n[3] = {nx, ny, nz};
@@ -579,7 +605,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         }
         cross(n, te, fe);
         cross(n, th, fh);
-        const Real ce = (Real)-1 / (z + z), ch = (Real)1 / (y + y);
+        const Real ce = (Real)a.k[2], ch = (Real)a.k[3];
 #pragma unroll
         for (int x = 0; x < 3; ++x) {
           out[x * FS] = -scale * (ce * fe[x]);
@@ -607,14 +633,14 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           for (int fj = 0; fj < NFPT; ++fj)
             acc = fma(sL[fj * NP + i], fl[k * E * NFPT + fj], acc);
         }
-        if constexpr (EQ == DG_MAXWELL) acc = acc / (k < 3 ? p1 : p2);
+        if constexpr (EQ == DG_MAXWELL) acc = acc * (k < 3 ? inv_eps : inv_mu);
         double val;
         if constexpr (T::MIXED) val = f2d_alu(acc);
         else val = acc;
-        if constexpr (MODE == MODE_STAGE)
+        if constexpr (STAGE)
           if (a.rhs_unscaled) a.rhs_unscaled[gidx] = val;
         if (a.elem_scale) val *= __ldg(a.elem_scale + e0 + el);
-        if constexpr (MODE == MODE_RHS) {
+        if constexpr (!STAGE) {
           a.rhs[gidx] = val;
         } else {
           const double r =

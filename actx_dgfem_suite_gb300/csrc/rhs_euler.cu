@@ -10,4 +10,11 @@ cudaError_t launch_euler(int order, int precision, int mode, const RhsArgs& a,
                          int grid, cudaStream_t s) {
   return launch_any<DG_EULER>(order, precision, mode, a, grid, s);
 }
+cudaError_t face_blocks_euler(int order, int* blocks_per_sm) {
+  return face_blocks_any<DG_EULER>(order, blocks_per_sm);
+}
+cudaError_t face_launch_euler(int order, const FaceArgs& a, int grid, int aux_grid,
+                           cudaStream_t s) {
+  return face_launch_any<DG_EULER>(order, a, grid, aux_grid, s);
+}
 }  // namespace dg

@@ -1,8 +1,12 @@
 // Instantiates the RHS kernel of one equation for orders 1..4, FP64 and
-// mixed precision, plain RHS and fused RK stage, and defines the equation's
+// mixed precision, plain RHS and fused RK stage (FP64 also in the
+// face-shared split form, with its face kernel), and defines the equation's
 // shape/launch entry points.  Included by exactly one .cu file per equation.
 #pragma once
 
+#include <type_traits>
+
+#include "dg_face.cuh"
 #include "dg_launch.h"
 #include "dg_rhs.cuh"
 
@@ -33,28 +37,58 @@ cudaError_t launch_impl(const RhsArgs& a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <int N, int EQ, typename Real>
+cudaError_t shape_mode(int mode, LaunchShape* out) {
+  switch (mode) {
+    case MODE_RHS: return shape_impl<N, EQ, Real, MODE_RHS>(out);
+    case MODE_STAGE: return shape_impl<N, EQ, Real, MODE_STAGE>(out);
+    default: break;
+  }
+  if constexpr (std::is_same<Real, double>::value) {
+    switch (mode) {
+      case MODE_SPLIT: return shape_impl<N, EQ, Real, MODE_SPLIT>(out);
+      case MODE_SPLIT | MODE_STAGE:
+        return shape_impl<N, EQ, Real, MODE_SPLIT | MODE_STAGE>(out);
+      default: break;
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int N, int EQ, typename Real>
+cudaError_t launch_mode(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
+  switch (mode) {
+    case MODE_RHS: return launch_impl<N, EQ, Real, MODE_RHS>(a, grid, s);
+    case MODE_STAGE: return launch_impl<N, EQ, Real, MODE_STAGE>(a, grid, s);
+    default: break;
+  }
+  if constexpr (std::is_same<Real, double>::value) {
+    switch (mode) {
+      case MODE_SPLIT: return launch_impl<N, EQ, Real, MODE_SPLIT>(a, grid, s);
+      case MODE_SPLIT | MODE_STAGE:
+        return launch_impl<N, EQ, Real, MODE_SPLIT | MODE_STAGE>(a, grid, s);
+      default: break;
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
 template <int N, int EQ>
 cudaError_t shape_n(int precision, int mode, LaunchShape* out) {
-  if (precision == 0)
-    return mode == 0 ? shape_impl<N, EQ, double, MODE_RHS>(out)
-                     : shape_impl<N, EQ, double, MODE_STAGE>(out);
-  return mode == 0 ? shape_impl<N, EQ, float, MODE_RHS>(out)
-                   : shape_impl<N, EQ, float, MODE_STAGE>(out);
+  return precision == 0 ? shape_mode<N, EQ, double>(mode, out)
+                        : shape_mode<N, EQ, float>(mode, out);
 }
 
 template <int N, int EQ>
 cudaError_t launch_n(int precision, int mode, const RhsArgs& a, int grid,
                      cudaStream_t s) {
-  if (precision == 0)
-    return mode == 0 ? launch_impl<N, EQ, double, MODE_RHS>(a, grid, s)
-                     : launch_impl<N, EQ, double, MODE_STAGE>(a, grid, s);
-  return mode == 0 ? launch_impl<N, EQ, float, MODE_RHS>(a, grid, s)
-                   : launch_impl<N, EQ, float, MODE_STAGE>(a, grid, s);
+  return precision == 0 ? launch_mode<N, EQ, double>(mode, a, grid, s)
+                        : launch_mode<N, EQ, float>(mode, a, grid, s);
 }
 
 template <int EQ>
 cudaError_t shape_any(int order, int precision, int mode, LaunchShape* out) {
-  if ((precision != 0 && precision != 1) || (mode != 0 && mode != 1))
+  if ((precision != 0 && precision != 1) || mode < 0 || mode > 3)
     return cudaErrorInvalidValue;
   switch (order) {
     case 1: return shape_n<1, EQ>(precision, mode, out);
@@ -68,7 +102,7 @@ cudaError_t shape_any(int order, int precision, int mode, LaunchShape* out) {
 template <int EQ>
 cudaError_t launch_any(int order, int precision, int mode, const RhsArgs& a,
                        int grid, cudaStream_t s) {
-  if ((precision != 0 && precision != 1) || (mode != 0 && mode != 1))
+  if ((precision != 0 && precision != 1) || mode < 0 || mode > 3)
     return cudaErrorInvalidValue;
   switch (order) {
     case 1: return launch_n<1, EQ>(precision, mode, a, grid, s);
@@ -78,6 +112,47 @@ cudaError_t launch_any(int order, int precision, int mode, const RhsArgs& a,
     default: return cudaErrorInvalidValue;
   }
 }
+
+// {{{ face-shared path: the face kernel (and, for Euler, the per-node table)
+
+template <int N, int EQ>
+cudaError_t face_blocks_n(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      blocks_per_sm, dg_face_flux_kernel<N, EQ>, kFaceBlock, 0);
+}
+
+template <int EQ>
+cudaError_t face_blocks_any(int order, int* blocks_per_sm) {
+  switch (order) {
+    case 1: return face_blocks_n<1, EQ>(blocks_per_sm);
+    case 2: return face_blocks_n<2, EQ>(blocks_per_sm);
+    case 3: return face_blocks_n<3, EQ>(blocks_per_sm);
+    case 4: return face_blocks_n<4, EQ>(blocks_per_sm);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int EQ>
+cudaError_t face_launch_any(int order, const FaceArgs& a, int grid, int aux_grid,
+                            cudaStream_t s) {
+  if constexpr (EQ == DG_EULER) {
+    dg_euler_aux_kernel<EQ><<<aux_grid, kFaceBlock, 0, s>>>(
+        a.q, const_cast<double*>(a.aux),
+        (uint32_t)(a.nel * ((order + 1) * (order + 2) * (order + 3) / 6)), a.p0);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  switch (order) {
+    case 1: dg_face_flux_kernel<1, EQ><<<grid, kFaceBlock, 0, s>>>(a); break;
+    case 2: dg_face_flux_kernel<2, EQ><<<grid, kFaceBlock, 0, s>>>(a); break;
+    case 3: dg_face_flux_kernel<3, EQ><<<grid, kFaceBlock, 0, s>>>(a); break;
+    case 4: dg_face_flux_kernel<4, EQ><<<grid, kFaceBlock, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// }}}
 
 }  // namespace
 }  // namespace dg

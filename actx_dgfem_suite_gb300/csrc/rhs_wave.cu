@@ -10,4 +10,11 @@ cudaError_t launch_wave(int order, int precision, int mode, const RhsArgs& a,
                          int grid, cudaStream_t s) {
   return launch_any<DG_WAVE>(order, precision, mode, a, grid, s);
 }
+cudaError_t face_blocks_wave(int order, int* blocks_per_sm) {
+  return face_blocks_any<DG_WAVE>(order, blocks_per_sm);
+}
+cudaError_t face_launch_wave(int order, const FaceArgs& a, int grid, int aux_grid,
+                           cudaStream_t s) {
+  return face_launch_any<DG_WAVE>(order, a, grid, aux_grid, s);
+}
 }  // namespace dg

@@ -67,7 +67,7 @@ class DeviceBoxDiscretization:
     arrays in the C ABI's formats; ``nodes()`` returns the (3, Nel, Np) node
     coordinates as a device tensor."""
 
-    def __init__(self, order: int, n, a, b, device=None, with_partner: bool = False,
+    def __init__(self, order: int, n, a, b, device=None, with_partner: bool = True,
                  with_nodes: bool = True):
         if np.isscalar(n):
             n = (int(n),) * 3
@@ -139,7 +139,7 @@ class DeviceBoxDiscretization:
 
 def device_problem(equation: str, order: int, nel_1d: int,
                    definition: str = "baseline", device=None, seed: int = 0,
-                   with_partner: bool = False):
+                   with_partner: bool = True):
     """The builders' problem with mesh, geometry and initial state made on
     the device (same definitions as ``equations.*.*_problem``)."""
     from actx_dgfem_suite_gb300.equations import euler, maxwell, wave

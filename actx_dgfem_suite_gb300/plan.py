@@ -29,10 +29,16 @@ def _stream_handle(stream) -> ctypes.c_void_p:
 
 class DeviceMesh:
     """Geometry, gather index and reference operators of one discretisation,
-    uploaded once."""
+    uploaded once.
+
+    ``with_partner``: also hold the glued face-point index, which FP64 plans
+    use for the face-shared path (each glued pair's flux evaluated once) and
+    the adjoint needs.  ``None`` (default): whenever the discretisation
+    provides it; ``False``: never (FP64 plans then use the single fused
+    launch); ``True``: required."""
 
     def __init__(self, disc: DGDiscretization, device=None,
-                 with_partner: bool = False):
+                 with_partner: bool | None = None):
         if not torch.cuda.is_available():
             raise RuntimeError("DeviceMesh needs a CUDA device")
         self.disc = disc
@@ -46,7 +52,7 @@ class DeviceMesh:
                 raise ValueError("device-built mesh lives on another device")
             self.metric, self.face_geom, self.gather = (
                 disc.metric, disc.face_geom, disc.gather)
-            self.partner = disc.partner
+            self.partner = disc.partner if with_partner is not False else None
             if with_partner and self.partner is None:
                 raise ValueError("device mesh was built without face partners")
         else:
@@ -55,9 +61,10 @@ class DeviceMesh:
                 np.ascontiguousarray(disc.face_geometry())).to(self.device)
             self.gather = torch.from_numpy(
                 disc.gather_index().view(np.int32)).to(self.device)
-            # glued face-point index, needed only by the adjoint
-            self.partner = (torch.from_numpy(disc.face_partner()).to(self.device)
-                            if with_partner else None)
+            # glued face-point index (face-shared path, adjoint)
+            self.partner = None
+            if with_partner is not False and (with_partner or disc.perm_id is not None):
+                self.partner = torch.from_numpy(disc.face_partner()).to(self.device)
         ref = disc.ref
         self._weak = np.ascontiguousarray(ref.weak_diff, dtype=np.float64)
         self._strong = np.ascontiguousarray(ref.diff, dtype=np.float64)
@@ -133,8 +140,18 @@ class DevicePlan:
         _lib.check(self._lib.dg_plan_info(self._handle, ctypes.byref(nel),
                                           *[ctypes.byref(v) for v in vals]))
         order, nf, grid, block, smem = (v.value for v in vals)
+        shared, launches = ctypes.c_int32(), ctypes.c_int32()
+        owned = ctypes.c_int64()
+        _lib.check(self._lib.dg_plan_path(self._handle, ctypes.byref(shared),
+                                          ctypes.byref(launches), ctypes.byref(owned)))
         return dict(nelements=nel.value, order=order, nfields=nf, grid=grid,
-                    block=block, smem_bytes=smem)
+                    block=block, smem_bytes=smem, face_shared=bool(shared.value),
+                    launches_per_rhs=launches.value, owned_faces=owned.value)
+
+    @property
+    def launches_per_rhs(self) -> int:
+        """Kernel launches of one ``rhs`` or ``rk_stage`` call."""
+        return self.info()["launches_per_rhs"]
 
     def _check_tensor(self, x: torch.Tensor, name: str):
         if x.dtype != torch.float64 or x.device != self.mesh.device:

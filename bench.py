@@ -124,14 +124,15 @@ def _peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def _ncu_traffic() -> dict:
-    """Per-launch DRAM bytes from the committed ncu summary, keyed by case."""
+def _ncu_traffic(path: str) -> dict:
+    """DRAM bytes of one RHS (all its launches) from the committed ncu
+    summary, keyed by case, for the FP64 path ``path`` ("shared"/"fused")."""
     out = {}
     p = ROOT / "profiles" / "dram_traffic_fp64_rhs.txt"
     if p.exists():
         for ln in p.read_text().splitlines():
             f = ln.split()
-            if len(f) >= 3 and f[0] == "traffic":
+            if len(f) >= 4 and f[0] == "traffic" and f[3] == path:
                 out[f[1]] = float(f[2])
     return out
 
@@ -147,7 +148,10 @@ def fp64_peak_tflops(torch) -> float:
     buf = torch.empty(grid * block, dtype=torch.float64, device="cuda")
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     best = 0.0
-    for _ in range(3):
+    for _ in range(2):   # let the clocks settle before timing
+        _lib.check(L.dg_fp64_fma_probe(ctypes.c_void_p(buf.data_ptr()), iters,
+                                       grid, block, st))
+    for _ in range(5):
         s, e = torch.cuda.Event(True), torch.cuda.Event(True)
         s.record()
         _lib.check(L.dg_fp64_fma_probe(ctypes.c_void_p(buf.data_ptr()), iters,
@@ -446,15 +450,24 @@ def our_arm(args) -> None:
     c = rd["cost"]
     t_dom = case_ms[dom] * 1e-3
     achieved_gbs = c.bytes / t_dom / 1e9
-    traffic = _ncu_traffic().get(f"{rd['eq']}{rd['order']}")
-    if traffic is not None and args.scale != 1:
+    info = rd["compiled"].plan.info()
+    path = "shared" if info["face_shared"] else "fused"
+    traffic = _ncu_traffic(path).get(f"{rd['eq']}{rd['order']}")
+    if traffic is not None and (args.scale != 1 or args.precision != "fp64"):
         traffic = None
+    kname = (f"dg_rhs_kernel<{rd['order']}, {rd['eq']}, "
+             f"{'double' if args.precision == 'fp64' else 'float'}, "
+             f"{'SPLIT' if info['face_shared'] else 'RHS'}>")
+    if info["face_shared"]:
+        kname = (f"dg_face_flux_kernel<{rd['order']}, {rd['eq']}>"
+                 + (" + dg_euler_aux_kernel" if rd["eq"] == "euler" else "")
+                 + " + " + kname + " (one RHS)")
     fp64_achieved = 2.0 * c.fma / t_dom / 1e12
     roofline = {
         "bound": "hbm", "achieved": achieved_gbs, "peak": peaks["hbm_gbs"],
         "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
         "traffic": traffic,
-        "kernel": f"dg_rhs_kernel<{rd['order']}, {rd['eq']}, {'double' if args.precision == 'fp64' else 'float'}, RHS>",
+        "kernel": kname,
         "peak_source": peaks["source"],
         "fp64_pipe": {"achieved_tflops": fp64_achieved,
                       "peak_tflops": fp64_peak,
@@ -503,7 +516,7 @@ def our_arm(args) -> None:
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clock_info,
-            "gpu_launches": len(runs) * K,
+            "gpu_launches": K * sum(r["compiled"].plan.launches_per_rhs for r in runs),
             "setup_s": setup_s,
             "cases": per_case,
             "extras": extras,

@@ -63,13 +63,25 @@ typedef struct dg_mesh_desc {
   const int32_t* face_nodes; /* host, (4, Nfp): volume node of each face node */
   const int32_t* face_partner; /* device, (Nel, 4, Nfp): flat face-point index
                                   (e'*4 + f')*Nfp + j' of the glued face point,
-                                  -1 on the boundary; optional, needed only by
-                                  dg_rhs_adjoint */
+                                  -1 on the boundary; optional.  FP64 plans use
+                                  it for the face-shared path (see
+                                  dg_plan_create); dg_rhs_adjoint needs it */
 } dg_mesh_desc;
 
 /* Build a plan: validate the description, stage the reference operators in
  * device memory (in the plan's precision) and size the persistent launch.
  * params: wave {c}; euler {gamma}; maxwell {alpha, epsilon, mu}.
+ *
+ * FP64 plans on meshes with face_partner (and Nel * 4 * Nfp < 2^31) take the
+ * face-shared path: each glued pair of face points has its numerical flux
+ * evaluated once (for Euler, pressure and wave speed once per node) by one
+ * or two extra launches before the volume/LIFT kernel; face_partner must then
+ * pair whole faces consistently with gather, which plan creation checks
+ * (DG_ERR_ARGUMENT otherwise).  Such a plan keeps face values in its own
+ * device buffers, so its dg_rhs / dg_rk_stage calls must not run
+ * concurrently with each other (issue them on one stream).  All other plans
+ * evaluate the RHS in one fused launch and have no such restriction.
+ *
  * Replaces the compile step of the reference's array contexts:
  * actx.compile(rhs) (actx_dgfem_suite/run/__main__.py:74) and the DAG/loopy
  * pipeline behind it (actx_dgfem_suite/arraycontext/dgfem_optimizer.py:182-245). */
@@ -175,6 +187,13 @@ int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 /* Release the plan's device buffers.  Replaces dropping the compiled program
  * and freeing the memory pool (actx_dgfem_suite/tools/wave_dof_scaling.py:108-126). */
 int dg_plan_destroy(dg_plan* plan);
+
+/* Which path the plan takes: face_shared 1 for the face-shared path, 0 for
+ * the single fused launch; launches_per_rhs = kernel launches of one dg_rhs
+ * or dg_rk_stage; owned_faces = faces whose flux the face kernel evaluates.
+ * Any output pointer may be NULL. */
+int dg_plan_path(const dg_plan* plan, int32_t* face_shared,
+                 int32_t* launches_per_rhs, int64_t* owned_faces);
 
 /* Describe a plan: any output pointer may be NULL.  grid/block/smem are the
  * persistent launch shape chosen at plan creation. */

@@ -1,5 +1,9 @@
 """FP64 parity of the CUDA RHS kernels against the CPU oracle, through the
-C ABI (DevicePlan -> dg_rhs).  Bound: relative L2 <= 1e-12."""
+C ABI (DevicePlan -> dg_rhs).  Bound: relative L2 <= 1e-12.
+
+Both FP64 paths are covered: ``shared`` (mesh uploaded with face partners:
+face kernel evaluates each glued pair's flux once, then volume + LIFT) and
+``fused`` (no partners: one launch computes every face point's flux)."""
 
 from __future__ import annotations
 
@@ -15,14 +19,16 @@ pytestmark = pytest.mark.gpu
 
 EQUATIONS = ("wave", "euler", "maxwell")
 ORDERS = (1, 2, 3, 4)
+PATHS = ("shared", "fused")
 
 
-def _gpu_rhs(problem):
+def _gpu_rhs(problem, path="shared"):
     import torch
 
     from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
-    dm = DeviceMesh(problem.disc, "cuda:0")
+    dm = DeviceMesh(problem.disc, "cuda:0", with_partner=(path == "shared"))
     plan = DevicePlan(dm, problem.equation, problem.params)
+    assert plan.info()["face_shared"] == (path == "shared")
     q = torch.from_numpy(problem.fields).to("cuda:0")
     out = plan.rhs(q)
     plan.finish()
@@ -32,51 +38,98 @@ def _gpu_rhs(problem):
 @pytest.mark.parametrize("equation", EQUATIONS)
 @pytest.mark.parametrize("order", ORDERS)
 @pytest.mark.parametrize("definition", ("reference", "baseline"))
-def test_parity_box(equation, order, definition):
+@pytest.mark.parametrize("path", PATHS)
+def test_parity_box(equation, order, definition, path):
     prob = get_problem(equation, 3, order, definition=definition, nel_1d=3)
-    got, _ = _gpu_rhs(prob)
+    got, _ = _gpu_rhs(prob, path)
     ref, scale = oracle_rhs(prob, parts=True)
     assert parity_error(got, ref, scale) <= FP64_RTOL
 
 
 @pytest.mark.parametrize("equation", EQUATIONS)
 @pytest.mark.parametrize("order", ORDERS)
-def test_parity_jittered_mesh(equation, order):
+@pytest.mark.parametrize("path", PATHS)
+def test_parity_jittered_mesh(equation, order, path):
     prob = make_problem(equation, jittered_box_mesh(4), order, seed=order)
-    got, _ = _gpu_rhs(prob)
+    got, _ = _gpu_rhs(prob, path)
     ref, scale = oracle_rhs(prob, parts=True)
     assert parity_error(got, ref, scale) <= FP64_RTOL
 
 
 @pytest.mark.parametrize("equation", EQUATIONS)
 @pytest.mark.parametrize("order", ORDERS)
-def test_parity_single_element(equation, order):
+@pytest.mark.parametrize("path", PATHS)
+def test_parity_single_element(equation, order, path):
     prob = make_problem(equation, single_tet_mesh(), order)
-    got, _ = _gpu_rhs(prob)
+    got, _ = _gpu_rhs(prob, path)
     ref, scale = oracle_rhs(prob, parts=True)
     assert parity_error(got, ref, scale) <= FP64_RTOL
 
 
 @pytest.mark.parametrize("equation", EQUATIONS)
-def test_parity_single_hex(equation):
+@pytest.mark.parametrize("path", PATHS)
+def test_parity_single_hex(equation, path):
     prob = make_problem(equation, generate_box_tet_mesh(0.0, 1.0, 1), 3)
-    got, _ = _gpu_rhs(prob)
+    got, _ = _gpu_rhs(prob, path)
     ref, scale = oracle_rhs(prob, parts=True)
     assert parity_error(got, ref, scale) <= FP64_RTOL
 
 
 @pytest.mark.parametrize("equation", EQUATIONS)
-def test_parity_anisotropic_box(equation):
+@pytest.mark.parametrize("path", PATHS)
+def test_parity_anisotropic_box(equation, path):
     """n = (5, 2, 3) hexahedra per axis: a tile tail and uneven neighbours."""
     prob = make_problem(equation, generate_box_tet_mesh((0, 0, 0), (2.0, 0.5, 1.0),
                                                         (5, 2, 3)), 2, seed=3)
-    got, _ = _gpu_rhs(prob)
+    got, _ = _gpu_rhs(prob, path)
     ref, scale = oracle_rhs(prob, parts=True)
     assert parity_error(got, ref, scale) <= FP64_RTOL
 
 
-def test_deterministic_bitwise():
+@pytest.mark.parametrize("path", PATHS)
+def test_deterministic_bitwise(path):
     prob = make_problem("euler", jittered_box_mesh(4), 3)
-    a, plan = _gpu_rhs(prob)
-    b, _ = _gpu_rhs(prob)
+    a, plan = _gpu_rhs(prob, path)
+    b, _ = _gpu_rhs(prob, path)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("equation", EQUATIONS)
+def test_paths_agree_and_launch_counts(equation):
+    """The two FP64 paths agree to round-off; the shared path reports its
+    extra launches and owns each interior face once."""
+    prob = make_problem(equation, jittered_box_mesh(4), 2, seed=5)
+    a, plan_s = _gpu_rhs(prob, "shared")
+    b, plan_f = _gpu_rhs(prob, "fused")
+    assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b)
+    info_s, info_f = plan_s.info(), plan_f.info()
+    assert info_s["launches_per_rhs"] == (3 if equation == "euler" else 2)
+    assert info_f["launches_per_rhs"] == 1 and not info_f["face_shared"]
+    d = prob.disc
+    nbdry = int((d.neighbor < 0).sum())
+    assert info_s["owned_faces"] == nbdry + (4 * d.nelements - nbdry) // 2
+
+
+def test_inconsistent_partner_rejected():
+    """A partner table that does not pair whole faces consistently with the
+    gather index is refused at plan creation (checked by the ownership
+    kernel, which reads only in-range indices)."""
+    import torch
+
+    from actx_dgfem_suite_gb300._lib import DGError
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem("wave", jittered_box_mesh(3), 2)
+    dm = DeviceMesh(prob.disc, "cuda:0", with_partner=True)
+    part = prob.disc.face_partner().copy()
+    inner = np.flatnonzero(part.reshape(-1) >= 0)
+    bad = part.reshape(-1)
+    i, j = inner[0], inner[-1]
+    bad[i], bad[j] = bad[j], bad[i]          # two points now point at wrong faces
+    dm.partner = torch.from_numpy(bad.reshape(part.shape)).to("cuda:0")
+    with pytest.raises(DGError, match="face_partner"):
+        DevicePlan(dm, "wave", prob.params)
+    bad2 = part.reshape(-1).copy()
+    bad2[inner[0]] = 10**9                    # out of range: rejected, never read
+    dm.partner = torch.from_numpy(bad2.reshape(part.shape)).to("cuda:0")
+    with pytest.raises(DGError, match="face_partner"):
+        DevicePlan(dm, "wave", prob.params)
