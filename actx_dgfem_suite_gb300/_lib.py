@@ -25,6 +25,7 @@ DG_MAXWELL = 2
 
 DG_FP64 = 0
 DG_FP32_MIXED = 1
+DG_FP64_TC = 2
 
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
@@ -125,7 +126,7 @@ def lib() -> ctypes.CDLL:
     L.dg_plan_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), i32p, i32p,
                                i32p, i32p, i32p]
     L.dg_plan_info.restype = ctypes.c_int
-    L.dg_plan_path.argtypes = [vp, i32p, i32p, ctypes.POINTER(ctypes.c_int64)]
+    L.dg_plan_path.argtypes = [vp, i32p, i32p, i32p, ctypes.POINTER(ctypes.c_int64)]
     L.dg_plan_path.restype = ctypes.c_int
     L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, vp]

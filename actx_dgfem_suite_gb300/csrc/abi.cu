@@ -148,6 +148,12 @@ struct dg_plan {
   double* d_aux = nullptr;     // euler: (3, Nel, Np)
   int face_grid = 0, aux_grid = 0;
   const int32_t* d_face_nodes = nullptr;  // inside d_ops
+  // tensor-core contractions (DG_FP64_TC on the face-shared path)
+  bool tc = false;
+  void* d_tc_ops = nullptr;
+  uint32_t tc_ops_bytes = 0;
+  dg::LaunchShape tc_shape;
+  int tc_grid = 0;
   // face-shared path and adjoint (wave, FP64): the mesh's face_partner
   const int32_t* face_partner = nullptr;
   void* d_adj_ops = nullptr;
@@ -345,6 +351,96 @@ void pack_ops_fp32(std::vector<unsigned char>& buf, const dg::OpsOffsets& off,
   for (int k = 0; k < 4 * nfp; ++k) fn[k] = face_nodes[k];
 }
 
+// {{{ operator digits for the tensor-core kernel (layout: tc::Plan in dg_tc.cuh)
+
+int r16h(int x) { return (x + 15) & ~15; }
+
+// One product's block: A (m x k, element (r, c) = at(r, c)) as 8 digit slices
+// of its rows' 54-bit fixed-point integers, then the row exponents.
+template <class At>
+int pack_gemm(unsigned char* out, int m, int k, At at) {
+  const int mp = r16h(m), kp = r16h(k), mt = mp / 16, kt = kp / 16;
+  const int digits = 8 * mt * kt * 256;
+  const int bytes = (digits + mp * 4 + 15) & ~15;
+  if (!out) return bytes;
+  std::memset(out, 64, digits);          // digit 0 (biased)
+  std::memset(out + digits, 0, bytes - digits);
+  int32_t* row_exp = reinterpret_cast<int32_t*>(out + digits);
+  for (int r = 0; r < m; ++r) {
+    double mx = 0.0;
+    for (int c = 0; c < k; ++c) mx = std::fmax(mx, std::fabs(at(r, c)));
+    int e = 0;
+    if (mx > 0.0) std::frexp(mx, &e);    // |A_rc| < 2^e
+    row_exp[r] = e;
+    for (int c = 0; c < k; ++c) {
+      long long x = std::llrint(std::ldexp(at(r, c), 54 - e));
+      // balanced base-128 digits, least significant first (slice 7)
+      const int rr = r & 15, cc = c & 15;
+      const int lane = (rr & 7) * 4 + ((cc & 7) >> 1);
+      const int reg = (rr >> 3) + 2 * (cc >> 3);
+      const int within = lane * 8 + reg * 2 + (cc & 1);
+      for (int sl = 7; sl >= 0; --sl) {
+        const long long d = ((x + 64) & 127) - 64;
+        x = (x - d) >> 7;
+        out[((sl * mt + (r >> 4)) * kt + (c >> 4)) * 256 + within] =
+            static_cast<unsigned char>(d + 64);
+      }
+    }
+  }
+  return bytes;
+}
+
+}  // namespace
+
+namespace dg {
+int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
+                unsigned char* out, int out_bytes) {
+  const int np = (order + 1) * (order + 2) * (order + 3) / 6;
+  const int nfpt = 2 * (order + 1) * (order + 2);
+  auto g1 = [&](int r, int c) { return diff[(size_t)r * np + c]; };  // [A_0; A_1; A_2]
+  auto g2 = [&](int r, int c) {                                      // [A_0 A_1 A_2]
+    const int q = c / np;
+    return diff[((size_t)q * np + r) * np + (c - q * np)];
+  };
+  auto gl = [&](int r, int c) { return lift[(size_t)r * nfpt + c]; };
+  const bool has_g1 = eq != DG_EULER, has_g2 = eq != DG_MAXWELL;
+  int total = 0;
+  if (has_g1) total += pack_gemm(nullptr, 3 * np, np, g1);
+  if (has_g2) total += pack_gemm(nullptr, np, 3 * np, g2);
+  total += pack_gemm(nullptr, np, nfpt, gl);
+  if (!out) return total;
+  if (out_bytes != total) return -1;
+  int off = 0;
+  if (has_g1) off += pack_gemm(out + off, 3 * np, np, g1);
+  if (has_g2) off += pack_gemm(out + off, np, 3 * np, g2);
+  pack_gemm(out + off, np, nfpt, gl);
+  return total;
+}
+}  // namespace dg
+
+namespace {
+
+cudaError_t tc_shape_of(int eq, int order, int mode, dg::LaunchShape* out) {
+  switch (eq) {
+    case DG_WAVE: return dg::tc_shape_wave(order, mode, out);
+    case DG_EULER: return dg::tc_shape_euler(order, mode, out);
+    case DG_MAXWELL: return dg::tc_shape_maxwell(order, mode, out);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t tc_launch_of(int eq, int order, int mode, const dg::RhsArgs& a, int grid,
+                         cudaStream_t s) {
+  switch (eq) {
+    case DG_WAVE: return dg::tc_launch_wave(order, mode, a, grid, s);
+    case DG_EULER: return dg::tc_launch_euler(order, mode, a, grid, s);
+    case DG_MAXWELL: return dg::tc_launch_maxwell(order, mode, a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// }}}
+
 }  // namespace
 
 extern "C" {
@@ -362,8 +458,9 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   if (!mesh) return fail(DG_ERR_ARGUMENT, "mesh description is NULL");
   const int nf = nfields_of(equation);
   if (nf == 0) return fail(DG_ERR_ARGUMENT, "unknown equation");
-  if (precision != DG_FP64 && precision != DG_FP32_MIXED)
+  if (precision != DG_FP64 && precision != DG_FP32_MIXED && precision != DG_FP64_TC)
     return fail(DG_ERR_ARGUMENT, "unknown precision");
+  const int kprec = precision == DG_FP32_MIXED ? 1 : 0;  // kernel arithmetic type
   if (mesh->order < 1 || mesh->order > 4)
     return fail(DG_ERR_UNSUPPORTED, "order must be 1..4");
   if (mesh->nelements < 1) return fail(DG_ERR_ARGUMENT, "nelements must be >= 1");
@@ -399,8 +496,9 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
 
   // face-shared path: FP64 plans on meshes that carry face_partner and whose
   // face points fit 31-bit indices; the fused kernel serves all others
-  const bool split = mesh->face_partner && precision == DG_FP64 &&
+  const bool split = mesh->face_partner && kprec == 0 &&
                      mesh->nelements * 4 * (int64_t)nfp < (int64_t(1) << 31);
+  const bool tc = split && precision == DG_FP64_TC;
   if (mesh->face_partner) {
     cudaPointerAttributes attr;
     if (cudaPointerGetAttributes(&attr, mesh->face_partner) != cudaSuccess ||
@@ -411,23 +509,23 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   }
 
   dg::LaunchShape shape;
-  cudaError_t err = shape_of(equation, N, precision, 0, &shape);
+  cudaError_t err = shape_of(equation, N, kprec, 0, &shape);
   for (int mode = 1; mode < (split ? 4 : 2) && err == cudaSuccess; ++mode) {
     dg::LaunchShape other;
-    err = shape_of(equation, N, precision, mode, &other);
+    err = shape_of(equation, N, kprec, mode, &other);
     if (other.blocks_per_sm < shape.blocks_per_sm)
       shape.blocks_per_sm = other.blocks_per_sm;
   }
   if (err != cudaSuccess) return cuda_fail(err, "kernel configuration");
   if (shape.blocks_per_sm < 1)
     return fail(DG_ERR_UNSUPPORTED, "kernel does not fit on an SM");
-  const int rs = precision == DG_FP64 ? 8 : 4;
+  const int rs = kprec == 0 ? 8 : 4;
   const dg::OpsOffsets off = dg::ops_offsets(np, nfp, rs);
   if (off.size != shape.ops_bytes)
     return fail(DG_ERR_CUDA, "operator layout mismatch between host and kernel");
 
   std::vector<unsigned char> ops(off.size, 0);
-  if (precision == DG_FP64)
+  if (kprec == 0)
     pack_ops_fp64(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
   else
     pack_ops_fp32(ops, off, np, nfp, diff, mesh->lift, mesh->face_nodes);
@@ -485,7 +583,40 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     }
   }
 
-  if (mesh->face_partner && equation == DG_WAVE && precision == DG_FP64) {
+  if (tc) {
+    dg::LaunchShape ts, ts_stage;
+    err = tc_shape_of(equation, N, 0, &ts);
+    if (err == cudaSuccess) err = tc_shape_of(equation, N, 1, &ts_stage);
+    if (err != cudaSuccess) {
+      dg_plan_destroy(p);
+      return cuda_fail(err, "tensor-core kernel configuration");
+    }
+    if (ts_stage.blocks_per_sm < ts.blocks_per_sm) ts.blocks_per_sm = ts_stage.blocks_per_sm;
+    const int bytes = dg::pack_tc_ops(equation, N, diff, mesh->lift, nullptr, 0);
+    if (bytes != ts.ops_bytes || ts.blocks_per_sm < 1) {
+      dg_plan_destroy(p);
+      return fail(DG_ERR_CUDA, ts.blocks_per_sm < 1
+                                   ? "tensor-core kernel does not fit on an SM"
+                                   : "tensor-core operator layout mismatch");
+    }
+    std::vector<unsigned char> tops(bytes);
+    dg::pack_tc_ops(equation, N, diff, mesh->lift, tops.data(), bytes);
+    err = cudaMalloc(&p->d_tc_ops, bytes);
+    if (err == cudaSuccess)
+      err = cudaMemcpy(p->d_tc_ops, tops.data(), bytes, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) {
+      dg_plan_destroy(p);
+      return cuda_fail(err, "tensor-core operator buffer");
+    }
+    p->tc = true;
+    p->tc_ops_bytes = static_cast<uint32_t>(bytes);
+    p->tc_shape = ts;
+    const int64_t tiles = (p->nel + ts.elems_per_tile - 1) / ts.elems_per_tile;
+    const int64_t tfull = (int64_t)nsm * ts.blocks_per_sm;
+    p->tc_grid = (int)(tiles < tfull ? tiles : tfull);
+  }
+
+  if (mesh->face_partner && equation == DG_WAVE && kprec == 0) {
     if (p->nel * 8 * (int64_t)nfp >= (int64_t(1) << 32)) {
       dg_plan_destroy(p);
       return fail(DG_ERR_ARGUMENT, "mesh too large for the adjoint's 32-bit face indices");
@@ -584,8 +715,15 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     cudaError_t err = launch_faces(p, q, s);
     if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
   }
-  cudaError_t err = launch_of(p->equation, p->order, p->precision,
-                              p->split ? dg::MODE_SPLIT : dg::MODE_RHS, a, p->grid, s);
+  cudaError_t err;
+  if (p->tc) {
+    a.ops = p->d_tc_ops;
+    a.ops_bytes = p->tc_ops_bytes;
+    err = tc_launch_of(p->equation, p->order, 0, a, p->tc_grid, s);
+  } else {
+    err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
+                    p->split ? dg::MODE_SPLIT : dg::MODE_RHS, a, p->grid, s);
+  }
   if (err != cudaSuccess) return cuda_fail(err, "rhs launch");
   return DG_OK;
 }
@@ -618,9 +756,15 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     cudaError_t err = launch_faces(p, q_in, s);
     if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
   }
-  cudaError_t err = launch_of(p->equation, p->order, p->precision,
-                              dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0), a,
-                              p->grid, s);
+  cudaError_t err;
+  if (p->tc) {
+    a.ops = p->d_tc_ops;
+    a.ops_bytes = p->tc_ops_bytes;
+    err = tc_launch_of(p->equation, p->order, 1, a, p->tc_grid, s);
+  } else {
+    err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
+                    dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0), a, p->grid, s);
+  }
   if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
   return DG_OK;
 }
@@ -706,7 +850,8 @@ int dg_plan_destroy(dg_plan* p) {
   if (p->d_ops && cudaFree(p->d_ops) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_status && cudaFree(p->d_status) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
-  for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux})
+  for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux,
+                  (void*)p->d_tc_ops})
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
@@ -724,10 +869,11 @@ int dg_fp64_fma_probe(double* out, int64_t iters, int32_t grid, int32_t block,
   return DG_OK;
 }
 
-int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* launches_per_rhs,
-                 int64_t* owned_faces) {
+int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* tensor_cores,
+                 int32_t* launches_per_rhs, int64_t* owned_faces) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (face_shared) *face_shared = p->split ? 1 : 0;
+  if (tensor_cores) *tensor_cores = p->tc ? 1 : 0;
   if (launches_per_rhs)
     *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : 1;
   if (owned_faces) *owned_faces = p->split ? p->nowned : 0;
@@ -741,9 +887,9 @@ int dg_plan_info(const dg_plan* p, int64_t* nelements, int32_t* order,
   if (nelements) *nelements = p->nel;
   if (order) *order = p->order;
   if (nfields) *nfields = p->nfields;
-  if (grid) *grid = p->grid;
+  if (grid) *grid = p->tc ? p->tc_grid : p->grid;
   if (block) *block = dg::kBlock;
-  if (smem_bytes) *smem_bytes = p->shape.smem_bytes;
+  if (smem_bytes) *smem_bytes = p->tc ? p->tc_shape.smem_bytes : p->shape.smem_bytes;
   return DG_OK;
 }
 

@@ -50,6 +50,8 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
 // cudaErrorInvalidValue for a combination that is not compiled in.
 // face_blocks_*: resident CTAs per SM of the face kernel; face_launch_*:
 // (Euler: the per-node table, then) the face kernel of the face-shared path.
+// tc_shape_* / tc_launch_*: the face-shared volume/LIFT kernel with the
+// contractions on the tensor cores (mode 0 RHS, 1 RK stage).
 #define DG_DECLARE_EQ(name)                                                   \
   cudaError_t shape_##name(int order, int precision, int mode,               \
                            LaunchShape* out);                                \
@@ -57,11 +59,23 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
                             const RhsArgs& a, int grid, cudaStream_t s);     \
   cudaError_t face_blocks_##name(int order, int* blocks_per_sm);             \
   cudaError_t face_launch_##name(int order, const FaceArgs& a, int grid,     \
-                                 int aux_grid, cudaStream_t s);
+                                 int aux_grid, cudaStream_t s);              \
+  cudaError_t tc_shape_##name(int order, int mode, LaunchShape* out);        \
+  cudaError_t tc_launch_##name(int order, int mode, const RhsArgs& a,        \
+                               int grid, cudaStream_t s);
 DG_DECLARE_EQ(wave)
 DG_DECLARE_EQ(euler)
 DG_DECLARE_EQ(maxwell)
 #undef DG_DECLARE_EQ
+
+// Operator block of the tensor-core kernel (layout of tc::Plan<N, EQ> in
+// dg_tc.cuh): products G1 = [A_0; A_1; A_2] (3 Np x Np, wave and maxwell),
+// G2 = [A_0 A_1 A_2] (Np x 3 Np, wave and euler), GL = LIFT (Np x 4 Nfp).
+// Each: 8 digit slices of 256-byte blocks (slice, m-tile, k-step) in mma A
+// fragment lane order, int8 digits + 64, then one int32 exponent per padded
+// row; blocks padded to 16 bytes.  Returns the block size.
+int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
+                unsigned char* out, int out_bytes);
 
 // Record `msg` as the calling thread's last error (dg_last_error) and
 // return `code`; shared by the translation units behind the C ABI.

@@ -1,5 +1,6 @@
 // RHS kernels for the euler equation: orders 1..4, FP64 and mixed
-// precision, plain RHS and fused RK stage.
+// precision, plain RHS and fused RK stage; face-shared FP64 forms with FP64
+// or tensor-core contractions.
 #include "rhs_instantiate.cuh"
 
 namespace dg {
@@ -16,5 +17,12 @@ cudaError_t face_blocks_euler(int order, int* blocks_per_sm) {
 cudaError_t face_launch_euler(int order, const FaceArgs& a, int grid, int aux_grid,
                            cudaStream_t s) {
   return face_launch_any<DG_EULER>(order, a, grid, aux_grid, s);
+}
+cudaError_t tc_shape_euler(int order, int mode, LaunchShape* out) {
+  return tc_shape_any<DG_EULER>(order, mode, out);
+}
+cudaError_t tc_launch_euler(int order, int mode, const RhsArgs& a, int grid,
+                        cudaStream_t s) {
+  return tc_launch_any<DG_EULER>(order, mode, a, grid, s);
 }
 }  // namespace dg

@@ -7,6 +7,7 @@
 #include <type_traits>
 
 #include "dg_face.cuh"
+#include "dg_tc.cuh"
 #include "dg_launch.h"
 #include "dg_rhs.cuh"
 
@@ -150,6 +151,67 @@ cudaError_t face_launch_any(int order, const FaceArgs& a, int grid, int aux_grid
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+// }}}
+
+// {{{ FP64 with tensor-core contractions (face-shared path only)
+
+template <int N, int EQ, int MODE>
+cudaError_t tc_shape_impl(LaunchShape* out) {
+  using P = tc::Plan<N, EQ>;
+  auto kern = dg_rhs_tc_kernel<N, EQ, MODE>;
+  cudaError_t err = cudaFuncSetAttribute(
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
+  if (err != cudaSuccess) return err;
+  int nb = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, P::SMEM_BYTES);
+  out->smem_bytes = P::SMEM_BYTES;
+  out->blocks_per_sm = nb;
+  out->elems_per_tile = P::E;
+  out->ops_bytes = P::OPS_BYTES;
+  return err;
+}
+
+template <int N, int EQ>
+cudaError_t tc_shape_n(int mode, LaunchShape* out) {
+  return mode == 0 ? tc_shape_impl<N, EQ, MODE_SPLIT>(out)
+                   : tc_shape_impl<N, EQ, MODE_SPLIT | MODE_STAGE>(out);
+}
+
+template <int N, int EQ>
+cudaError_t tc_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
+  using P = tc::Plan<N, EQ>;
+  if (mode == 0)
+    dg_rhs_tc_kernel<N, EQ, MODE_SPLIT><<<grid, kBlock, P::SMEM_BYTES, s>>>(a);
+  else
+    dg_rhs_tc_kernel<N, EQ, MODE_SPLIT | MODE_STAGE><<<grid, kBlock, P::SMEM_BYTES, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int EQ>
+cudaError_t tc_shape_any(int order, int mode, LaunchShape* out) {
+  if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
+  switch (order) {
+    case 1: return tc_shape_n<1, EQ>(mode, out);
+    case 2: return tc_shape_n<2, EQ>(mode, out);
+    case 3: return tc_shape_n<3, EQ>(mode, out);
+    case 4: return tc_shape_n<4, EQ>(mode, out);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int EQ>
+cudaError_t tc_launch_any(int order, int mode, const RhsArgs& a, int grid,
+                          cudaStream_t s) {
+  if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
+  switch (order) {
+    case 1: return tc_launch_n<1, EQ>(mode, a, grid, s);
+    case 2: return tc_launch_n<2, EQ>(mode, a, grid, s);
+    case 3: return tc_launch_n<3, EQ>(mode, a, grid, s);
+    case 4: return tc_launch_n<4, EQ>(mode, a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 // }}}

@@ -98,13 +98,16 @@ class DeviceMesh:
                    for t in (self.metric, self.face_geom, self.gather))
 
 
-PRECISIONS = {"fp64": _lib.DG_FP64, "fp32-mixed": _lib.DG_FP32_MIXED}
+PRECISIONS = {"fp64": _lib.DG_FP64, "fp32-mixed": _lib.DG_FP32_MIXED,
+              "fp64-tc": _lib.DG_FP64_TC}
 
 
 class DevicePlan:
     """One compiled RHS: ``rhs(q, out)`` with q, out of shape (nfields, Nel, Np).
 
-    ``precision``: ``"fp64"`` (plain path) or ``"fp32-mixed"`` (FP32
+    ``precision``: ``"fp64"`` (FP64 arithmetic throughout), ``"fp64-tc"``
+    (FP64 results; with face partners the contractions run on the tensor
+    cores as an exact FP64 emulation) or ``"fp32-mixed"`` (FP32
     derivative/flux arithmetic, FP64 state, FP64 Euler pressure recovery and
     FP64 RK accumulation)."""
 
@@ -140,12 +143,14 @@ class DevicePlan:
         _lib.check(self._lib.dg_plan_info(self._handle, ctypes.byref(nel),
                                           *[ctypes.byref(v) for v in vals]))
         order, nf, grid, block, smem = (v.value for v in vals)
-        shared, launches = ctypes.c_int32(), ctypes.c_int32()
+        shared, tcores, launches = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         owned = ctypes.c_int64()
         _lib.check(self._lib.dg_plan_path(self._handle, ctypes.byref(shared),
-                                          ctypes.byref(launches), ctypes.byref(owned)))
+                                          ctypes.byref(tcores), ctypes.byref(launches),
+                                          ctypes.byref(owned)))
         return dict(nelements=nel.value, order=order, nfields=nf, grid=grid,
                     block=block, smem_bytes=smem, face_shared=bool(shared.value),
+                    tensor_cores=bool(tcores.value),
                     launches_per_rhs=launches.value, owned_faces=owned.value)
 
     @property

@@ -452,12 +452,17 @@ def our_arm(args) -> None:
     achieved_gbs = c.bytes / t_dom / 1e9
     info = rd["compiled"].plan.info()
     path = "shared" if info["face_shared"] else "fused"
+    if info["tensor_cores"]:
+        path = "tc"
     traffic = _ncu_traffic(path).get(f"{rd['eq']}{rd['order']}")
-    if traffic is not None and (args.scale != 1 or args.precision != "fp64"):
+    if traffic is not None and (args.scale != 1 or args.precision == "fp32-mixed"):
         traffic = None
-    kname = (f"dg_rhs_kernel<{rd['order']}, {rd['eq']}, "
-             f"{'double' if args.precision == 'fp64' else 'float'}, "
-             f"{'SPLIT' if info['face_shared'] else 'RHS'}>")
+    if info["tensor_cores"]:
+        kname = f"dg_rhs_tc_kernel<{rd['order']}, {rd['eq']}, SPLIT>"
+    else:
+        kname = (f"dg_rhs_kernel<{rd['order']}, {rd['eq']}, "
+                 f"{'float' if args.precision == 'fp32-mixed' else 'double'}, "
+                 f"{'SPLIT' if info['face_shared'] else 'RHS'}>")
     if info["face_shared"]:
         kname = (f"dg_face_flux_kernel<{rd['order']}, {rd['eq']}>"
                  + (" + dg_euler_aux_kernel" if rd["eq"] == "euler" else "")
@@ -503,7 +508,7 @@ def our_arm(args) -> None:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": K, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f32 (f64 state)",
+            "dtype": "f32 (f64 state)" if args.precision == "fp32-mixed" else "f64",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "problem": "baseline definitions",
                        "precision": args.precision,
@@ -542,7 +547,7 @@ def main(argv=None):
                     help="skip the mixed-precision, ensemble and adjoint extras")
     ap.add_argument("--host-setup", action="store_true",
                     help="build meshes on the host (NumPy) instead of on the GPU")
-    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32-mixed"),
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp64-tc", "fp32-mixed"),
                     help="arithmetic of the timed RHS (the benchmark metric is fp64)")
     args = ap.parse_args(argv)
     if args.impl == "reference":

@@ -47,7 +47,14 @@ enum dg_equation { DG_WAVE = 0, DG_EULER = 1, DG_MAXWELL = 2 };
  * operators and geometry, while the state stays FP64 in memory, the Euler
  * pressure is recovered from total energy in FP64, and RK stage updates
  * accumulate in FP64. */
-enum dg_precision { DG_FP64 = 0, DG_FP32_MIXED = 1 };
+/* DG_FP64: FP64 arithmetic throughout (contractions as FP64 FMAs).
+ * DG_FP32_MIXED: FP32 derivative/flux/LIFT arithmetic, FP64 state, FP64
+ *   Euler pressure recovery and FP64 RK accumulation.
+ * DG_FP64_TC: FP64 state and results with the volume and LIFT contractions
+ *   on the tensor cores as an exact FP64 emulation by FP16 digit slices
+ *   (error ~2^-53 of sum |A||x|, the size of FP64 rounding); needs the
+ *   face-shared path (see dg_plan_create), else it falls back to DG_FP64. */
+enum dg_precision { DG_FP64 = 0, DG_FP32_MIXED = 1, DG_FP64_TC = 2 };
 
 typedef struct dg_plan dg_plan;
 
@@ -189,10 +196,11 @@ int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 int dg_plan_destroy(dg_plan* plan);
 
 /* Which path the plan takes: face_shared 1 for the face-shared path, 0 for
- * the single fused launch; launches_per_rhs = kernel launches of one dg_rhs
+ * the single fused launch; tensor_cores 1 when the contractions run on the
+ * tensor cores (DG_FP64_TC on the face-shared path); launches_per_rhs = kernel launches of one dg_rhs
  * or dg_rk_stage; owned_faces = faces whose flux the face kernel evaluates.
  * Any output pointer may be NULL. */
-int dg_plan_path(const dg_plan* plan, int32_t* face_shared,
+int dg_plan_path(const dg_plan* plan, int32_t* face_shared, int32_t* tensor_cores,
                  int32_t* launches_per_rhs, int64_t* owned_faces);
 
 /* Describe a plan: any output pointer may be NULL.  grid/block/smem are the

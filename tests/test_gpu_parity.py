@@ -1,8 +1,10 @@
 """FP64 parity of the CUDA RHS kernels against the CPU oracle, through the
 C ABI (DevicePlan -> dg_rhs).  Bound: relative L2 <= 1e-12.
 
-Both FP64 paths are covered: ``shared`` (mesh uploaded with face partners:
-face kernel evaluates each glued pair's flux once, then volume + LIFT) and
+All FP64 paths are covered: ``tc`` (``fp64-tc``, mesh uploaded with face
+partners: face kernel evaluates each glued pair's flux once, then volume +
+LIFT with the contractions on the tensor cores as an exact FP64 emulation),
+``shared`` (the same split with FP64-FMA contractions, the ``fp64`` default) and
 ``fused`` (no partners: one launch computes every face point's flux)."""
 
 from __future__ import annotations
@@ -19,16 +21,19 @@ pytestmark = pytest.mark.gpu
 
 EQUATIONS = ("wave", "euler", "maxwell")
 ORDERS = (1, 2, 3, 4)
-PATHS = ("shared", "fused")
+PATHS = ("tc", "shared", "fused")
 
 
-def _gpu_rhs(problem, path="shared"):
+def _gpu_rhs(problem, path="tc"):
     import torch
 
     from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
-    dm = DeviceMesh(problem.disc, "cuda:0", with_partner=(path == "shared"))
-    plan = DevicePlan(dm, problem.equation, problem.params)
-    assert plan.info()["face_shared"] == (path == "shared")
+    dm = DeviceMesh(problem.disc, "cuda:0", with_partner=(path != "fused"))
+    plan = DevicePlan(dm, problem.equation, problem.params,
+                      "fp64-tc" if path == "tc" else "fp64")
+    info = plan.info()
+    assert info["face_shared"] == (path != "fused")
+    assert info["tensor_cores"] == (path == "tc")
     q = torch.from_numpy(problem.fields).to("cuda:0")
     out = plan.rhs(q)
     plan.finish()
@@ -101,7 +106,10 @@ def test_paths_agree_and_launch_counts(equation):
     prob = make_problem(equation, jittered_box_mesh(4), 2, seed=5)
     a, plan_s = _gpu_rhs(prob, "shared")
     b, plan_f = _gpu_rhs(prob, "fused")
+    c, plan_t = _gpu_rhs(prob, "tc")
     assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b)
+    assert np.linalg.norm(c - b) <= 1e-13 * np.linalg.norm(b)
+    assert plan_t.info()["launches_per_rhs"] == plan_s.info()["launches_per_rhs"]
     info_s, info_f = plan_s.info(), plan_f.info()
     assert info_s["launches_per_rhs"] == (3 if equation == "euler" else 2)
     assert info_f["launches_per_rhs"] == 1 and not info_f["face_shared"]
