@@ -355,16 +355,28 @@ void pack_ops_fp32(std::vector<unsigned char>& buf, const dg::OpsOffsets& off,
 
 int r16h(int x) { return (x + 15) & ~15; }
 
-// One product's block: A (m x k, element (r, c) = at(r, c)) as 8 digit slices
-// of its rows' 54-bit fixed-point integers, then the row exponents.
+// IEEE half bits of an integer |d| <= 2048 (exact)
+uint16_t half_bits(int d) {
+  if (d == 0) return 0;
+  const uint16_t sign = d < 0 ? 0x8000 : 0;
+  const int a = d < 0 ? -d : d;
+  int e = 0;
+  while ((a >> (e + 1)) != 0) ++e;                 // 2^e <= a < 2^(e+1)
+  const int mant = ((a << 10) >> e) & 0x3ff;
+  return static_cast<uint16_t>(sign | ((e + 15) << 10) | mant);
+}
+
+// One product's block: A (m x k, element (r, c) = at(r, c)) as 8 FP16 digit
+// slices of its rows' 54-bit fixed-point integers (balanced base-128 digits,
+// slice 0 most significant), in 512-byte ldmatrix.x4 blocks per (slice,
+// m-tile, k-step), then the row exponents.
 template <class At>
 int pack_gemm(unsigned char* out, int m, int k, At at) {
   const int mp = r16h(m), kp = r16h(k), mt = mp / 16, kt = kp / 16;
-  const int digits = 8 * mt * kt * 256;
+  const int digits = 8 * mt * kt * 512;
   const int bytes = (digits + mp * 4 + 15) & ~15;
   if (!out) return bytes;
-  std::memset(out, 64, digits);          // digit 0 (biased)
-  std::memset(out + digits, 0, bytes - digits);
+  std::memset(out, 0, bytes);             // FP16 zero
   int32_t* row_exp = reinterpret_cast<int32_t*>(out + digits);
   for (int r = 0; r < m; ++r) {
     double mx = 0.0;
@@ -374,16 +386,15 @@ int pack_gemm(unsigned char* out, int m, int k, At at) {
     row_exp[r] = e;
     for (int c = 0; c < k; ++c) {
       long long x = std::llrint(std::ldexp(at(r, c), 54 - e));
-      // balanced base-128 digits, least significant first (slice 7)
       const int rr = r & 15, cc = c & 15;
-      const int lane = (rr & 7) * 4 + ((cc & 7) >> 1);
-      const int reg = (rr >> 3) + 2 * (cc >> 3);
-      const int within = lane * 8 + reg * 2 + (cc & 1);
-      for (int sl = 7; sl >= 0; --sl) {
+      const int within = ((rr >> 3) + 2 * (cc >> 3)) * 128 + (rr & 7) * 16 + (cc & 7) * 2;
+      for (int sl = 7; sl >= 0; --sl) {   // least significant digit first
         const long long d = ((x + 64) & 127) - 64;
         x = (x - d) >> 7;
-        out[((sl * mt + (r >> 4)) * kt + (c >> 4)) * 256 + within] =
-            static_cast<unsigned char>(d + 64);
+        const uint16_t h = half_bits(static_cast<int>(d));
+        unsigned char* dst = out + ((sl * mt + (r >> 4)) * kt + (c >> 4)) * 512 + within;
+        dst[0] = static_cast<unsigned char>(h & 0xff);
+        dst[1] = static_cast<unsigned char>(h >> 8);
       }
     }
   }
@@ -397,23 +408,21 @@ int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
                 unsigned char* out, int out_bytes) {
   const int np = (order + 1) * (order + 2) * (order + 3) / 6;
   const int nfpt = 2 * (order + 1) * (order + 2);
-  auto g1 = [&](int r, int c) { return diff[(size_t)r * np + c]; };  // [A_0; A_1; A_2]
-  auto g2 = [&](int r, int c) {                                      // [A_0 A_1 A_2]
+  auto stacked = [&](int r, int c) { return diff[(size_t)r * np + c]; };  // [A_0; A_1; A_2]
+  auto concat = [&](int r, int c) {                                      // [A_0 A_1 A_2]
     const int q = c / np;
     return diff[((size_t)q * np + r) * np + (c - q * np)];
   };
   auto gl = [&](int r, int c) { return lift[(size_t)r * nfpt + c]; };
-  const bool has_g1 = eq != DG_EULER, has_g2 = eq != DG_MAXWELL;
-  int total = 0;
-  if (has_g1) total += pack_gemm(nullptr, 3 * np, np, g1);
-  if (has_g2) total += pack_gemm(nullptr, np, 3 * np, g2);
-  total += pack_gemm(nullptr, np, nfpt, gl);
+  const bool st = eq != DG_EULER;
+  const int gv = st ? pack_gemm(nullptr, 3 * np, np, stacked)
+                    : pack_gemm(nullptr, np, 3 * np, concat);
+  const int total = gv + pack_gemm(nullptr, np, nfpt, gl);
   if (!out) return total;
   if (out_bytes != total) return -1;
-  int off = 0;
-  if (has_g1) off += pack_gemm(out + off, 3 * np, np, g1);
-  if (has_g2) off += pack_gemm(out + off, np, 3 * np, g2);
-  pack_gemm(out + off, np, nfpt, gl);
+  if (st) pack_gemm(out, 3 * np, np, stacked);
+  else pack_gemm(out, np, 3 * np, concat);
+  pack_gemm(out + gv, np, nfpt, gl);
   return total;
 }
 }  // namespace dg

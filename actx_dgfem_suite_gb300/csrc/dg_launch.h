@@ -69,11 +69,11 @@ DG_DECLARE_EQ(maxwell)
 #undef DG_DECLARE_EQ
 
 // Operator block of the tensor-core kernel (layout of tc::Plan<N, EQ> in
-// dg_tc.cuh): products G1 = [A_0; A_1; A_2] (3 Np x Np, wave and maxwell),
-// G2 = [A_0 A_1 A_2] (Np x 3 Np, wave and euler), GL = LIFT (Np x 4 Nfp).
-// Each: 8 digit slices of 256-byte blocks (slice, m-tile, k-step) in mma A
-// fragment lane order, int8 digits + 64, then one int32 exponent per padded
-// row; blocks padded to 16 bytes.  Returns the block size.
+// dg_tc.cuh): the volume product [A_0; A_1; A_2] (3 Np x Np, wave and
+// maxwell) or [A_0 A_1 A_2] (Np x 3 Np, euler), then LIFT (Np x 4 Nfp).
+// Each: 8 FP16 digit slices of 512-byte blocks (slice, m-tile, k-step) in
+// ldmatrix.x4 order, then one int32 exponent per padded row; blocks padded
+// to 16 bytes.  Returns the block size.
 int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
                 unsigned char* out, int out_bytes);
 

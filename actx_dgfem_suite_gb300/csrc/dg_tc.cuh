@@ -35,6 +35,8 @@
 
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "dg_face.cuh"
 #include "dg_rhs.cuh"
 
@@ -50,64 +52,74 @@ constexpr int r8(int x) { return (x + 7) & ~7; }
 constexpr int p16(int bytes) { return (bytes + 15) & ~15; }
 
 // One emulated product: operator A (M x K) times NC data columns of length K.
-//   operator block (global and shared): int8 digits + 64, blocks of 256 bytes
-//   per (digit s, m-tile, k-step) in lane order (8 bytes per lane: the four
-//   half2 registers of the mma A fragment), then M_P int32 row exponents;
+//   operator block (global and shared): FP16 digits in blocks of 512 bytes per
+//   (digit s, m-tile, k-step), each block the four 8 x 8 matrices of the mma
+//   A fragment in ldmatrix.x4 order (rows 0-7 / 8-15 x columns 0-7 / 8-15),
+//   then M_P int32 row exponents;
 //   data slices (shared): FP16 digits, blocks of 256 bytes per (digit, n-tile,
-//   k-step) in ldmatrix order (two 8 x 8 matrices, row = column n).
+//   k-step) in ldmatrix.x2 order (two 8 x 8 matrices, row = column n).
+// A warp unit covers 1 or 2 m-tiles x 2 n-tiles, so every operator
+// fragment loaded from shared memory feeds two tensor-core products.
 template <int M_, int K_, int NC_>
 struct Gemm {
   static constexpr int M = M_, K = K_, NC = NC_;
   static constexpr int MP = r16(M), KP = r16(K), NCP = r8(NC);
   static constexpr int MT = MP / 16, KT = KP / 16, NT = NCP / 8;
-  static constexpr int NT2 = (NT + 1) / 2;     // n-tile pairs (one warp unit)
-  static constexpr int UNITS = MT * NT2;
-  static constexpr int DIGITS = kS * MT * KT * 256;
+  // warp unit: UM x 2 tiles; UM = 2 only when that still leaves >= 16 units
+  static constexpr int UM = ((MT + 1) / 2) * ((NT + 1) / 2) >= 16 ? 2 : 1;
+  static constexpr int MB = (MT + UM - 1) / UM, NB = (NT + 1) / 2;
+  static constexpr int UNITS = MB * NB;
+  static constexpr int DIGITS = kS * MT * KT * 512;
   static constexpr int OPS_BYTES = p16(DIGITS + MP * 4);
-  static constexpr int SLICE_BYTES = kS * NT * KT * 256;
+  static constexpr int SLICE_STRIDE = NT * KT * 256;   // bytes per digit slice
+  static constexpr int SLICE_BYTES = kS * SLICE_STRIDE;
   static_assert(K <= 112, "exact FP32 level sums need K <= 112");
 };
 
-// Products of one equation at order N: G1 = stacked rows [A_0; A_1; A_2]
-// (3 Np x Np), G2 = concatenated columns [A_0 A_1 A_2] (Np x 3 Np), GL = LIFT.
+// Elements per CTA tile: 256 / Np, fewer at order 4 so the FP16 operator
+// digits and the tile's slices fit in shared memory.
+constexpr int tile_elems(int N, int EQ, int np) {
+  return N < 4 ? 256 / np : (EQ == DG_EULER ? 5 : (EQ == DG_MAXWELL ? 6 : 7));
+}
+
+// Products of one equation at order N.  GV, the volume product:
+//   wave, maxwell: stacked rows [A_0; A_1; A_2] (3 Np x Np) applied to
+//     columns (field f, element e) at n = f E + e -- maxwell the six fields,
+//     wave u and the three metric-combined velocity components (of whose
+//     products only the diagonal blocks are used);
+//   euler: concatenated columns [A_0 A_1 A_2] (Np x 3 Np) applied to the
+//     metric-combined fluxes of each (field, element);
+// GL: LIFT (Np x 4 Nfp) applied to the face values of each (field, element).
 template <int N, int EQ>
 struct Plan {
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
   static constexpr int NF = EqInfo<EQ>::NF;
-  static constexpr int E = kBlock / NP;
-  static constexpr bool HAS_G1 = EQ != DG_EULER;
-  static constexpr bool HAS_G2 = EQ != DG_MAXWELL;
-  // data columns: wave G1/G2 one per element; euler G2, maxwell G1 one per
-  // (field, element) at column k * E + el; LIFT one per (field, element)
-  using G1 = Gemm<3 * NP, NP, (EQ == DG_WAVE ? E : NF * E)>;
-  using G2 = Gemm<NP, 3 * NP, (EQ == DG_WAVE ? E : NF * E)>;
+  static constexpr int E = tile_elems(N, EQ, NP);
+  static constexpr bool STACKED = EQ != DG_EULER;
+  using GV = typename std::conditional<
+      STACKED, Gemm<3 * NP, NP, (EQ == DG_WAVE ? 4 : NF) * E>,
+      Gemm<NP, 3 * NP, NF * E>>::type;
   using GL = Gemm<NP, NFPT, NF * E>;
-  // operator block: [G1 | G2 | GL] (absent products take no space)
-  static constexpr int OPS_G1 = 0;
-  static constexpr int OPS_G2 = OPS_G1 + (HAS_G1 ? G1::OPS_BYTES : 0);
-  static constexpr int OPS_GL = OPS_G2 + (HAS_G2 ? G2::OPS_BYTES : 0);
+  static constexpr int OPS_GV = 0;
+  static constexpr int OPS_GL = GV::OPS_BYTES;
   static constexpr int OPS_BYTES = OPS_GL + GL::OPS_BYTES;
 
   static constexpr int NAUX = EQ == DG_WAVE ? 3 : (EQ == DG_EULER ? 15 : 0);
   static constexpr int cmax(int x, int y) { return x > y ? x : y; }
-  static constexpr int VOL_SLICES = (HAS_G1 ? G1::SLICE_BYTES : 0) +
-                                    (HAS_G2 ? G2::SLICE_BYTES : 0);
-  static constexpr int R1_BYTES = p16(cmax(VOL_SLICES, GL::SLICE_BYTES));
-  static constexpr int OUT_G1 = HAS_G1 ? G1::M * G1::NC : 0;  // doubles
-  static constexpr int OUT_G2 = HAS_G2 ? G2::M * G2::NC : 0;
-  static constexpr int R2_BYTES = p16(8 * cmax(cmax(NAUX * E * NP, OUT_G1 + OUT_G2),
+  static constexpr int R1_BYTES = p16(cmax(GV::SLICE_BYTES, GL::SLICE_BYTES));
+  static constexpr int R2_BYTES = p16(8 * cmax(cmax(NAUX * E * NP, GV::M * GV::NC),
                                                NF * E * NFPT + GL::M * GL::NC));
-  static constexpr int NCOLS = cmax(cmax(HAS_G1 ? G1::NCP : 0, HAS_G2 ? G2::NCP : 0),
-                                    GL::NCP);
+  static constexpr int NCOLS = cmax(GV::NCP, GL::NCP);
   // shared memory: ops | state (FP64) | R1 (slices) | R2 (FP64 scratch) |
-  // metric | column exponents (two sets)
+  // metric | column exponents
   static constexpr int SM_OPS = 0;
   static constexpr int SM_Q = p16(OPS_BYTES);
   static constexpr int SM_R1 = SM_Q + p16(NF * E * NP * 8);
   static constexpr int SM_R2 = SM_R1 + R1_BYTES;
   static constexpr int SM_GEO = SM_R2 + R2_BYTES;
   static constexpr int SM_EXP = SM_GEO + p16(9 * E * 8);
-  static constexpr int SMEM_BYTES = SM_EXP + p16(2 * NCOLS * 4);
+  static constexpr int SMEM_BYTES = SM_EXP + p16(NCOLS * 4);
+  static_assert(SMEM_BYTES <= 227 * 1024, "tile does not fit in shared memory");
 };
 
 // {{{ device helpers
@@ -121,9 +133,9 @@ __device__ __forceinline__ void mma16816(float* c, const uint32_t* a, uint32_t b
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// The "memory" clobber keeps the compiler from moving this shared-memory read
-// above the barrier and the stores that fill the slices: the address is a
-// plain integer, so without it the read is invisible to alias analysis.
+// The "memory" clobbers keep the compiler from moving these shared-memory
+// reads above the barrier and the stores that fill the slices: the address
+// is a plain integer, so without it the read is invisible to alias analysis.
 __device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, uint32_t addr) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
                : "=r"(r0), "=r"(r1)
@@ -131,28 +143,24 @@ __device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, uint32_t add
                : "memory");
 }
 
-// two biased int8 digits (byte + 64 each) -> half2 of the digits: the bit
-// pattern 0x6600 + d is the half 1536 + d for |d| <= 64; one HSUB2 removes
-// the 1536 exactly
-// (bit moves through the __ushort_as_half / __half_as_ushort intrinsics: no
-// pointer type punning, which the optimiser is free to break)
-__device__ __forceinline__ uint32_t digits_to_half2(uint32_t packed16) {
-  const uint32_t bits = packed16 + 0x65C065C0u;
-  const __half2 h = __halves2half2(__ushort_as_half((unsigned short)(bits & 0xffffu)),
-                                   __ushort_as_half((unsigned short)(bits >> 16)));
+__device__ __forceinline__ void ldsm_x4(uint32_t* r, uint32_t addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr)
+               : "memory");
+}
+
+// two digits in [-64, 64] -> half2: the bit pattern 0x6600 + d is the half
+// 1536 + d, and one HSUB2 removes the 1536 exactly (bits move through the
+// __ushort_as_half / __half_as_ushort intrinsics, not pointer punning)
+__device__ __forceinline__ uint32_t digits_to_half2(int d0, int d1) {
+  const __half2 h = __halves2half2(__ushort_as_half((unsigned short)(0x6600 + d0)),
+                                   __ushort_as_half((unsigned short)(0x6600 + d1)));
   const __half2 c = __halves2half2(__ushort_as_half((unsigned short)0x6600u),
                                    __ushort_as_half((unsigned short)0x6600u));
   const __half2 d = __hsub2(h, c);
   return (uint32_t)__half_as_ushort(__low2half(d)) |
          ((uint32_t)__half_as_ushort(__high2half(d)) << 16);
-}
-
-// 8 biased digit bytes (one lane's share of an A fragment) -> a0..a3
-__device__ __forceinline__ void expand_a(const uint2 w, uint32_t* a) {
-  a[0] = digits_to_half2(__byte_perm(w.x, 0u, 0x4140));
-  a[1] = digits_to_half2(__byte_perm(w.x, 0u, 0x4342));
-  a[2] = digits_to_half2(__byte_perm(w.y, 0u, 0x4140));
-  a[3] = digits_to_half2(__byte_perm(w.y, 0u, 0x4342));
 }
 
 // FP32 holding an exact integer |v| < 2^22 -> int32 (FADD + IADD, no conversion unit)
@@ -193,6 +201,27 @@ __device__ __forceinline__ long long to_fixed(double x, int emax) {
   return bits < 0 ? -r : r;
 }
 
+// 8 balanced base-128 digits of |x| <= 2^54, most significant first, with
+// 32-bit arithmetic: the low 28 bits give digits 4..7 (leaving a carry of
+// 0 or 1), the high part plus the carry gives digits 0..3
+__device__ __forceinline__ void digits8(long long x, int* d) {
+  int hi = (int)(x >> 28);
+  int lo = (int)(x & 0x0fffffffLL);
+#pragma unroll
+  for (int s = 7; s >= 4; --s) {
+    const int q = ((lo + 64) & 127) - 64;
+    d[s] = q;
+    lo = (lo - q) >> 7;
+  }
+  hi += lo;
+#pragma unroll
+  for (int s = 3; s >= 0; --s) {
+    const int q = ((hi + 64) & 127) - 64;
+    d[s] = q;
+    hi = (hi - q) >> 7;
+  }
+}
+
 // }}}
 
 // Split data columns into FP16 digit slices (+ column exponent fields).
@@ -200,113 +229,141 @@ __device__ __forceinline__ long long to_fixed(double x, int emax) {
 template <class G, class Src>
 __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_emax,
                                               Src src) {
-  const int t = threadIdx.x;
-  // column exponents (one thread per column)
-  for (int n = t; n < G::NCP; n += kBlock) {
+  const int t = threadIdx.x, lane = t & 31;
+  // column exponents: one warp per column, lanes split the rows
+  for (int n = t >> 5; n < G::NCP; n += kBlock / 32) {
     int em = 0;
     if (n < G::NC)
-      for (int k = 0; k < G::K; ++k) {
+      for (int k = lane; k < G::K; k += 32) {
         const int ex = dexp(src(n, k));
         em = ex > em ? ex : em;
       }
-    col_emax[n] = em;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const int o = __shfl_xor_sync(0xffffffffu, em, off);
+      em = o > em ? o : em;
+    }
+    if (lane == 0) col_emax[n] = em;
   }
   __syncthreads();
-  // digits: one thread per (column, pair of rows)
-  constexpr int KH = G::KP / 2;
-  for (int idx = t; idx < G::NCP * KH; idx += kBlock) {
-    const int n = idx / KH;
-    const int k = 2 * (idx - n * KH);
+  // digits: each warp fills whole 8 x 8 matrices, one 4-byte word (two rows
+  // k, k + 1 of one column) per lane, so the stores are free of bank conflicts
+  constexpr int ITEMS = G::NT * G::KT * 64;
+  for (int idx = t; idx < ITEMS; idx += kBlock) {
+    const int kp4 = idx & 3, nr = (idx >> 2) & 7, kh = (idx >> 5) & 1;
+    const int blk = idx >> 6;                 // nt * KT + kt
+    const int nt = blk / G::KT, kt = blk - nt * G::KT;
+    const int n = nt * 8 + nr;
+    const int k = kt * 16 + kh * 8 + 2 * kp4;
     long long x0 = 0, x1 = 0;
     if (n < G::NC) {
       const int em = col_emax[n];
       if (k < G::K) x0 = to_fixed(src(n, k), em);
       if (k + 1 < G::K) x1 = to_fixed(src(n, k + 1), em);
     }
-    const int nt = n >> 3, kt = k >> 4;
-    unsigned char* dst = slices + (nt * G::KT + kt) * 256 + ((k & 15) >> 3) * 128 +
-                         (n & 7) * 16 + (k & 7) * 2;
+    int d0[kS], d1[kS];
+    digits8(x0, d0);
+    digits8(x1, d1);
+    unsigned char* dst = slices + blk * 256 + kh * 128 + nr * 16 + kp4 * 4;
 #pragma unroll
-    for (int s = kS - 1; s >= 0; --s) {  // least significant digit first
-      const long long d0 = ((x0 + 64) & 127) - 64;
-      const long long d1 = ((x1 + 64) & 127) - 64;
-      x0 = (x0 - d0) >> 7;
-      x1 = (x1 - d1) >> 7;
-      const uint32_t packed =
-          ((uint32_t)(d0 + 64) & 0xffffu) | (((uint32_t)(d1 + 64) & 0xffffu) << 16);
-      *reinterpret_cast<uint32_t*>(dst + s * (G::NT * G::KT * 256)) =
-          digits_to_half2(packed);
-    }
+    for (int sl = 0; sl < kS; ++sl)
+      *reinterpret_cast<uint32_t*>(dst + sl * G::SLICE_STRIDE) = digits_to_half2(d0[sl], d1[sl]);
   }
 }
 
-// One warp's unit of an emulated product: rows of m-tile mt, columns of
-// n-tiles 2 p and 2 p + 1.  Writes C (FP64) into out[row * NC + col].
+// One warp's unit of an emulated product: m-tiles 2 mb, 2 mb + 1 and n-tiles
+// 2 nb, 2 nb + 1 (where they exist).  Writes C (FP64) into out[row * NC + col].
 template <class G>
-__device__ __forceinline__ void gemm_unit(int unit, const unsigned char* ops,
+__device__ __forceinline__ void gemm_unit(int unit, uint32_t ops_s, const int* row_exp,
                                           uint32_t slices_s, const int* col_emax,
                                           double* out) {
   const int lane = threadIdx.x & 31;
-  const int mt = unit / G::NT2;
-  const int nt0 = 2 * (unit - mt * G::NT2);
-  const bool two = nt0 + 1 < G::NT;
-  const int* row_exp = reinterpret_cast<const int*>(ops + G::DIGITS);
-  long long ghi[2][4], glo[2][4];
+  const int mb = unit / G::NB;
+  const int mt0 = G::UM * mb, nt0 = 2 * (unit - mb * G::NB);
+  const bool m2 = G::UM == 2 && mt0 + 1 < G::MT, n2 = nt0 + 1 < G::NT;
+  long long ghi[2][2][4], glo[2][2][4];
 #pragma unroll
-  for (int q = 0; q < 2; ++q)
+  for (int a = 0; a < 2; ++a)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) ghi[q][c] = glo[q][c] = 0;
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ghi[a][b][c] = glo[a][b][c] = 0;
 
 #pragma unroll 1
   for (int l = 2; l <= kLevels; ++l) {
-    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    float acc[2][2][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
     const int ilo = l - kS > 1 ? l - kS : 1;
     const int ihi = l - 1 < kS ? l - 1 : kS;
-#pragma unroll 1
+#pragma unroll 2
     for (int i = ilo; i <= ihi; ++i) {
       const int j = l - i;
-      const unsigned char* ablk = ops + ((i - 1) * G::MT + mt) * G::KT * 256 + lane * 8;
-      const uint32_t bblk = slices_s + (((j - 1) * G::NT + nt0) * G::KT) * 256 +
-                            (lane & 15) * 16;
+      const uint32_t ablk = ops_s + ((i - 1) * G::MT + mt0) * G::KT * 512 + lane * 16;
+      const uint32_t bblk =
+          slices_s + (j - 1) * G::SLICE_STRIDE + nt0 * G::KT * 256 + (lane & 15) * 16;
 #pragma unroll
       for (int kt = 0; kt < G::KT; ++kt) {
-        uint32_t afr[4];
-        expand_a(*reinterpret_cast<const uint2*>(ablk + kt * 256), afr);
-        uint32_t b0, b1;
-        ldsm_x2(b0, b1, bblk + kt * 256);
-        mma16816(acc[0], afr, b0, b1);
-        if (two) {
-          ldsm_x2(b0, b1, bblk + (G::KT + kt) * 256);
-          mma16816(acc[1], afr, b0, b1);
+        uint32_t a0[4], a1[4], b0[2], b1[2];
+        ldsm_x4(a0, ablk + kt * 512);
+        ldsm_x2(b0[0], b0[1], bblk + kt * 256);
+        mma16816(acc[0][0], a0, b0[0], b0[1]);
+        if (n2) {
+          ldsm_x2(b1[0], b1[1], bblk + (G::KT + kt) * 256);
+          mma16816(acc[0][1], a0, b1[0], b1[1]);
+        }
+        if (m2) {
+          ldsm_x4(a1, ablk + (G::KT + kt) * 512);
+          mma16816(acc[1][0], a1, b0[0], b0[1]);
+          if (n2) mma16816(acc[1][1], a1, b1[0], b1[1]);
         }
       }
     }
     const int sh = l <= 5 ? 7 * (5 - l) : 7 * (9 - l);
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
+    for (int a = 0; a < 2; ++a)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const long long v =
-            (long long)((unsigned long long)(long long)f32_exact_int(acc[q][c]) << sh);
-        if (l <= 5) ghi[q][c] += v;
-        else glo[q][c] += v;
-      }
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const long long v = (long long)((unsigned long long)(long long)
+                                              f32_exact_int(acc[a][b][c]) << sh);
+          if (l <= 5) ghi[a][b][c] += v;
+          else glo[a][b][c] += v;
+        }
   }
   const int g = lane >> 2, tq = lane & 3;
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    if (q == 1 && !two) break;
+  for (int a = 0; a < 2; ++a) {
+    if (a == 1 && !m2) break;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const int row = mt * 16 + g + (c >= 2 ? 8 : 0);
-      const int col = (nt0 + q) * 8 + 2 * tq + (c & 1);
-      if (row < G::M && col < G::NC) {
-        const double r = fma(i64_exact_double(glo[q][c]), 0x1p-28,
-                             i64_exact_double(ghi[q][c]));
-        out[row * G::NC + col] = r * pow2(row_exp[row] + col_emax[col] - 1022 - 31);
+    for (int b = 0; b < 2; ++b) {
+      if (b == 1 && !n2) break;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int row = (mt0 + a) * 16 + g + (c >= 2 ? 8 : 0);
+        const int col = (nt0 + b) * 8 + 2 * tq + (c & 1);
+        if (row < G::M && col < G::NC) {
+          const double r = fma(i64_exact_double(glo[a][b][c]), 0x1p-28,
+                               i64_exact_double(ghi[a][b][c]));
+          out[row * G::NC + col] = r * pow2(row_exp[row] + col_emax[col] - 1022 - 31);
+        }
       }
     }
   }
+}
+
+// All units of one product, spread over the CTA's warps.
+template <class G>
+__device__ __forceinline__ void gemm_all(uint32_t ops_s, const int* row_exp,
+                                         uint32_t slices_s, const int* col_emax,
+                                         double* out) {
+  for (int u = threadIdx.x >> 5; u < G::UNITS; u += kBlock / 32)
+    gemm_unit<G>(u, ops_s, row_exp, slices_s, col_emax, out);
 }
 
 }  // namespace tc
@@ -314,6 +371,8 @@ __device__ __forceinline__ void gemm_unit(int unit, const unsigned char* ops,
 template <int N, int EQ, int MODE>
 __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   using P = tc::Plan<N, EQ>;
+  using GV = typename P::GV;
+  using GL = typename P::GL;
   constexpr int NP = P::NP, NFPT = P::NFPT, NF = P::NF, E = P::E;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -321,7 +380,6 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   __shared__ int ops_ok;
 
   const int t = threadIdx.x;
-  const int warp = t >> 5;
   if (t == 0) {
     mbar_init(&bar, 1);
     mbar_arrive_expect_tx(&bar, a.ops_bytes);
@@ -336,7 +394,9 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   __syncthreads();
   if (!ops_ok) return;
 
-  const unsigned char* ops = smem + P::SM_OPS;
+  const uint32_t ops_s = smem_u32(smem + P::SM_OPS);
+  const int* rexp_v = reinterpret_cast<const int*>(smem + P::SM_OPS + P::OPS_GV + GV::DIGITS);
+  const int* rexp_l = reinterpret_cast<const int*>(smem + P::SM_OPS + P::OPS_GL + GL::DIGITS);
   double* sQ = reinterpret_cast<double*>(smem + P::SM_Q);
   unsigned char* sR1 = smem + P::SM_R1;
   const uint32_t sR1_s = smem_u32(sR1);
@@ -412,51 +472,23 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
     if constexpr (P::NAUX > 0) __syncthreads();
     // }}}
 
-    // {{{ 3. volume data -> digit slices
-    using G1 = typename P::G1;
-    using G2 = typename P::G2;
-    using GL = typename P::GL;
-    constexpr int SL2 = P::HAS_G1 ? G1::SLICE_BYTES : 0;  // G2 slices after G1's
+    // {{{ 3. volume data -> digit slices, 4. volume product -> R2 (FP64)
     if constexpr (EQ == DG_WAVE) {
-      tc::split_columns<G1>(sR1, sExp, [&](int n, int k) {  // u of element n
-        return sQ[(0 * E + n) * NP + k];
-      });
-      tc::split_columns<G2>(sR1 + SL2, sExp + P::NCOLS, [&](int n, int k) {
-        const int r = k / NP, j = k - r * NP;  // (G v)_r of element n
-        return sR2[(r * E + n) * NP + j];
+      tc::split_columns<GV>(sR1, sExp, [&](int n, int k) {
+        const int f = n / E, e = n - f * E;  // f = 0: u; f = 1..3: (G v)_{f-1}
+        return f == 0 ? sQ[e * NP + k] : sR2[((f - 1) * E + e) * NP + k];
       });
     } else if constexpr (EQ == DG_EULER) {
-      tc::split_columns<G2>(sR1 + SL2, sExp + P::NCOLS, [&](int n, int k) {
+      tc::split_columns<GV>(sR1, sExp, [&](int n, int k) {
         const int f = n / E, e = n - f * E;  // column (field, element)
         const int r = k / NP, j = k - r * NP;
         return sR2[((f * 3 + r) * E + e) * NP + j];
       });
     } else {
-      tc::split_columns<G1>(sR1, sExp, [&](int n, int k) {  // q_f of element e
-        return sQ[n * NP + k];
-      });
+      tc::split_columns<GV>(sR1, sExp, [&](int n, int k) { return sQ[n * NP + k]; });
     }
     __syncthreads();
-    // }}}
-
-    // {{{ 4. volume products (tensor cores) -> R2 (FP64)
-    {
-      constexpr int U1 = P::HAS_G1 ? G1::UNITS : 0;
-      constexpr int U2 = P::HAS_G2 ? G2::UNITS : 0;
-      double* out1 = sR2;
-      double* out2 = sR2 + P::OUT_G1;
-      // One call site per loop: G1 units from warp 0 up, G2 units from the
-      // last warp down, so the two products run side by side.  (With both
-      // inlined calls in one loop body, selected per unit, the G1 outputs of
-      // the order-3 wave kernel were lost in code generation.)
-      constexpr int NW = kBlock / 32;
-      if constexpr (P::HAS_G1)
-        for (int u = warp; u < U1; u += NW)
-          tc::gemm_unit<G1>(u, ops + P::OPS_G1, sR1_s, sExp, out1);
-      if constexpr (P::HAS_G2)
-        for (int u = NW - 1 - warp; u < U2; u += NW)
-          tc::gemm_unit<G2>(u, ops + P::OPS_G2, sR1_s + SL2, sExp + P::NCOLS, out2);
-    }
+    tc::gemm_all<GV>(ops_s + P::OPS_GV, rexp_v, sR1_s, sExp, sR2);
     __syncthreads();
     // }}}
 
@@ -466,26 +498,28 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
     for (int k = 0; k < NF; ++k) vol[k] = 0.0;
     if (active) {
       const double* G = sG + el * 9;
+      const double* o = sR2;  // GV::M x GV::NC
+      constexpr int NC = GV::NC;
       if constexpr (EQ == DG_WAVE) {
+        // ur_r = W_r u (column 0 block); div = sum_r W_r (G v)_r (diagonal blocks)
         const double c = a.p0;
-        const double* ur = sR2;                  // (3 Np) x E: row r Np + i
-        const double* dv = sR2 + P::OUT_G1;      // Np x E
-        const double u0 = ur[(0 * NP + i) * E + el], u1 = ur[(1 * NP + i) * E + el],
-                     u2 = ur[(2 * NP + i) * E + el];
-        vol[0] = -c * dv[i * E + el];
+        const double u0 = o[(0 * NP + i) * NC + el], u1 = o[(1 * NP + i) * NC + el],
+                     u2 = o[(2 * NP + i) * NC + el];
+        const double dv = o[(0 * NP + i) * NC + 1 * E + el] +
+                          o[(1 * NP + i) * NC + 2 * E + el] +
+                          o[(2 * NP + i) * NC + 3 * E + el];
+        vol[0] = -c * dv;
 #pragma unroll
         for (int x = 0; x < 3; ++x)
           vol[1 + x] = -c * fma(G[0 * 3 + x], u0, fma(G[1 * 3 + x], u1, G[2 * 3 + x] * u2));
       } else if constexpr (EQ == DG_EULER) {
-        const double* o = sR2 + P::OUT_G1;       // Np x (5 E)
 #pragma unroll
-        for (int k = 0; k < 5; ++k) vol[k] = o[i * (5 * E) + k * E + el];
+        for (int k = 0; k < 5; ++k) vol[k] = o[i * NC + k * E + el];
       } else {
-        const double* o = sR2;                   // (3 Np) x (6 E)
         auto dx = [&](int k, int x) {
-          const double d0 = o[(0 * NP + i) * (6 * E) + k * E + el];
-          const double d1 = o[(1 * NP + i) * (6 * E) + k * E + el];
-          const double d2 = o[(2 * NP + i) * (6 * E) + k * E + el];
+          const double d0 = o[(0 * NP + i) * NC + k * E + el];
+          const double d1 = o[(1 * NP + i) * NC + k * E + el];
+          const double d2 = o[(2 * NP + i) * NC + k * E + el];
           return fma(G[0 * 3 + x], d0, fma(G[1 * 3 + x], d1, G[2 * 3 + x] * d2));
         };
         vol[0] = dx(5, 1) - dx(4, 2);
@@ -499,7 +533,7 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
     __syncthreads();
     // }}}
 
-    // {{{ 6. face values of the tile -> R2, then digit slices
+    // {{{ 6. face values of the tile -> R2, digit slices, 7. LIFT product
     double* sF = sR2;                            // (NF, E, 4 Nfp)
     {
       const int64_t nfpt_all = nel * NFPT;
@@ -512,12 +546,8 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
     __syncthreads();
     tc::split_columns<GL>(sR1, sExp, [&](int n, int k) { return sF[n * NFPT + k]; });
     __syncthreads();
-    // }}}
-
-    // {{{ 7. LIFT product -> R2 after the face values
     double* sL = sR2 + NF * E * NFPT;            // Np x (NF E)
-    for (int u = warp; u < GL::UNITS; u += kBlock / 32)
-      tc::gemm_unit<GL>(u, ops + P::OPS_GL, sR1_s, sExp, sL);
+    tc::gemm_all<GL>(ops_s + P::OPS_GL, rexp_l, sR1_s, sExp, sL);
     __syncthreads();
     // }}}
 
