@@ -106,8 +106,10 @@ __global__ void fp64_fma_probe_kernel(double* out, int iters) {
   double v[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = 1.0 + 1e-9 * (double)(tid + k);
-  const double b = 0.9999999, c = 1e-7;
-  // 32-bit trip count, unrolled: the loop overhead stays off the timed pipe
+  // operands in registers (FP64 FMAs with constant-bank operands issue
+  // measurably slower on GB300); 32-bit trip count, unrolled loop
+  const double b = 1.0 - 1e-7 * (1.0 + 1e-12 * (double)threadIdx.x);
+  const double c = 1e-7 * (1.0 + 1e-12 * (double)threadIdx.x);
 #pragma unroll 4
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
