@@ -15,10 +15,17 @@ initial state and to ``c_e`` is the discrete adjoint of those steps:
   (r^s - a_s r^{s-1}) / (dt c_e)``), so the reverse sweep recomputes them
   segment by segment from checkpoints.
 
-Checkpointing: states are stored every ``k`` steps in the forward sweep; the
-reverse sweep replays one segment at a time, keeping its 5 k residuals.
-Memory is ``N/k + 5k`` states, minimal at ``k = sqrt(N / 5)`` (square-root
-scaling); each forward step is recomputed exactly once.
+Checkpointing (``checkpointing=``):
+
+* ``"binomial"`` (default): Revolve-type binomial checkpointing with
+  ``ceil(sqrt(N))`` state slots (:mod:`actx_dgfem_suite_gb300.checkpointing`);
+  the forward sweep keeps the states the schedule stores first, the reverse
+  sweep recomputes the rest, and each reversed step records its 5 stage
+  residuals only while it is being reversed.  Memory: sqrt(N) + 5 states;
+  about three forward steps per reversed step at N = 300.
+* ``"segments"``: states every ``k`` steps, segments replayed once with all
+  their 5 k residuals kept; memory ``N/k + 5k`` states, minimal at
+  ``k = sqrt(N / 5)``; each forward step recomputed exactly once.
 
 :class:`WaveMisfitFunction` wraps this as a ``torch.autograd.Function``.
 """
@@ -30,6 +37,7 @@ import math
 import numpy as np
 import torch
 
+from actx_dgfem_suite_gb300.checkpointing import BinomialSchedule, default_slots
 from actx_dgfem_suite_gb300.discretization import DGDiscretization
 from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
 from actx_dgfem_suite_gb300.refelem import BIUNIT_TET_VERTICES, pkdo_tet
@@ -103,7 +111,11 @@ class WaveAdjointSolver:
     """Forward traces and their adjoint for one mesh, time step and step count."""
 
     def __init__(self, disc: DGDiscretization, dt: float, nsteps: int,
-                 receivers: Receivers, device=None, segment: int | None = None):
+                 receivers: Receivers, device=None, segment: int | None = None,
+                 checkpointing: str = "binomial", slots: int | None = None):
+        if checkpointing not in ("binomial", "segments"):
+            raise ValueError(f"unknown checkpointing {checkpointing!r}")
+        self.checkpointing = checkpointing
         self.mesh = DeviceMesh(disc, device, with_partner=True)
         self.device = self.mesh.device
         self.plan = DevicePlan(self.mesh, "wave", (1.0,), "fp64")
@@ -111,6 +123,9 @@ class WaveAdjointSolver:
         self.nsteps = int(nsteps)
         self.rec = receivers
         self.segment = segment or max(1, int(round(math.sqrt(self.nsteps / 5.0))))
+        self.slots = default_slots(self.nsteps) if slots is None else int(slots)
+        self.schedule = (BinomialSchedule(self.nsteps, self.slots)
+                         if checkpointing == "binomial" else None)
         shape = self.plan.shape
         self._buf = torch.empty(shape, dtype=torch.float64, device=self.device)
         self._res = torch.zeros(shape, dtype=torch.float64, device=self.device)
@@ -132,12 +147,14 @@ class WaveAdjointSolver:
         self.plan.set_element_scale(c)
         q = q0.clone()
         ckpts = {0: q0.clone()}
+        keep = (set(self.schedule.first_descent()) if self.schedule is not None
+                else {n for n in range(self.segment, self.nsteps, self.segment)})
         traces = torch.empty((self.nsteps, self.rec.npoints), dtype=torch.float64,
                              device=self.device)
         for n in range(self.nsteps):
             self._step(q)
             traces[n] = self.rec.sample(q)
-            if (n + 1) % self.segment == 0 and n + 1 < self.nsteps:
+            if n + 1 in keep:
                 ckpts[n + 1] = q.clone()
         return traces, ckpts
 
@@ -170,6 +187,28 @@ class WaveAdjointSolver:
         self.plan.set_element_scale(c)
         lam = torch.zeros(self.plan.shape, dtype=torch.float64, device=self.device)
         cbar = torch.zeros_like(c)
+        if self.schedule is not None:
+            def advance(q, a, b):
+                q = q.clone()
+                for _ in range(a, b):
+                    self._step(q)
+                return q
+
+            def reverse_step(q_n, n):
+                q = q_n.clone()
+                rec: list = []
+                self._step(q, rec)
+                # trace n was sampled after step n, i.e. from q_{n+1}
+                self.rec.inject(lam, grad_traces[n])
+                self._adjoint_step(lam, rec, c, cbar)
+
+            stored = {k: v for k, v in ckpts.items() if k != 0}
+            st: dict = {}
+            self.schedule.reverse(ckpts[0], advance, reverse_step, stored, st)
+            self.stats = {"recomputed_steps": st["advanced"],
+                          "peak_stored_states": st["peak_slots"] + 1,
+                          "slots": self.slots}
+            return lam, cbar
         starts = sorted(ckpts)
         for seg_start in reversed(starts):
             seg_end = min(self.nsteps, seg_start + self.segment)

@@ -85,7 +85,15 @@ def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
 
     cost = RhsCost("wave", order, d.nelements)
     state_bytes = 4 * d.nelements * d.np_ * 8
-    nck = (nsteps - 1) // solver.segment + 1
+    if solver.schedule is not None:
+        ck = {"checkpointing": "binomial", "slots": solver.slots,
+              "recomputed_steps": solver.stats.get("recomputed_steps"),
+              "peak_stored_states": solver.stats.get("peak_stored_states"),
+              "peak_extra_states": solver.stats.get("peak_stored_states", 0) + 5}
+    else:
+        nck = (nsteps - 1) // solver.segment + 1
+        ck = {"checkpointing": "segments", "checkpoint_segment": solver.segment,
+              "checkpoint_states": nck, "peak_extra_states": nck + 5 * solver.segment}
     return {
         "workload": (f"wave P{order}, 6*{n}^3 tets, {nsteps} LSRK45 steps, "
                      f"{nrec} receivers, c_e ~ U[0.8,1.2]"),
@@ -96,9 +104,7 @@ def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
         "adjoint_ms_per_step": 1e3 * t_bwd / nsteps,
         "adjoint_over_forward": t_bwd / t_fwd,
         "forward_dof_updates_per_s": 5 * nsteps * cost.dofs / t_fwd,
-        "checkpoint_segment": solver.segment,
-        "checkpoint_states": nck,
-        "peak_extra_states": nck + 5 * solver.segment,
+        **ck,
         "state_mb": state_bytes / 1e6,
         "fd_checks": checks,
         "setup_s": setup_s,

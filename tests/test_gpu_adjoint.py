@@ -66,7 +66,7 @@ def test_adjoint_matches_oracle_matrix():
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= 1e-12
 
 
-def _small_solver(nsteps=12, order=2):
+def _small_solver(nsteps=12, order=2, checkpointing="binomial", slots=None):
     from actx_dgfem_suite_gb300.adjoint import (Receivers, WaveAdjointSolver,
                                                 random_interior_points)
     from actx_dgfem_suite_gb300.equations.wave import wave_problem
@@ -76,16 +76,18 @@ def _small_solver(nsteps=12, order=2):
     pts = random_interior_points(8, (-1, -1, -1), (1, 1, 1), 0.1, seed=4)
     rec = Receivers(d, pts, "cuda:0")
     dt = 0.5 * estimate_rk4_timestep(d, 1.2)
-    solver = WaveAdjointSolver(d, dt, nsteps, rec, "cuda:0", segment=5)
+    solver = WaveAdjointSolver(d, dt, nsteps, rec, "cuda:0", segment=5,
+                               checkpointing=checkpointing, slots=slots)
     q0 = torch.from_numpy(prob.fields).cuda()
     rng = np.random.default_rng(1)
     c = torch.from_numpy(rng.uniform(0.8, 1.2, d.nelements)).cuda()
     return solver, q0, c
 
 
-def test_gradient_matches_finite_differences():
+@pytest.mark.parametrize("checkpointing", ["binomial", "segments"])
+def test_gradient_matches_finite_differences(checkpointing):
     from actx_dgfem_suite_gb300.adjoint import WaveMisfitFunction
-    solver, q0, c = _small_solver()
+    solver, q0, c = _small_solver(checkpointing=checkpointing)
     obs = WaveMisfitFunction.apply(q0, c * 1.05, solver).detach()
 
     def loss(qq, cc):
@@ -125,3 +127,22 @@ def test_gradient_deterministic():
         grads.append((qv.grad.clone(), cv.grad.clone()))
     assert torch.equal(grads[0][0], grads[1][0])
     assert torch.equal(grads[0][1], grads[1][1])
+
+
+def test_checkpointing_schemes_agree():
+    """Binomial (few slots, many recomputations) and segment checkpointing
+    give the same gradient."""
+    from actx_dgfem_suite_gb300.adjoint import WaveMisfitFunction
+    grads = []
+    for scheme, slots in (("segments", None), ("binomial", 2), ("binomial", 5)):
+        solver, q0, c = _small_solver(nsteps=17, checkpointing=scheme, slots=slots)
+        qv = q0.clone().requires_grad_(True)
+        cv = c.clone().requires_grad_(True)
+        t = WaveMisfitFunction.apply(qv, cv, solver)
+        (0.5 * (t ** 2).sum()).backward()
+        grads.append((qv.grad.clone(), cv.grad.clone()))
+        if scheme == "binomial":
+            assert solver.stats["peak_stored_states"] <= slots + 1
+    for gq, gc in grads[1:]:
+        assert float(torch.linalg.norm(gq - grads[0][0])) <= 1e-12 * float(torch.linalg.norm(grads[0][0]))
+        assert float(torch.linalg.norm(gc - grads[0][1])) <= 1e-12 * float(torch.linalg.norm(grads[0][1]))
