@@ -17,15 +17,18 @@ initial state and to ``c_e`` is the discrete adjoint of those steps:
 
 Checkpointing (``checkpointing=``):
 
-* ``"binomial"`` (default): Revolve-type binomial checkpointing with
+* ``"binomial"``: Revolve-type binomial checkpointing with
   ``ceil(sqrt(N))`` state slots (:mod:`actx_dgfem_suite_gb300.checkpointing`);
   the forward sweep keeps the states the schedule stores first, the reverse
   sweep recomputes the rest, and each reversed step records its 5 stage
   residuals only while it is being reversed.  Memory: sqrt(N) + 5 states;
   about three forward steps per reversed step at N = 300.
-* ``"segments"``: states every ``k`` steps, segments replayed once with all
-  their 5 k residuals kept; memory ``N/k + 5k`` states, minimal at
-  ``k = sqrt(N / 5)``; each forward step recomputed exactly once.
+* ``"segments"`` (default): states every ``k`` steps, segments replayed once
+  with all their 5 k residuals kept; memory ``N/k + 5k`` states, minimal at
+  ``k = sqrt(N / 5)``; each forward step recomputed exactly once, so the
+  reverse sweep costs one forward sweep plus the adjoint operators.  The
+  binomial schedule trades about two more forward steps per step for a
+  third of the memory (measured by ``tools/bench_adjoint.py``).
 
 :class:`WaveMisfitFunction` wraps this as a ``torch.autograd.Function``.
 """
@@ -112,7 +115,7 @@ class WaveAdjointSolver:
 
     def __init__(self, disc: DGDiscretization, dt: float, nsteps: int,
                  receivers: Receivers, device=None, segment: int | None = None,
-                 checkpointing: str = "binomial", slots: int | None = None):
+                 checkpointing: str = "segments", slots: int | None = None):
         if checkpointing not in ("binomial", "segments"):
             raise ValueError(f"unknown checkpointing {checkpointing!r}")
         self.checkpointing = checkpointing

@@ -21,7 +21,7 @@ import json
 
 
 def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
-        cfl: float = 0.5, fd_eps: float = 1e-5) -> dict:
+        cfl: float = 0.5, fd_eps: float = 1e-5, compare_binomial: bool = True) -> dict:
     import time
 
     import numpy as np
@@ -85,6 +85,31 @@ def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
 
     cost = RhsCost("wave", order, d.nelements)
     state_bytes = 4 * d.nelements * d.np_ * 8
+    # the same gradient with binomial checkpointing (sqrt(N) state slots)
+    binom = None
+    if compare_binomial:
+        bsolver = WaveAdjointSolver(d, dt, nsteps, rec, checkpointing="binomial")
+        qb = q0.clone().requires_grad_(True)
+        cb = c.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        s = time.perf_counter()
+        tb = WaveMisfitFunction.apply(qb, cb, bsolver)
+        Jb = 0.5 * torch.sum((tb - obs) ** 2)
+        torch.cuda.synchronize()
+        tb_fwd = time.perf_counter() - s
+        s = time.perf_counter()
+        Jb.backward()
+        torch.cuda.synchronize()
+        tb_bwd = time.perf_counter() - s
+        binom = {"slots": bsolver.slots,
+                 "peak_stored_states": bsolver.stats["peak_stored_states"],
+                 "peak_extra_states": bsolver.stats["peak_stored_states"] + 5,
+                 "recomputed_steps": bsolver.stats["recomputed_steps"],
+                 "adjoint_over_forward": tb_bwd / tb_fwd,
+                 "grad_rel_diff_vs_segments": {
+                     "q0": float(torch.linalg.norm(qb.grad - gq) / torch.linalg.norm(gq)),
+                     "c": float(torch.linalg.norm(cb.grad - gc) / torch.linalg.norm(gc))}}
+
     if solver.schedule is not None:
         ck = {"checkpointing": "binomial", "slots": solver.slots,
               "recomputed_steps": solver.stats.get("recomputed_steps"),
@@ -105,6 +130,7 @@ def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
         "adjoint_over_forward": t_bwd / t_fwd,
         "forward_dof_updates_per_s": 5 * nsteps * cost.dofs / t_fwd,
         **ck,
+        "binomial_checkpointing": binom,
         "state_mb": state_bytes / 1e6,
         "fd_checks": checks,
         "setup_s": setup_s,
