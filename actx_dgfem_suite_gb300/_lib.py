@@ -30,7 +30,7 @@ DG_FP64_TC = 2
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
-                    "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
+                    "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc", "dg_rhs_vjp",
                     "dg_box_mesh_build",
                     "dg_plan_path", "dg_plan_info", "dg_fp64_fma_probe",
                     "dg_last_error",
@@ -114,6 +114,8 @@ def lib() -> ctypes.CDLL:
     L.dg_plan_set_element_scale.restype = ctypes.c_int
     L.dg_rhs_adjoint.argtypes = [vp, vp, vp, vp, vp]
     L.dg_rhs_adjoint.restype = ctypes.c_int
+    L.dg_rhs_vjp.argtypes = [vp, vp, vp, vp, vp]
+    L.dg_rhs_vjp.restype = ctypes.c_int
     L.dg_rhs_adjoint_noalloc.argtypes = [vp, vp, vp, vp]
     L.dg_rhs_adjoint_noalloc.restype = ctypes.c_int
     L.dg_box_mesh_build.argtypes = [ctypes.POINTER(BoxDesc), vp]

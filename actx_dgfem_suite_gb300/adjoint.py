@@ -252,3 +252,21 @@ class WaveMisfitFunction(torch.autograd.Function):
                                       c.contiguous())
         ctx.ckpts = None
         return dq0, dc, None
+
+
+class RHSFunction(torch.autograd.Function):
+    """``L(q)`` of a plan with the hand-written transposed Jacobian as its
+    backward (``dg_rhs_vjp``): wave and Euler FP64 plans on meshes with face
+    partners.  ``RHSFunction.apply(q, plan)``."""
+
+    @staticmethod
+    def forward(ctx, q, plan: DevicePlan):
+        q = q.detach().contiguous()
+        ctx.plan = plan
+        ctx.save_for_backward(q)
+        return plan.rhs(q)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (q,) = ctx.saved_tensors
+        return ctx.plan.vjp(q, grad_out.contiguous()), None

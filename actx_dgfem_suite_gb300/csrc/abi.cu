@@ -10,6 +10,7 @@
 
 #include "../../include/dgfem_gb300.h"
 #include "dg_adjoint.cuh"  // AdjArgs, AdjOpsLayout
+#include "dg_adjoint_euler.cuh"  // VjpArgs
 #include "dg_face.cuh"     // FaceArgs
 #include "dg_launch.h"
 #include "dg_rhs.cuh"  // RhsArgs, kBlock
@@ -627,13 +628,17 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     p->tc_grid = (int)(tiles < tfull ? tiles : tfull);
   }
 
-  if (mesh->face_partner && equation == DG_WAVE && kprec == 0) {
+  // adjoint operators: wave (transpose) and, on the face-shared path, Euler
+  // (transposed Jacobian)
+  if (mesh->face_partner && kprec == 0 &&
+      (equation == DG_WAVE || (equation == DG_EULER && split))) {
     if (p->nel * 8 * (int64_t)nfp >= (int64_t(1) << 32)) {
       dg_plan_destroy(p);
       return fail(DG_ERR_ARGUMENT, "mesh too large for the adjoint's 32-bit face indices");
     }
     dg::LaunchShape ashape;
-    err = dg::adjoint_shape_wave(N, &ashape);
+    err = equation == DG_WAVE ? dg::adjoint_shape_wave(N, &ashape)
+                              : dg::vjp_shape_euler(N, &ashape);
     if (err != cudaSuccess || ashape.blocks_per_sm < 1) {
       dg_plan_destroy(p);
       return err != cudaSuccess ? cuda_fail(err, "adjoint configuration")
@@ -683,7 +688,7 @@ int dg_plan_set_element_scale(dg_plan* p, const double* scale) {
 int dg_rhs_adjoint(dg_plan* p, const double* x, double* y, double* face_scratch,
                    void* stream) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
-  if (!p->d_adj_ops)
+  if (!p->d_adj_ops || p->equation != DG_WAVE)
     return fail(DG_ERR_UNSUPPORTED,
                 "adjoint needs an FP64 wave plan built with face_partner");
   if (!x || !y || !face_scratch)
@@ -710,6 +715,44 @@ int dg_rhs_adjoint(dg_plan* p, const double* x, double* y, double* face_scratch,
   cudaError_t err = dg::adjoint_launch_wave(p->order, a, p->adj_grid, p->nsm,
                                             reinterpret_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(err, "adjoint launch");
+  return DG_OK;
+}
+
+int dg_rhs_vjp(dg_plan* p, const double* q, const double* x, double* y,
+               void* stream) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!q || !x || !y) return fail(DG_ERR_ARGUMENT, "q, x or y is NULL");
+  if (!p->d_adj_ops || !p->split)
+    return fail(DG_ERR_UNSUPPORTED,
+                "the transposed Jacobian needs an FP64 wave or Euler plan built "
+                "with face_partner");
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  if (overlap(y, q, bytes) || overlap(y, x, bytes))
+    return fail(DG_ERR_ARGUMENT, "y must not overlap q or x");
+  if (p->equation == DG_WAVE)  // linear: the transpose, scratch in the face buffer
+    return dg_rhs_adjoint(p, x, y, p->d_flux, stream);
+  dg::VjpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.q = q;
+  a.x = x;
+  a.y = y;
+  a.aux = p->d_aux;
+  a.scratch = p->d_flux;
+  a.elem_scale = p->elem_scale;
+  a.metric = p->metric;
+  a.face_geom = p->face_geom;
+  a.gather = p->gather;
+  a.partner = p->face_partner;
+  a.owned = p->d_owned;
+  a.nowned = p->nowned;
+  a.ops = p->d_adj_ops;
+  a.ops_bytes = p->adj_ops_bytes;
+  a.nel = p->nel;
+  a.status = p->d_status;
+  a.gamma = p->params[0];
+  cudaError_t err = dg::vjp_launch_euler(p->order, a, p->adj_grid, p->nsm,
+                                         reinterpret_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return cuda_fail(err, "vjp launch");
   return DG_OK;
 }
 
@@ -816,7 +859,7 @@ extern "C" {
 int dg_rhs_adjoint_noalloc(dg_plan* p, const double* x, double* y,
                            void* stream) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
-  if (!p->d_adj_ops)
+  if (!p->d_adj_ops || p->equation != DG_WAVE)
     return fail(DG_ERR_UNSUPPORTED,
                 "adjoint needs an FP64 wave plan built with face_partner");
   if (!x || !y) return fail(DG_ERR_ARGUMENT, "x or y is NULL");

@@ -11,6 +11,7 @@ namespace dg {
 struct RhsArgs;
 struct AdjArgs;
 struct FaceArgs;
+struct VjpArgs;
 
 struct LaunchShape {
   int smem_bytes = 0;      // dynamic shared memory per CTA
@@ -87,5 +88,11 @@ int set_error(int code, const char* msg);
 cudaError_t adjoint_shape_wave(int order, LaunchShape* out);
 cudaError_t adjoint_launch_wave(int order, const AdjArgs& a, int grid, int nsm,
                                 cudaStream_t s);
+
+// Transposed Jacobian of the FP64 Euler RHS (dg_adjoint_euler.cuh): shape of
+// the volume kernel, and the launches (node table, volume, face, node gather).
+cudaError_t vjp_shape_euler(int order, LaunchShape* out);
+cudaError_t vjp_launch_euler(int order, const VjpArgs& a, int grid, int nsm,
+                             cudaStream_t s);
 
 }  // namespace dg

@@ -226,6 +226,20 @@ class DevicePlan:
             ctypes.c_void_p(scratch.data_ptr()), _stream_handle(stream)))
         return out
 
+    def vjp(self, q: torch.Tensor, x: torch.Tensor, out: torch.Tensor | None = None,
+            stream=None) -> torch.Tensor:
+        """``(dL/dq (q))^T x`` (FP64 wave and Euler plans with face partners)."""
+        self._check_tensor(q, "q")
+        self._check_tensor(x, "x")
+        if out is None:
+            out = torch.empty_like(x)
+        else:
+            self._check_tensor(out, "out")
+        _lib.check(self._lib.dg_rhs_vjp(
+            self._handle, ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(x.data_ptr()),
+            ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
+        return out
+
     def finish(self, stream=None) -> None:
         _lib.check(self._lib.dg_finish(self._handle, _stream_handle(stream)))
 

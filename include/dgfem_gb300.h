@@ -133,6 +133,21 @@ int dg_plan_set_element_scale(dg_plan* plan, const double* scale);
 int dg_rhs_adjoint(dg_plan* plan, const double* x, double* y,
                    double* face_scratch, void* stream);
 
+/* Transposed Jacobian of the plan's operator at state q: y = (dL/dq (q))^T x
+ * (the vector-Jacobian product; for the linear wave operator, L^T x).
+ * FP64 wave and Euler plans on the face-shared path (mesh with
+ * face_partner).  Euler: transposed weak derivatives and LIFT, the flux
+ * Jacobians J_x(q)^T at every node, the Lax-Friedrichs flux's Jacobians
+ * (including the derivative of its wave-speed maximum, taken on the side
+ * the forward picks) and the wall mirror, all computed deterministically
+ * (gathers over glued face points, no atomics).  A per-element scale set
+ * with dg_plan_set_element_scale is honoured.  Works in the plan's own
+ * face buffers: do not run it concurrently with other calls on the plan.
+ * No counterpart in the reference (which has no adjoint); it is the Euler
+ * part of the adjoint RHS. */
+int dg_rhs_vjp(dg_plan* plan, const double* q, const double* x, double* y,
+               void* stream);
+
 /* Size of the device buffer that dg_rhs_adjoint_noalloc works in. */
 #define DG_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 

@@ -1,0 +1,98 @@
+"""Transposed Jacobian of the RHS (dg_rhs_vjp) against finite differences of
+the forward RHS: <x, (L(q + e v) - L(q - e v)) / 2e> = <L'(q)^T x, v>."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from tests._helpers import jittered_box_mesh, make_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(equation, order, seed=0):
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem(equation, jittered_box_mesh(3), order, seed=seed)
+    plan = DevicePlan(DeviceMesh(prob.disc, "cuda:0", with_partner=True), equation,
+                      prob.params)
+    return prob, plan
+
+
+def _euler_state(shape, rng):
+    q = np.empty(shape)
+    q[0] = 1.0 + 0.2 * rng.random(shape[1:])                 # rho
+    q[2:] = 0.3 * rng.standard_normal((3,) + shape[1:])      # momentum
+    ke = 0.5 * (q[2:] ** 2).sum(axis=0) / q[0]
+    q[1] = 2.5 + 0.3 * rng.random(shape[1:]) + ke            # energy, p ~ 1
+    return q
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_euler_vjp_matches_finite_differences(order):
+    prob, plan = _plan("euler", order, seed=order)
+    rng = np.random.default_rng(order)
+    q = torch.from_numpy(_euler_state(prob.fields.shape, rng)).cuda()
+    x = torch.from_numpy(rng.standard_normal(prob.fields.shape)).cuda()
+    v = torch.from_numpy(rng.standard_normal(prob.fields.shape)).cuda()
+    y = plan.vjp(q, x)
+    eps = 1e-6
+    dl = (plan.rhs(q + eps * v) - plan.rhs(q - eps * v)) / (2 * eps)
+    plan.finish()
+    lhs, rhs = float((x * dl).sum()), float((y * v).sum())
+    assert abs(lhs - rhs) <= 1e-6 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_euler_vjp_per_component_and_scale():
+    """Directional checks along single fields, and with a per-element scale."""
+    prob, plan = _plan("euler", 2, seed=9)
+    rng = np.random.default_rng(3)
+    q = torch.from_numpy(_euler_state(prob.fields.shape, rng)).cuda()
+    scale = torch.from_numpy(rng.uniform(0.5, 1.5, prob.disc.nelements)).cuda()
+    plan.set_element_scale(scale)
+    x = torch.from_numpy(rng.standard_normal(prob.fields.shape)).cuda()
+    y = plan.vjp(q, x)
+    eps = 1e-6
+    for k in range(5):
+        v = torch.zeros_like(q)
+        v[k] = torch.from_numpy(rng.standard_normal(prob.fields.shape[1:])).cuda()
+        dl = (plan.rhs(q + eps * v) - plan.rhs(q - eps * v)) / (2 * eps)
+        lhs, rhs = float((x * dl).sum()), float((y * v).sum())
+        assert abs(lhs - rhs) <= 1e-6 * max(abs(lhs), abs(rhs)), (k, lhs, rhs)
+    plan.finish()
+
+
+def test_wave_vjp_is_the_adjoint():
+    prob, plan = _plan("wave", 3)
+    rng = np.random.default_rng(0)
+    q = torch.from_numpy(rng.standard_normal(prob.fields.shape)).cuda()
+    x = torch.from_numpy(rng.standard_normal(prob.fields.shape)).cuda()
+    a = plan.vjp(q, x)
+    b = plan.adjoint(x)
+    plan.finish()
+    assert float(torch.linalg.norm(a - b)) <= 1e-14 * float(torch.linalg.norm(b))
+
+
+def test_rhs_function_autograd():
+    from actx_dgfem_suite_gb300.adjoint import RHSFunction
+    prob, plan = _plan("euler", 3, seed=2)
+    rng = np.random.default_rng(5)
+    q = torch.from_numpy(_euler_state(prob.fields.shape, rng)).cuda().requires_grad_(True)
+    w = torch.from_numpy(rng.standard_normal(prob.fields.shape)).cuda()
+    loss = (RHSFunction.apply(q, plan) * w).sum()
+    loss.backward()
+    ref = plan.vjp(q.detach(), w)
+    plan.finish()
+    assert torch.equal(q.grad, ref)
+
+
+def test_vjp_unsupported_without_partners():
+    from actx_dgfem_suite_gb300._lib import DGError
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem("euler", jittered_box_mesh(2), 2)
+    plan = DevicePlan(DeviceMesh(prob.disc, "cuda:0", with_partner=False), "euler",
+                      prob.params)
+    q = torch.from_numpy(prob.fields).cuda()
+    with pytest.raises(DGError):
+        plan.vjp(q, q.clone())
