@@ -270,3 +270,91 @@ class RHSFunction(torch.autograd.Function):
     def backward(ctx, grad_out):
         (q,) = ctx.saved_tensors
         return ctx.plan.vjp(q, grad_out.contiguous()), None
+
+
+class EulerAdjointSolver:
+    """Gradient of a receiver misfit with respect to the initial state through
+    LSRK(5,4) steps of the (nonlinear) Euler operator.
+
+    Receivers sample the density.  The reverse of one step needs the five
+    stage input states ``q^(s)``: stage ``s`` computes ``r^s = a_s r^{s-1} + dt
+    L(q^(s))`` and ``q^(s+1) = q^(s) + b_s r^s``, so its adjoint applies the
+    transposed Jacobian ``L'(q^(s))^T`` (``dg_rhs_vjp``) to the residual
+    adjoint.  Checkpoints every ``segment`` steps; a segment is replayed once
+    with its stage states kept (memory ``N/k + 5k`` states)."""
+
+    def __init__(self, disc: DGDiscretization, gamma: float, dt: float, nsteps: int,
+                 receivers: Receivers, device=None, segment: int | None = None):
+        self.mesh = DeviceMesh(disc, device, with_partner=True)
+        self.device = self.mesh.device
+        self.plan = DevicePlan(self.mesh, "euler", (float(gamma),), "fp64")
+        self.dt = float(dt)
+        self.nsteps = int(nsteps)
+        self.rec = receivers
+        self.segment = segment or max(1, int(round(math.sqrt(self.nsteps / 5.0))))
+        shape = self.plan.shape
+        self._buf = torch.empty(shape, dtype=torch.float64, device=self.device)
+        self._res = torch.zeros(shape, dtype=torch.float64, device=self.device)
+
+    def _step(self, q: torch.Tensor, record: list | None = None) -> None:
+        src, dst = q, self._buf
+        for s in range(5):
+            if record is not None:
+                record.append(src.clone())       # stage input state q^(s)
+            self.plan.rk_stage(src, dst, self._res, RK4A[s], RK4B[s], self.dt)
+            src, dst = dst, src
+        q.copy_(src)
+
+    def forward(self, q0: torch.Tensor):
+        q = q0.clone()
+        ckpts = {0: q0.clone()}
+        traces = torch.empty((self.nsteps, self.rec.npoints), dtype=torch.float64,
+                             device=self.device)
+        for n in range(self.nsteps):
+            self._step(q)
+            traces[n] = self.rec.sample(q)
+            if (n + 1) % self.segment == 0 and n + 1 < self.nsteps:
+                ckpts[n + 1] = q.clone()
+        return traces, ckpts
+
+    def _adjoint_step(self, lam: torch.Tensor, stages: list) -> None:
+        rbar = torch.zeros_like(lam)
+        y = torch.empty_like(lam)
+        for s in range(4, -1, -1):
+            rbar.add_(lam, alpha=RK4B[s])
+            self.plan.vjp(stages[s], rbar, y)
+            lam.add_(y, alpha=self.dt)
+            rbar.mul_(RK4A[s])
+
+    def backward(self, grad_traces: torch.Tensor, ckpts: dict) -> torch.Tensor:
+        lam = torch.zeros(self.plan.shape, dtype=torch.float64, device=self.device)
+        for seg_start in reversed(sorted(ckpts)):
+            seg_end = min(self.nsteps, seg_start + self.segment)
+            q = ckpts[seg_start].clone()
+            records = []
+            for _ in range(seg_start, seg_end):
+                rec: list = []
+                self._step(q, rec)
+                records.append(rec)
+            for n in range(seg_end - 1, seg_start - 1, -1):
+                self.rec.inject(lam, grad_traces[n])
+                self._adjoint_step(lam, records[n - seg_start])
+        return lam
+
+
+class EulerMisfitFunction(torch.autograd.Function):
+    """``traces = F(q0)`` for an :class:`EulerAdjointSolver`, with the
+    hand-written adjoint as its backward."""
+
+    @staticmethod
+    def forward(ctx, q0, solver: EulerAdjointSolver):
+        traces, ckpts = solver.forward(q0.detach().contiguous())
+        ctx.solver = solver
+        ctx.ckpts = ckpts
+        return traces
+
+    @staticmethod
+    def backward(ctx, grad_traces):
+        lam = ctx.solver.backward(grad_traces.contiguous(), ctx.ckpts)
+        ctx.ckpts = None
+        return lam, None

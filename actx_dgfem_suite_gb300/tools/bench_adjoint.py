@@ -137,6 +137,64 @@ def run(n: int = 40, order: int = 3, nsteps: int = 300, nrec: int = 256,
     }
 
 
+def run_euler(n: int = 24, order: int = 3, nsteps: int = 100, nrec: int = 64,
+              cfl: float = 0.5, fd_eps: float = 1e-6) -> dict:
+    """Euler P3 adjoint: gradient of a density-receiver misfit with respect to
+    the initial state through ``nsteps`` LSRK45 steps (transposed Jacobian
+    ``dg_rhs_vjp`` per stage), with its cost against the forward sweep and a
+    central finite-difference check along a random direction."""
+    import time
+
+    import numpy as np
+    import torch
+
+    from actx_dgfem_suite_gb300.adjoint import (EulerAdjointSolver, EulerMisfitFunction,
+                                                Receivers, random_interior_points)
+    from actx_dgfem_suite_gb300.equations.euler import euler_problem
+    from actx_dgfem_suite_gb300.timestepping import estimate_rk4_timestep
+
+    prob = euler_problem(order, n, "baseline")
+    d = prob.disc
+    pts = random_interior_points(nrec, (-0.5,) * 3, (0.5,) * 3, 0.05, seed=1)
+    rec = Receivers(d, pts, "cuda")
+    dt = estimate_rk4_timestep(d, 1.3, cfl)
+    solver = EulerAdjointSolver(d, prob.params[0], dt, nsteps, rec)
+    q0 = torch.from_numpy(prob.fields).to(solver.device)
+    rng = np.random.default_rng(3)
+    pert = torch.from_numpy(1 + 0.01 * rng.standard_normal(tuple(q0.shape))).to(solver.device)
+    with torch.no_grad():
+        obs = EulerMisfitFunction.apply(q0 * pert, solver)
+
+    def loss(qq):
+        return 0.5 * torch.sum((EulerMisfitFunction.apply(qq, solver) - obs) ** 2)
+
+    qv = q0.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    s = time.perf_counter()
+    J = loss(qv)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - s
+    s = time.perf_counter()
+    J.backward()
+    torch.cuda.synchronize()
+    t_bwd = time.perf_counter() - s
+    dq = torch.from_numpy(rng.standard_normal(tuple(q0.shape))).to(solver.device)
+    with torch.no_grad():
+        fd = (float(loss(q0 + fd_eps * dq)) - float(loss(q0 - fd_eps * dq))) / (2 * fd_eps)
+    an = float(torch.sum(qv.grad * dq))
+    return {
+        "workload": (f"Euler P{order}, 6*{n}^3 tets, {nsteps} LSRK45 steps, {nrec} "
+                     "density receivers, gradient wrt the initial state"),
+        "nelements": d.nelements,
+        "forward_ms_per_step": 1e3 * t_fwd / nsteps,
+        "adjoint_ms_per_step": 1e3 * t_bwd / nsteps,
+        "adjoint_over_forward": t_bwd / t_fwd,
+        "checkpoint_segment": solver.segment,
+        "fd_check_q0": {"adjoint": an, "finite_difference": fd,
+                        "rel_diff": abs(an - fd) / max(abs(fd), 1e-300)},
+    }
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m actx_dgfem_suite_gb300.tools.bench_adjoint")
     ap.add_argument("--n", type=int, default=40)

@@ -299,11 +299,14 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step) -> dict:
     for name, mod, kw in (
             ("mixed_precision_euler_p3_lsrk45", "bench_mixed", {}),
             ("ensemble_maxwell_p3_64", "bench_ensemble", {"reps": 5}),
-            ("adjoint_wave_p3", "bench_adjoint", {})):
+            ("adjoint_wave_p3", "bench_adjoint", {}),
+            ("adjoint_euler_p3", "bench_adjoint", {"_fn": "run_euler"})):
         try:
             import importlib
             m = importlib.import_module(f"actx_dgfem_suite_gb300.tools.{mod}")
-            res = m.run(**kw)
+            kw = dict(kw)
+            fn = getattr(m, kw.pop("_fn", "run"))
+            res = fn(**kw)
             res.pop("err_per_step", None)
             res.pop("member_sizes", None)
             out[name] = res

@@ -96,3 +96,34 @@ def test_vjp_unsupported_without_partners():
     q = torch.from_numpy(prob.fields).cuda()
     with pytest.raises(DGError):
         plan.vjp(q, q.clone())
+
+
+def test_euler_misfit_gradient_matches_finite_differences():
+    """Gradient of a density-receiver misfit through 8 LSRK45 steps of the
+    Euler operator with respect to the initial state."""
+    from actx_dgfem_suite_gb300.adjoint import (EulerAdjointSolver, EulerMisfitFunction,
+                                                Receivers, random_interior_points)
+    from actx_dgfem_suite_gb300.equations.euler import euler_problem
+    from actx_dgfem_suite_gb300.timestepping import estimate_rk4_timestep
+    prob = euler_problem(2, 3, "baseline")
+    d = prob.disc
+    pts = random_interior_points(10, (-0.5, -0.5, -0.5), (0.5, 0.5, 0.5), 0.05, seed=4)
+    rec = Receivers(d, pts, "cuda:0")
+    dt = 0.5 * estimate_rk4_timestep(d, 1.3)
+    solver = EulerAdjointSolver(d, prob.params[0], dt, 8, rec, "cuda:0", segment=3)
+    q0 = torch.from_numpy(prob.fields).cuda()
+    rng = np.random.default_rng(2)
+    obs = EulerMisfitFunction.apply(q0 * (1 + 0.01 * torch.from_numpy(
+        rng.standard_normal(q0.shape)).cuda()), solver).detach()
+
+    def loss(qq):
+        return 0.5 * torch.sum((EulerMisfitFunction.apply(qq, solver) - obs) ** 2)
+
+    qv = q0.clone().requires_grad_(True)
+    loss(qv).backward()
+    dq = torch.from_numpy(rng.standard_normal(tuple(q0.shape))).cuda()
+    eps = 1e-6
+    with torch.no_grad():
+        fd = (float(loss(q0 + eps * dq)) - float(loss(q0 - eps * dq))) / (2 * eps)
+    an = float(torch.sum(qv.grad * dq))
+    assert abs(an - fd) <= 1e-5 * abs(fd), (an, fd)
