@@ -32,7 +32,8 @@ EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc", "dg_rhs_vjp",
                     "dg_box_mesh_build",
-                    "dg_plan_path", "dg_plan_info", "dg_fp64_fma_probe",
+                    "dg_plan_path", "dg_plan_info", "dg_plan_set_variant",
+                    "dg_plan_autotune", "dg_fp64_fma_probe",
                     "dg_last_error",
                     "dg_abi_version")
 
@@ -129,6 +130,11 @@ def lib() -> ctypes.CDLL:
                                i32p, i32p, i32p]
     L.dg_plan_info.restype = ctypes.c_int
     L.dg_plan_path.argtypes = [vp, i32p, i32p, i32p, ctypes.POINTER(ctypes.c_int64)]
+    L.dg_plan_set_variant.argtypes = [vp, ctypes.c_int32]
+    L.dg_plan_set_variant.restype = ctypes.c_int
+    L.dg_plan_autotune.argtypes = [vp, vp, vp, ctypes.c_int32, vp, i32p,
+                                   ctypes.POINTER(ctypes.c_float)]
+    L.dg_plan_autotune.restype = ctypes.c_int
     L.dg_plan_path.restype = ctypes.c_int
     L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, vp]

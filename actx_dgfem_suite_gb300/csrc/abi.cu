@@ -138,6 +138,9 @@ struct dg_plan {
   int* d_status = nullptr;
   double params[3] = {0, 0, 0};
   int grid = 0;
+  int64_t ntiles = 0;      // tiles of the main kernel
+  int grid_mtc = 0;        // mixed precision with tensor-core products
+  int variant = 0;         // bit 0: tensor-core products (mixed); bit 1: one CTA per tile
   dg::LaunchShape shape;
   int device = 0;
   int nsm = 0;
@@ -281,6 +284,15 @@ int setup_split(dg_plan* p, const int32_t* partner, const int32_t* d_face_nodes)
   p->aux_grid = (int)(ablocks < afull ? ablocks : afull);
   p->split = true;
   return DG_OK;
+}
+
+// Mode bits and grid of the main kernel under the plan's variant.
+int main_mode(const dg_plan* p, int base) {
+  return base | ((p->variant & 1) && p->precision == DG_FP32_MIXED ? dg::MODE_TC : 0);
+}
+int main_grid(const dg_plan* p) {
+  if (p->variant & 2) return (int)(p->ntiles < 0x7fffffff ? p->ntiles : 0x7fffffff);
+  return (p->variant & 1) && p->precision == DG_FP32_MIXED ? p->grid_mtc : p->grid;
 }
 
 // The face-shared path's first launches (Euler table, face kernel) for state q.
@@ -583,6 +595,19 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
       (p->nel + shape.elems_per_tile - 1) / shape.elems_per_tile;
   const int64_t full = (int64_t)nsm * shape.blocks_per_sm;
   p->grid = (int)(ntiles < full ? ntiles : full);
+  p->ntiles = ntiles;
+  if (kprec == 1) {  // the tensor-core variant of the mixed kernel
+    dg::LaunchShape t0, t1;
+    err = shape_of(equation, N, 1, dg::MODE_TC, &t0);
+    if (err == cudaSuccess) err = shape_of(equation, N, 1, dg::MODE_TC | dg::MODE_STAGE, &t1);
+    if (err != cudaSuccess) {
+      dg_plan_destroy(p);
+      return cuda_fail(err, "tensor-core mixed kernel configuration");
+    }
+    const int bps = t1.blocks_per_sm < t0.blocks_per_sm ? t1.blocks_per_sm : t0.blocks_per_sm;
+    const int64_t tfull = (int64_t)nsm * (bps > 0 ? bps : 1);
+    p->grid_mtc = (int)(ntiles < tfull ? ntiles : tfull);
+  }
   p->face_partner = mesh->face_partner;
 
   if (split) {
@@ -669,6 +694,59 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   }
   *plan_out = p;
   return DG_OK;
+}
+
+int dg_plan_set_variant(dg_plan* p, int32_t variant) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (variant < 0 || variant > 3) return fail(DG_ERR_ARGUMENT, "variant must be 0..3");
+  if ((variant & 1) && p->precision != DG_FP32_MIXED)
+    return fail(DG_ERR_UNSUPPORTED, "tensor-core products are a mixed-precision variant");
+  if (p->tc) return fail(DG_ERR_UNSUPPORTED, "DG_FP64_TC plans have one variant");
+  p->variant = variant;
+  return DG_OK;
+}
+
+int dg_plan_autotune(dg_plan* p, const double* q, double* rhs, int32_t reps,
+                     void* stream, int32_t* chosen, float* ms_per_variant) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!q || !rhs || reps < 1) return fail(DG_ERR_ARGUMENT, "bad autotune arguments");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int nvar = p->tc ? 1 : 4;
+  cudaEvent_t e0, e1;
+  cudaError_t err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
+  if (err != cudaSuccess) return cuda_fail(err, "autotune events");
+  const int saved = p->variant;
+  int best = -1;
+  float best_ms = 0.f;
+  int code = DG_OK;
+  for (int v = 0; v < 4 && code == DG_OK; ++v) {
+    float ms = -1.f;
+    if (v < nvar && ((v & 1) == 0 || p->precision == DG_FP32_MIXED)) {
+      p->variant = v;
+      code = dg_rhs(p, q, rhs, stream);  // warm-up
+      if (code == DG_OK) err = cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && code == DG_OK && err == cudaSuccess; ++r)
+        code = dg_rhs(p, q, rhs, stream);
+      if (code == DG_OK && err == cudaSuccess) err = cudaEventRecord(e1, s);
+      if (code == DG_OK && err == cudaSuccess) err = cudaEventSynchronize(e1);
+      if (code == DG_OK && err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+      if (code == DG_OK && err != cudaSuccess) code = cuda_fail(err, "autotune timing");
+      if (code == DG_OK) {
+        ms /= (float)reps;
+        if (best < 0 || ms < best_ms) {
+          best = v;
+          best_ms = ms;
+        }
+      }
+    }
+    if (ms_per_variant) ms_per_variant[v] = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  p->variant = code == DG_OK && best >= 0 ? best : saved;
+  if (chosen) *chosen = p->variant;
+  return code;
 }
 
 int dg_plan_set_element_scale(dg_plan* p, const double* scale) {
@@ -776,7 +854,8 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     err = tc_launch_of(p->equation, p->order, 0, a, p->tc_grid, s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
-                    p->split ? dg::MODE_SPLIT : dg::MODE_RHS, a, p->grid, s);
+                    main_mode(p, p->split ? dg::MODE_SPLIT : dg::MODE_RHS), a,
+                    main_grid(p), s);
   }
   if (err != cudaSuccess) return cuda_fail(err, "rhs launch");
   return DG_OK;
@@ -817,7 +896,8 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     err = tc_launch_of(p->equation, p->order, 1, a, p->tc_grid, s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
-                    dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0), a, p->grid, s);
+                    main_mode(p, dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0)), a,
+                    main_grid(p), s);
   }
   if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
   return DG_OK;
@@ -927,7 +1007,8 @@ int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* tensor_cores,
                  int32_t* launches_per_rhs, int64_t* owned_faces) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (face_shared) *face_shared = p->split ? 1 : 0;
-  if (tensor_cores) *tensor_cores = p->tc ? 1 : 0;
+  if (tensor_cores)
+    *tensor_cores = (p->tc || ((p->variant & 1) && p->precision == DG_FP32_MIXED)) ? 1 : 0;
   if (launches_per_rhs)
     *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : 1;
   if (owned_faces) *owned_faces = p->split ? p->nowned : 0;
@@ -941,7 +1022,7 @@ int dg_plan_info(const dg_plan* p, int64_t* nelements, int32_t* order,
   if (nelements) *nelements = p->nel;
   if (order) *order = p->order;
   if (nfields) *nfields = p->nfields;
-  if (grid) *grid = p->tc ? p->tc_grid : p->grid;
+  if (grid) *grid = p->tc ? p->tc_grid : main_grid(p);
   if (block) *block = dg::kBlock;
   if (smem_bytes) *smem_bytes = p->tc ? p->tc_shape.smem_bytes : p->shape.smem_bytes;
   return DG_OK;

@@ -47,8 +47,10 @@
 
 namespace dg {
 
-// bit 0: RK stage epilogue; bit 1: face values from the face-shared kernels
-enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_SPLIT = 2 };
+// bit 0: RK stage epilogue; bit 1: face values from the face-shared kernels;
+// bit 2: mixed precision with the volume and LIFT contractions on the tensor
+// cores (3xTF32 split, FP32 accumulation)
+enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_SPLIT = 2, MODE_TC = 4 };
 
 struct RhsArgs {
   const double* q;
@@ -145,9 +147,88 @@ struct Tile {
   static constexpr int FGEO = GEO + pad16(9 * E * RS);
   // mixed-precision Euler: FP64 pressure of every node of the tile
   static constexpr int PRES = FGEO + pad16(16 * E * RS);
-  static constexpr int SMEM_BYTES =
+  static constexpr int SMEM_BASE =
       PRES + ((MIXED && EQ == DG_EULER) ? pad16(E * NP * 8) : 0);
+  // MODE_TC: FP32 outputs of the tensor-core products (volume, then LIFT)
+  static constexpr int VOL_M = EQ == DG_EULER ? NP : 3 * NP;
+  static constexpr int VOL_NC = EQ == DG_MAXWELL ? NF * E : (EQ == DG_WAVE ? E : NF * E);
+  static constexpr int TC_FLOATS_VOL = VOL_M * VOL_NC + (EQ == DG_WAVE ? NP * E : 0);
+  static constexpr int TC_FLOATS = TC_FLOATS_VOL > NP * NF * E ? TC_FLOATS_VOL : NP * NF * E;
+  static constexpr int TC = SMEM_BASE;
+  static constexpr int SMEM_BYTES_TC = TC + pad16(TC_FLOATS * 4);
 };
+
+// {{{ 3xTF32 tensor-core products (mixed precision, MODE_TC)
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// x = hi + lo with both parts TF32: hi carries 11 significant bits, lo the next 11
+__device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_rna(x);
+  lo = tf32_rna(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32(float* c, const uint32_t* a, uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// C (M x NC, FP32, row-major with leading dimension NC) = A (M x K) B (K x NC)
+// with A(m, k), B(k, n) read through accessors (zero outside the ranges),
+// a b = a_hi b_hi + a_hi b_lo + a_lo b_hi in FP32 (relative error ~2^-21,
+// the accuracy of FP32 arithmetic).  Warp units: one m-tile x two n-tiles.
+template <int M, int K, int NC, class FA, class FB>
+__device__ __forceinline__ void tf32x3_gemm(FA fa, FB fb, float* out) {
+  constexpr int MT = (M + 15) / 16, KT = (K + 7) / 8, NT = (NC + 7) / 8;
+  constexpr int NB = (NT + 1) / 2, UNITS = MT * NB;
+  const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
+  for (int u = threadIdx.x >> 5; u < UNITS; u += kBlock / 32) {
+    const int mt = u / NB, nt0 = 2 * (u - mt * NB);
+    const bool two = nt0 + 1 < NT;
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    const int r0 = mt * 16 + g, r1 = r0 + 8;
+#pragma unroll 2
+    for (int kt = 0; kt < KT; ++kt) {
+      const int k0 = kt * 8 + tq, k1 = k0 + 4;
+      uint32_t ah[4], al[4];
+      tf32_split(r0 < M && k0 < K ? fa(r0, k0) : 0.f, ah[0], al[0]);
+      tf32_split(r1 < M && k0 < K ? fa(r1, k0) : 0.f, ah[1], al[1]);
+      tf32_split(r0 < M && k1 < K ? fa(r0, k1) : 0.f, ah[2], al[2]);
+      tf32_split(r1 < M && k1 < K ? fa(r1, k1) : 0.f, ah[3], al[3]);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        if (q == 1 && !two) break;
+        const int n = (nt0 + q) * 8 + g;
+        uint32_t bh0, bl0, bh1, bl1;
+        tf32_split(n < NC && k0 < K ? fb(k0, n) : 0.f, bh0, bl0);
+        tf32_split(n < NC && k1 < K ? fb(k1, n) : 0.f, bh1, bl1);
+        mma_tf32(acc[q], al, bh0, bh1);
+        mma_tf32(acc[q], ah, bl0, bl1);
+        mma_tf32(acc[q], ah, bh0, bh1);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q == 1 && !two) break;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int row = c >= 2 ? r1 : r0;
+        const int col = (nt0 + q) * 8 + 2 * tq + (c & 1);
+        if (row < M && col < NC) out[row * NC + col] = acc[q][c];
+      }
+    }
+  }
+}
+
+// }}}
 
 // FP64 reciprocal from the FP32 estimate refined by one Newton step
 // (relative error below 2^-45).  The mixed-precision path uses it for the
@@ -176,7 +257,9 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   using Ops = OpsLayout<N, Real>;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
   constexpr bool SPLIT = (MODE & MODE_SPLIT) != 0;
+  constexpr bool TCM = (MODE & MODE_TC) != 0;
   static_assert(!(SPLIT && T::MIXED), "the face-shared path is FP64 only");
+  static_assert(!TCM || T::MIXED, "tensor-core products are a mixed-precision mode");
   constexpr int NP = T::NP, NFPT = T::NFPT, NF = T::NF, E = T::E;
   constexpr int ROW = T::ROW, FROW = T::FROW;  // shared-memory row pitches
   extern __shared__ __align__(128) unsigned char smem[];
@@ -194,6 +277,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   Real* sG = reinterpret_cast<Real*>(smem + T::GEO);
   Real* sFG = reinterpret_cast<Real*>(smem + T::FGEO);
   double* sP = reinterpret_cast<double*>(smem + T::PRES);
+  float* sTC = reinterpret_cast<float*>(smem + T::TC);  // MODE_TC outputs
 
   const int t = threadIdx.x;
   if (t == 0) {
@@ -326,7 +410,60 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     Real vol[NF];
 #pragma unroll
     for (int k = 0; k < NF; ++k) vol[k] = zero;
-    if (active && el < ecount) {
+    if constexpr (TCM) {
+      // tensor-core products into sTC, then the per-node combinations
+      constexpr int VNC = T::VOL_NC;
+      if constexpr (EQ == DG_WAVE) {
+        tf32x3_gemm<3 * NP, NP, E>(
+            [&](int m, int k) { return sW[m * ROW + k]; },
+            [&](int k, int n) { return sQr[n * ROW + k]; }, sTC);
+        tf32x3_gemm<NP, 3 * NP, E>(
+            [&](int m, int k) { const int r = k / NP; return sW[(r * NP + m) * ROW + k - r * NP]; },
+            [&](int k, int n) { const int r = k / NP; return sAux[(r * E + n) * ROW + k - r * NP]; },
+            sTC + 3 * NP * E);
+      } else if constexpr (EQ == DG_EULER) {
+        tf32x3_gemm<NP, 3 * NP, VNC>(
+            [&](int m, int k) { const int r = k / NP; return sW[(r * NP + m) * ROW + k - r * NP]; },
+            [&](int k, int n) {
+              const int r = k / NP, f = n / E, e = n - f * E;
+              return sAux[((f * 3 + r) * E + e) * ROW + k - r * NP];
+            },
+            sTC);
+      } else {
+        tf32x3_gemm<3 * NP, NP, VNC>(
+            [&](int m, int k) { return sW[m * ROW + k]; },
+            [&](int k, int n) { return sQr[n * ROW + k]; }, sTC);
+      }
+      __syncthreads();
+      if (active && el < ecount) {
+        const Real* G = sG + el * 9;
+        if constexpr (EQ == DG_WAVE) {
+          const float ur0 = sTC[(0 * NP + i) * E + el], ur1 = sTC[(1 * NP + i) * E + el],
+                      ur2 = sTC[(2 * NP + i) * E + el];
+          const Real c = p0;
+          vol[0] = -c * sTC[3 * NP * E + i * E + el];
+#pragma unroll
+          for (int x = 0; x < 3; ++x)
+            vol[1 + x] = -c * fma(G[0 * 3 + x], ur0, fma(G[1 * 3 + x], ur1, G[2 * 3 + x] * ur2));
+        } else if constexpr (EQ == DG_EULER) {
+#pragma unroll
+          for (int k = 0; k < 5; ++k) vol[k] = sTC[i * VNC + k * E + el];
+        } else {
+          auto dx = [&](int k, int x) {
+            const float d0 = sTC[(0 * NP + i) * VNC + k * E + el];
+            const float d1 = sTC[(1 * NP + i) * VNC + k * E + el];
+            const float d2 = sTC[(2 * NP + i) * VNC + k * E + el];
+            return fma(G[0 * 3 + x], d0, fma(G[1 * 3 + x], d1, G[2 * 3 + x] * d2));
+          };
+          vol[0] = dx(5, 1) - dx(4, 2);
+          vol[1] = dx(3, 2) - dx(5, 0);
+          vol[2] = dx(4, 0) - dx(3, 1);
+          vol[3] = -(dx(2, 1) - dx(1, 2));
+          vol[4] = -(dx(0, 2) - dx(2, 0));
+          vol[5] = -(dx(1, 0) - dx(0, 1));
+        }
+      }
+    } else if (active && el < ecount) {
       const Real* G = sG + el * 9;
       if constexpr (T::MIXED) {
         // float4 operands: four matrix entries per 16-byte shared load
@@ -617,13 +754,21 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     // }}}
 
     // {{{ 5. LIFT, then store or fold into the RK stage
+    if constexpr (TCM) {
+      tf32x3_gemm<NP, NFPT, NF * E>(
+          [&](int m, int k) { return sL[m * FROW + k]; },
+          [&](int k, int n) { return sFlux[n * FROW + k]; }, sTC);
+      __syncthreads();
+    }
     if (active && el < ecount) {
       const Real* fl = sFlux + el * FROW;
       int64_t gidx = e0 * NP + (el * NP + i);  // advanced by nelnp per field
 #pragma unroll
       for (int k = 0; k < NF; ++k, gidx += nelnp) {
         Real acc = vol[k];
-        if constexpr (T::MIXED) {
+        if constexpr (TCM) {
+          acc += sTC[i * (NF * E) + k * E + el];
+        } else if constexpr (T::MIXED) {
           const float4* lv = reinterpret_cast<const float4*>(sL + i * FROW);
           const float4* fv = reinterpret_cast<const float4*>(fl + k * E * FROW);
 #pragma unroll

@@ -15,16 +15,21 @@ namespace dg {
 namespace {
 
 template <int N, int EQ, typename Real, int MODE>
+constexpr int smem_of() {
+  return (MODE & MODE_TC) ? Tile<N, EQ, Real>::SMEM_BYTES_TC : Tile<N, EQ, Real>::SMEM_BASE;
+}
+
+template <int N, int EQ, typename Real, int MODE>
 cudaError_t shape_impl(LaunchShape* out) {
   using T = Tile<N, EQ, Real>;
+  constexpr int SMEM = smem_of<N, EQ, Real, MODE>();
   auto kern = dg_rhs_kernel<N, EQ, Real, MODE>;
   cudaError_t err = cudaFuncSetAttribute(
-      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM_BYTES);
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
   if (err != cudaSuccess) return err;
   int nb = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock,
-                                                      T::SMEM_BYTES);
-  out->smem_bytes = T::SMEM_BYTES;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, SMEM);
+  out->smem_bytes = SMEM;
   out->blocks_per_sm = nb;
   out->elems_per_tile = T::E;
   out->ops_bytes = OpsLayout<N, Real>::SIZE;
@@ -33,8 +38,7 @@ cudaError_t shape_impl(LaunchShape* out) {
 
 template <int N, int EQ, typename Real, int MODE>
 cudaError_t launch_impl(const RhsArgs& a, int grid, cudaStream_t s) {
-  using T = Tile<N, EQ, Real>;
-  dg_rhs_kernel<N, EQ, Real, MODE><<<grid, kBlock, T::SMEM_BYTES, s>>>(a);
+  dg_rhs_kernel<N, EQ, Real, MODE><<<grid, kBlock, smem_of<N, EQ, Real, MODE>(), s>>>(a);
   return cudaGetLastError();
 }
 
@@ -50,6 +54,12 @@ cudaError_t shape_mode(int mode, LaunchShape* out) {
       case MODE_SPLIT: return shape_impl<N, EQ, Real, MODE_SPLIT>(out);
       case MODE_SPLIT | MODE_STAGE:
         return shape_impl<N, EQ, Real, MODE_SPLIT | MODE_STAGE>(out);
+      default: break;
+    }
+  } else {
+    switch (mode) {
+      case MODE_TC: return shape_impl<N, EQ, Real, MODE_TC>(out);
+      case MODE_TC | MODE_STAGE: return shape_impl<N, EQ, Real, MODE_TC | MODE_STAGE>(out);
       default: break;
     }
   }
@@ -68,6 +78,13 @@ cudaError_t launch_mode(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
       case MODE_SPLIT: return launch_impl<N, EQ, Real, MODE_SPLIT>(a, grid, s);
       case MODE_SPLIT | MODE_STAGE:
         return launch_impl<N, EQ, Real, MODE_SPLIT | MODE_STAGE>(a, grid, s);
+      default: break;
+    }
+  } else {
+    switch (mode) {
+      case MODE_TC: return launch_impl<N, EQ, Real, MODE_TC>(a, grid, s);
+      case MODE_TC | MODE_STAGE:
+        return launch_impl<N, EQ, Real, MODE_TC | MODE_STAGE>(a, grid, s);
       default: break;
     }
   }
@@ -89,7 +106,7 @@ cudaError_t launch_n(int precision, int mode, const RhsArgs& a, int grid,
 
 template <int EQ>
 cudaError_t shape_any(int order, int precision, int mode, LaunchShape* out) {
-  if ((precision != 0 && precision != 1) || mode < 0 || mode > 3)
+  if ((precision != 0 && precision != 1) || mode < 0 || mode > 7)
     return cudaErrorInvalidValue;
   switch (order) {
     case 1: return shape_n<1, EQ>(precision, mode, out);
@@ -103,7 +120,7 @@ cudaError_t shape_any(int order, int precision, int mode, LaunchShape* out) {
 template <int EQ>
 cudaError_t launch_any(int order, int precision, int mode, const RhsArgs& a,
                        int grid, cudaStream_t s) {
-  if ((precision != 0 && precision != 1) || mode < 0 || mode > 3)
+  if ((precision != 0 && precision != 1) || mode < 0 || mode > 7)
     return cudaErrorInvalidValue;
   switch (order) {
     case 1: return launch_n<1, EQ>(precision, mode, a, grid, s);

@@ -42,6 +42,13 @@ class Ensemble:
     def shape(self):
         return self.plan.shape
 
+    def autotune(self, q: torch.Tensor, reps: int = 3) -> dict:
+        """Pick the launch variant of the batched kernel (tensor-core or
+        CUDA-core products, persistent or one-CTA-per-tile grid) by timing
+        it on the ensemble state ``q``; call before :meth:`capture`."""
+        self.tuning = self.plan.autotune(q, reps)
+        return self.tuning
+
     def member(self, x: torch.Tensor, k: int) -> torch.Tensor:
         """View of member ``k`` in an ensemble-shaped tensor."""
         return x[:, int(self.offsets[k]):int(self.offsets[k + 1]), :]

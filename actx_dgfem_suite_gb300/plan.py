@@ -226,6 +226,27 @@ class DevicePlan:
             ctypes.c_void_p(scratch.data_ptr()), _stream_handle(stream)))
         return out
 
+    #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per tile
+    VARIANTS = {0: "persistent", 1: "tensor-core, persistent", 2: "one CTA per tile",
+                3: "tensor-core, one CTA per tile"}
+
+    def set_variant(self, variant: int) -> None:
+        _lib.check(self._lib.dg_plan_set_variant(self._handle, int(variant)))
+
+    def autotune(self, q: torch.Tensor, reps: int = 3, stream=None) -> dict:
+        """Time the supported launch variants on state ``q`` and keep the
+        fastest; returns ``{"chosen": v, "ms": {variant: ms or None}}``."""
+        self._check_tensor(q, "state")
+        out = torch.empty_like(q)
+        chosen = ctypes.c_int32()
+        ms = (ctypes.c_float * 4)()
+        _lib.check(self._lib.dg_plan_autotune(
+            self._handle, ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+            int(reps), _stream_handle(stream), ctypes.byref(chosen), ms))
+        return {"chosen": chosen.value,
+                "ms": {self.VARIANTS[v]: (float(ms[v]) if ms[v] >= 0 else None)
+                       for v in range(4)}}
+
     def vjp(self, q: torch.Tensor, x: torch.Tensor, out: torch.Tensor | None = None,
             stream=None) -> torch.Tensor:
         """``(dL/dq (q))^T x`` (FP64 wave and Euler plans with face partners)."""

@@ -61,6 +61,7 @@ def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
             p.disc._cache.clear()
     setup_s = time.perf_counter() - t0
 
+    tuning = ens.autotune(q, reps=3)
     ens.capture(q, out)
     stream = torch.cuda.current_stream()
     for _ in range(3):
@@ -111,6 +112,7 @@ def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
         "rel_l2_err_vs_fp64": float(np.sqrt(num / den)),
         "setup_s": setup_s,
         "plan": ens.plan.info(),
+        "autotune": tuning,
     }
 
 

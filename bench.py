@@ -268,6 +268,9 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step) -> dict:
             plans.append(op.plan_for(actx))
             op.precision = "fp64"
         outs = [torch.empty_like(r["q"]) for r in runs]
+        # the autotuner picks each plan's launch variant (tensor-core or CUDA-core
+        # products, persistent or one-CTA-per-tile grid) on the case's own state
+        tuned = [p.autotune(r["q"], reps=2) for p, r in zip(plans, runs)]
         for _ in range(2):
             for p, r, o in zip(plans, runs, outs):
                 p.rhs(r["q"], o)
@@ -291,6 +294,8 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step) -> dict:
             "speedup_vs_fp64": fp64_ms_per_step / sum(times),
             "max_rel_l2_err_vs_fp64": max(errs),
             "cases_ms": {f"{r['eq']}{r['order']}": t for r, t in zip(runs, times)},
+            "autotuned_variant": {f"{r['eq']}{r['order']}": p.VARIANTS[tu["chosen"]]
+                                  for r, p, tu in zip(runs, plans, tuned)},
         }
         del outs
     except Exception as exc:  # report, keep the main line

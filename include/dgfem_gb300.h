@@ -206,6 +206,22 @@ typedef struct dg_box_desc {
 
 int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 
+/* Launch variant of the plan's main kernel: bit 0 = contractions on the
+ * tensor cores (DG_FP32_MIXED plans: 3xTF32 split with FP32 accumulation,
+ * i.e. FP32 accuracy), bit 1 = one CTA per tile instead of the persistent
+ * grid.  Default 0.  No counterpart in the reference. */
+int dg_plan_set_variant(dg_plan* plan, int32_t variant);
+
+/* Time every variant the plan supports (after one warm-up launch, `reps`
+ * launches of dg_rhs(q -> rhs) each, CUDA events on `stream`), keep the
+ * fastest and report it in *chosen (may be NULL); ms_per_variant (may be
+ * NULL) receives 4 floats, -1 for variants the plan does not support.
+ * Writes rhs.  The autotuner of the batched (ensemble) path: the reference
+ * fixes its loop-nest tiling in its loopy transforms instead
+ * (actx_dgfem_suite/arraycontext/batched_einsum_loop_transforms.py:142). */
+int dg_plan_autotune(dg_plan* plan, const double* q, double* rhs, int32_t reps,
+                     void* stream, int32_t* chosen, float* ms_per_variant);
+
 /* Release the plan's device buffers.  Replaces dropping the compiled program
  * and freeing the memory pool (actx_dgfem_suite/tools/wave_dof_scaling.py:108-126). */
 int dg_plan_destroy(dg_plan* plan);

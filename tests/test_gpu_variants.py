@@ -1,0 +1,73 @@
+"""Launch variants and the autotuner: the mixed-precision kernel with its
+contractions on the tensor cores (3xTF32, FP32 accumulation) keeps the
+mixed path's accuracy; the one-CTA-per-tile grid gives identical results."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from tests._helpers import jittered_box_mesh, make_problem
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RTOL = 1e-5
+
+
+def _plans(equation, order, seed=0):
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem(equation, jittered_box_mesh(4), order, seed=seed)
+    dm = DeviceMesh(prob.disc, "cuda:0")
+    ref = DevicePlan(dm, equation, prob.params, "fp64")
+    mixed = DevicePlan(dm, equation, prob.params, "fp32-mixed")
+    return prob, ref, mixed
+
+
+@pytest.mark.parametrize("equation", ["wave", "euler", "maxwell"])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_tensor_core_mixed_matches_fp64(equation, order):
+    prob, ref, mixed = _plans(equation, order, seed=order)
+    q = torch.from_numpy(prob.fields).cuda()
+    r64 = ref.rhs(q)
+    mixed.set_variant(0)
+    r0 = mixed.rhs(q)
+    mixed.set_variant(1)
+    assert mixed.info()["tensor_cores"]
+    r1 = mixed.rhs(q)
+    mixed.set_variant(3)
+    r3 = mixed.rhs(q)
+    mixed.finish()
+    n64 = float(torch.linalg.norm(r64))
+    assert float(torch.linalg.norm(r1 - r64)) <= MIXED_RTOL * n64
+    assert float(torch.linalg.norm(r1 - r0)) <= MIXED_RTOL * n64
+    assert torch.equal(r1, r3)            # same tiles, same arithmetic
+
+
+def test_tensor_core_mixed_rk_stage():
+    prob, ref, mixed = _plans("euler", 3, seed=4)
+    q = torch.from_numpy(prob.fields).cuda()
+    outs = []
+    for plan, variant in ((ref, 0), (mixed, 1)):
+        plan.set_variant(variant)
+        res = torch.zeros_like(q)
+        qo = torch.empty_like(q)
+        plan.rk_stage(q, qo, res, 0.0, 0.5, 1e-3)
+        plan.finish()
+        outs.append((qo, res))
+    dres = float(torch.linalg.norm(outs[1][1] - outs[0][1]))
+    assert dres <= MIXED_RTOL * float(torch.linalg.norm(outs[0][1]))
+
+
+def test_autotune_picks_a_supported_variant():
+    prob, ref, mixed = _plans("maxwell", 3)
+    q = torch.from_numpy(prob.fields).cuda()
+    res = mixed.autotune(q, reps=2)
+    assert res["chosen"] in (0, 1, 2, 3)
+    assert all(v is not None and v > 0 for v in res["ms"].values())
+    res64 = ref.autotune(q, reps=2)
+    assert res64["chosen"] in (0, 2)
+    assert res64["ms"]["tensor-core, persistent"] is None
+    from actx_dgfem_suite_gb300._lib import DGError
+    with pytest.raises(DGError):
+        ref.set_variant(1)
