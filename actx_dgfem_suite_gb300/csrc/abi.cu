@@ -383,13 +383,17 @@ uint16_t half_bits(int d) {
 
 // One product's block: A (m x k, element (r, c) = at(r, c)) as 8 FP16 digit
 // slices of its rows' 54-bit fixed-point integers (balanced base-128 digits,
-// slice 0 most significant), in 512-byte ldmatrix.x4 blocks per (slice,
-// m-tile, k-step), then the row exponents.
+// slice 0 most significant) in the K-major no-swizzle layout of the
+// tensor-core descriptors (element (r, c) at (r/8) SBO + (c/8) 128 + (r%8) 16
+// + (c%8) 2 bytes, SBO = 128 * k-chunks, rows padded to a multiple of 8),
+// then the row exponents.
 template <class At>
 int pack_gemm(unsigned char* out, int m, int k, At at) {
-  const int mp = r16h(m), kp = r16h(k), mt = mp / 16, kt = kp / 16;
-  const int digits = 8 * mt * kt * 512;
-  const int bytes = (digits + mp * 4 + 15) & ~15;
+  const int mr8 = (m + 7) & ~7, kp = r16h(k), kc = kp / 8;
+  const int sbo = kc * 128;
+  const int slice = (mr8 / 8) * sbo;
+  const int digits = 8 * slice;
+  const int bytes = (digits + mr8 * 4 + 15) & ~15;
   if (!out) return bytes;
   std::memset(out, 0, bytes);             // FP16 zero
   int32_t* row_exp = reinterpret_cast<int32_t*>(out + digits);
@@ -401,13 +405,12 @@ int pack_gemm(unsigned char* out, int m, int k, At at) {
     row_exp[r] = e;
     for (int c = 0; c < k; ++c) {
       long long x = std::llrint(std::ldexp(at(r, c), 54 - e));
-      const int rr = r & 15, cc = c & 15;
-      const int within = ((rr >> 3) + 2 * (cc >> 3)) * 128 + (rr & 7) * 16 + (cc & 7) * 2;
+      const int within = (r / 8) * sbo + (c / 8) * 128 + (r % 8) * 16 + (c % 8) * 2;
       for (int sl = 7; sl >= 0; --sl) {   // least significant digit first
         const long long d = ((x + 64) & 127) - 64;
         x = (x - d) >> 7;
         const uint16_t h = half_bits(static_cast<int>(d));
-        unsigned char* dst = out + ((sl * mt + (r >> 4)) * kt + (c >> 4)) * 512 + within;
+        unsigned char* dst = out + sl * slice + within;
         dst[0] = static_cast<unsigned char>(h & 0xff);
         dst[1] = static_cast<unsigned char>(h >> 8);
       }
@@ -522,7 +525,7 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   // face points fit 31-bit indices; the fused kernel serves all others
   const bool split = mesh->face_partner && kprec == 0 &&
                      mesh->nelements * 4 * (int64_t)nfp < (int64_t(1) << 31);
-  const bool tc = split && precision == DG_FP64_TC;
+  const bool tc = split && precision == DG_FP64_TC && N >= 3;
   if (mesh->face_partner) {
     cudaPointerAttributes attr;
     if (cudaPointerGetAttributes(&attr, mesh->face_partner) != cudaSuccess ||

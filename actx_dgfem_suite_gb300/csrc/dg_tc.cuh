@@ -2,35 +2,43 @@
 // by FP16 digit slices (error-free splitting in the manner of Ozaki et al.,
 // "Error-free transformations of matrix multiplication by using fast
 // routines of matrix multiplication and its applicability", Numer.
-// Algorithms 59, 2012).
+// Algorithms 59, 2012), issued as tcgen05 products with accumulators in
+// tensor memory.
 //
-// GB300 issues FP64 at about 1.2 TFLOP/s but FP16 tensor-core products at
-// hundreds of TFLOP/s, and the high-order DG contractions (volume
-// derivatives, LIFT) keep the FP64 pipe ~97 % busy.  Here every contraction
-// C = A X (A: a reference operator, M x K; X: K x NC columns of FP64 data,
-// one column per element and field) is evaluated as
+// GB300 issues FP64 at about 1.25 TFLOP/s but FP16 tensor-core products at
+// petaflop rates, and the high-order DG contractions (volume derivatives,
+// LIFT) keep the FP64 pipe ~97 % busy.  Here every contraction C = A X
+// (A: a reference operator, M x K; X: K x NC columns of FP64 data, one column
+// per element and field) is evaluated as
 //
 //   A = 2^(e_m - 54) A_int,  X = 2^(e_n - 54) X_int   (per-row / per-column
 //   exponents, 54-bit integers), each integer written as 8 balanced base-128
 //   digits d_1..d_8 in [-64, 64] (exact in FP16);
-//   v_l = sum_{i + j = l} D^A_i D^X_j    for l = 2..9, one FP16 tensor-core
-//   GEMM per digit pair, accumulated in FP32 -- exactly, because
-//   |v_l| <= 8 * K * 64^2 < 2^22 for K <= 112;
+//   v_l = sum_{i + j = l} D^A_i D^X_j    for l = 2..9: one tcgen05.mma
+//   (kind::f16, M = 128, K = 16, FP32 accumulation in tensor memory) per
+//   digit pair and k-step, all pairs of a level accumulating into that
+//   level's tensor-memory columns -- exactly, because |v_l| <= 8 K 64^2 < 2^22
+//   for K <= 112;
 //   C = 2^(e_m + e_n - 31) (G_hi + 2^-28 G_lo),  G_hi = sum_{l<=5} v_l 2^(7(5-l)),
-//   G_lo = sum_{l>=6} v_l 2^(7(9-l)) in 64-bit integers (exact).
+//   G_lo = sum_{l>=6} v_l 2^(7(9-l)) in 64-bit integers (exact), read out of
+//   tensor memory with tcgen05.ld.
 //
 // Dropped digit pairs (l > 9) and the 54-bit rounding of the inputs bound the
 // error by ~2^-53 of sum_k |A_mk| |X_kn| -- the size of FP64's own
-// rounding.  Splitting and recombination are integer work (no FP64 pipe);
-// per output the FP64 pipe sees 4 instructions instead of K FMAs.
+// rounding.  Splitting and recombination are integer work (no FP64 pipe).
+//
+// One thread issues all products of a contraction (asynchronous, completion
+// signalled on an mbarrier through tcgen05.commit; the wait is bounded);
+// operands come from shared memory through matrix descriptors (K-major, no
+// swizzle: 8-row x 16-byte core matrices, k-chunks 128 bytes apart, 8-row
+// groups SBO bytes apart).  The CTA allocates tensor memory once (8 levels x
+// the padded column count, at most 512 columns) and frees it before it exits.
 //
 // The kernel is the volume/LIFT half of the face-shared path: face values
 // come from dg_face_flux_kernel (and, for Euler, pressure and 1/rho from
 // dg_euler_aux_kernel), pointwise work (Euler fluxes, metric terms, curl,
-// RK epilogue) stays in FP64.  Tensor-core products use the warp-level
-// mma.sync m16n8k16 FP16 -> FP32 form: its operands come from registers and
-// shared memory the kernel itself fills, so no tensor-memory allocation or
-// asynchronous completion is involved.
+// RK epilogue) stays in FP64.  Orders 3 and 4 (lower orders have too little
+// contraction work for the digit splitting to pay).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -52,37 +60,47 @@ constexpr int r8(int x) { return (x + 7) & ~7; }
 constexpr int p16(int bytes) { return (bytes + 15) & ~15; }
 
 // One emulated product: operator A (M x K) times NC data columns of length K.
-//   operator block (global and shared): FP16 digits in blocks of 512 bytes per
-//   (digit s, m-tile, k-step), each block the four 8 x 8 matrices of the mma
-//   A fragment in ldmatrix.x4 order (rows 0-7 / 8-15 x columns 0-7 / 8-15),
-//   then M_P int32 row exponents;
-//   data slices (shared): FP16 digits, blocks of 256 bytes per (digit, n-tile,
-//   k-step) in ldmatrix.x2 order (two 8 x 8 matrices, row = column n).
-// A warp unit covers 1 or 2 m-tiles x 2 n-tiles, so every operator
-// fragment loaded from shared memory feeds two tensor-core products.
+//   operator block (global and shared): 8 FP16 digit slices of A in the
+//   K-major canonical layout (element (m, k) at (m/8) SBO_A + (k/8) 128 +
+//   (m%8) 16 + (k%8) 2 bytes, SBO_A = KP/8 x 128; rows padded to a multiple of
+//   8), then one int32 exponent per padded row;
+//   data slices (shared): the same layout for the NPAD (>= NC) data columns.
+// The products read 128 operator rows from each slice: rows past the padded
+// M belong to the next slice or region and only feed output rows that are
+// never read.
 template <int M_, int K_, int NC_>
 struct Gemm {
   static constexpr int M = M_, K = K_, NC = NC_;
-  static constexpr int MP = r16(M), KP = r16(K), NCP = r8(NC);
-  static constexpr int MT = MP / 16, KT = KP / 16, NT = NCP / 8;
-  // warp unit: UM x 2 tiles; UM = 2 only when that still leaves >= 16 units
-  static constexpr int UM = ((MT + 1) / 2) * ((NT + 1) / 2) >= 16 ? 2 : 1;
-  static constexpr int MB = (MT + UM - 1) / UM, NB = (NT + 1) / 2;
-  static constexpr int UNITS = MB * NB;
-  static constexpr int DIGITS = kS * MT * KT * 512;
-  static constexpr int OPS_BYTES = p16(DIGITS + MP * 4);
-  static constexpr int SLICE_STRIDE = NT * KT * 256;   // bytes per digit slice
-  static constexpr int SLICE_BYTES = kS * SLICE_STRIDE;
+  static constexpr int MR8 = r8(M), KP = r16(K), KC = KP / 8, KT = KP / 16;
+  static constexpr int NPAD = r16(NC);
+  static constexpr int SBO = KC * 128;
+  static constexpr int A_SLICE = (MR8 / 8) * SBO;
+  static constexpr int DIGITS = kS * A_SLICE;
+  static constexpr int OPS_BYTES = p16(DIGITS + MR8 * 4);
+  static constexpr int A_READ = 16 * SBO;             // bytes a product reads per slice
+  static constexpr int B_SLICE = (NPAD / 8) * SBO;
+  static constexpr int SLICE_BYTES = kS * B_SLICE;
+  static constexpr int TMEM_COLS = (kLevels - 1) * NPAD;
+  // instruction descriptor: D FP32, A and B FP16, both K-major, N, M = 128
+  static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(NPAD >> 3) << 17) | (8u << 24);
+  static_assert(M <= 128, "one 128-row product per contraction");
   static_assert(K <= 112, "exact FP32 level sums need K <= 112");
+  static_assert(TMEM_COLS <= 512, "levels x columns must fit in tensor memory");
 };
 
-// Elements per CTA tile: 256 / Np, fewer at order 4 so the FP16 operator
-// digits and the tile's slices fit in shared memory.
-constexpr int tile_elems(int N, int EQ, int np) {
-  return N < 4 ? 256 / np : (EQ == DG_EULER ? 5 : (EQ == DG_MAXWELL ? 6 : 7));
+// Elements per CTA tile: at most 64 data columns per contraction so the 8
+// level accumulators fit the 512 tensor-memory columns, and shared memory
+// for the FP16 operator digits at order 4.
+constexpr int tile_elems(int N, int EQ) {
+  return N == 3 ? (EQ == DG_MAXWELL ? 10 : 12)
+                : (EQ == DG_EULER ? 5 : (EQ == DG_MAXWELL ? 6 : 7));
 }
 
-// Products of one equation at order N.  GV, the volume product:
+constexpr int pow2_cols(int c) {
+  return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
+}
+
+// Products of one equation at order N (3 or 4).  GV, the volume product:
 //   wave, maxwell: stacked rows [A_0; A_1; A_2] (3 Np x Np) applied to
 //     columns (field f, element e) at n = f E + e -- maxwell the six fields,
 //     wave u and the three metric-combined velocity components (of whose
@@ -92,9 +110,10 @@ constexpr int tile_elems(int N, int EQ, int np) {
 // GL: LIFT (Np x 4 Nfp) applied to the face values of each (field, element).
 template <int N, int EQ>
 struct Plan {
+  static_assert(N >= 3, "tensor-core products are built for orders 3 and 4");
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
   static constexpr int NF = EqInfo<EQ>::NF;
-  static constexpr int E = tile_elems(N, EQ, NP);
+  static constexpr int E = tile_elems(N, EQ);
   static constexpr bool STACKED = EQ != DG_EULER;
   using GV = typename std::conditional<
       STACKED, Gemm<3 * NP, NP, (EQ == DG_WAVE ? 4 : NF) * E>,
@@ -109,7 +128,8 @@ struct Plan {
   static constexpr int R1_BYTES = p16(cmax(GV::SLICE_BYTES, GL::SLICE_BYTES));
   static constexpr int R2_BYTES = p16(8 * cmax(cmax(NAUX * E * NP, GV::M * GV::NC),
                                                NF * E * NFPT + GL::M * GL::NC));
-  static constexpr int NCOLS = cmax(GV::NCP, GL::NCP);
+  static constexpr int NCOLS = cmax(GV::NPAD, GL::NPAD);
+  static constexpr int TMEM_ALLOC = pow2_cols(cmax(GV::TMEM_COLS, GL::TMEM_COLS));
   // shared memory: ops | state (FP64) | R1 (slices) | R2 (FP64 scratch) |
   // metric | column exponents
   static constexpr int SM_OPS = 0;
@@ -118,37 +138,68 @@ struct Plan {
   static constexpr int SM_R2 = SM_R1 + R1_BYTES;
   static constexpr int SM_GEO = SM_R2 + R2_BYTES;
   static constexpr int SM_EXP = SM_GEO + p16(9 * E * 8);
-  static constexpr int SMEM_BYTES = SM_EXP + p16(NCOLS * 4);
+  static constexpr int SMEM_USED = SM_EXP + p16(NCOLS * 4);
+  // a CTA that takes all 512 tensor-memory columns must be alone on its SM
+  static constexpr int SMEM_BYTES =
+      TMEM_ALLOC == 512 && SMEM_USED < 120 * 1024 ? 120 * 1024 : SMEM_USED;
   static_assert(SMEM_BYTES <= 227 * 1024, "tile does not fit in shared memory");
+  // every product's reads of 128 operator rows / NPAD data rows stay in the CTA
+  static_assert(OPS_GV + 7 * GV::A_SLICE + GV::A_READ <= SMEM_BYTES, "GV operand reads");
+  static_assert(OPS_GL + 7 * GL::A_SLICE + GL::A_READ <= SMEM_BYTES, "GL operand reads");
 };
 
 // {{{ device helpers
 
-__device__ __forceinline__ void mma16816(float* c, const uint32_t* a, uint32_t b0,
-                                         uint32_t b1) {
+// {{{ tcgen05 helpers
+
+// shared-memory matrix descriptor: start address, leading (k-chunk) and
+// stride (8-row group) byte offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3fff) | ((uint64_t)((lbo >> 4) & 0x3fff) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3fff) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                       uint32_t idesc, uint32_t accumulate) {
   asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+      ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
 }
 
-// The "memory" clobbers keep the compiler from moving these shared-memory
-// reads above the barrier and the stores that fill the slices: the address
-// is a plain integer, so without it the read is invisible to alias analysis.
-__device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, uint32_t addr) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
-               : "=r"(r0), "=r"(r1)
-               : "r"(addr)
-               : "memory");
+// arrive on `bar` once every tcgen05 operation this thread issued has completed
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+      ::"r"(smem_u32(bar))
+      : "memory");
 }
 
-__device__ __forceinline__ void ldsm_x4(uint32_t* r, uint32_t addr) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(addr)
-               : "memory");
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+        "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
 }
+
+__device__ __forceinline__ void tc_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// shared-memory stores of this thread become visible to the tensor cores
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// }}}
 
 // two digits in [-64, 64] -> half2: the bit pattern 0x6600 + d is the half
 // 1536 + d, and one HSUB2 removes the 1536 exactly (bits move through the
@@ -225,13 +276,14 @@ __device__ __forceinline__ void digits8(long long x, int* d) {
 // }}}
 
 // Split data columns into FP16 digit slices (+ column exponent fields).
-// src(n, k) returns the FP64 value of column n < NC, row k < K.
+// src(n, k) returns the FP64 value of column n < NC, row k < K; columns up to
+// NPAD and rows up to KP are written as zero digits.
 template <class G, class Src>
 __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_emax,
                                               Src src) {
   const int t = threadIdx.x, lane = t & 31;
   // column exponents: one warp per column, lanes split the rows
-  for (int n = t >> 5; n < G::NCP; n += kBlock / 32) {
+  for (int n = t >> 5; n < G::NPAD; n += kBlock / 32) {
     int em = 0;
     if (n < G::NC)
       for (int k = lane; k < G::K; k += 32) {
@@ -246,15 +298,15 @@ __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_em
     if (lane == 0) col_emax[n] = em;
   }
   __syncthreads();
-  // digits: each warp fills whole 8 x 8 matrices, one 4-byte word (two rows
-  // k, k + 1 of one column) per lane, so the stores are free of bank conflicts
-  constexpr int ITEMS = G::NT * G::KT * 64;
+  // digits: each warp fills whole 8 x 16-byte core matrices, one 4-byte word
+  // (rows k, k + 1 of one column) per lane: stores free of bank conflicts
+  constexpr int ITEMS = (G::NPAD / 8) * G::KC * 32;
   for (int idx = t; idx < ITEMS; idx += kBlock) {
-    const int kp4 = idx & 3, nr = (idx >> 2) & 7, kh = (idx >> 5) & 1;
-    const int blk = idx >> 6;                 // nt * KT + kt
-    const int nt = blk / G::KT, kt = blk - nt * G::KT;
-    const int n = nt * 8 + nr;
-    const int k = kt * 16 + kh * 8 + 2 * kp4;
+    const int kp4 = idx & 3, nr = (idx >> 2) & 7;
+    const int blk = idx >> 5;                 // n-group * KC + k-chunk
+    const int ng = blk / G::KC, kc = blk - ng * G::KC;
+    const int n = ng * 8 + nr;
+    const int k = kc * 8 + 2 * kp4;
     long long x0 = 0, x1 = 0;
     if (n < G::NC) {
       const int em = col_emax[n];
@@ -264,106 +316,91 @@ __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_em
     int d0[kS], d1[kS];
     digits8(x0, d0);
     digits8(x1, d1);
-    unsigned char* dst = slices + blk * 256 + kh * 128 + nr * 16 + kp4 * 4;
+    unsigned char* dst = slices + ng * G::SBO + kc * 128 + nr * 16 + kp4 * 4;
 #pragma unroll
     for (int sl = 0; sl < kS; ++sl)
-      *reinterpret_cast<uint32_t*>(dst + sl * G::SLICE_STRIDE) = digits_to_half2(d0[sl], d1[sl]);
+      *reinterpret_cast<uint32_t*>(dst + sl * G::B_SLICE) = digits_to_half2(d0[sl], d1[sl]);
   }
+  fence_async_smem();
 }
 
-// One warp's unit of an emulated product: m-tiles 2 mb, 2 mb + 1 and n-tiles
-// 2 nb, 2 nb + 1 (where they exist).  Writes C (FP64) into out[row * NC + col].
+// Issue every digit-pair product of one contraction (one thread): level l
+// accumulates into tensor-memory columns (l - 2) NPAD.., then commit on `bar`.
 template <class G>
-__device__ __forceinline__ void gemm_unit(int unit, uint32_t ops_s, const int* row_exp,
-                                          uint32_t slices_s, const int* col_emax,
-                                          double* out) {
-  const int lane = threadIdx.x & 31;
-  const int mb = unit / G::NB;
-  const int mt0 = G::UM * mb, nt0 = 2 * (unit - mb * G::NB);
-  const bool m2 = G::UM == 2 && mt0 + 1 < G::MT, n2 = nt0 + 1 < G::NT;
-  long long ghi[2][2][4], glo[2][2][4];
-#pragma unroll
-  for (int a = 0; a < 2; ++a)
-#pragma unroll
-    for (int b = 0; b < 2; ++b)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) ghi[a][b][c] = glo[a][b][c] = 0;
-
+__device__ __forceinline__ void issue_products(uint32_t a_s, uint32_t b_s, uint32_t tmem,
+                                              uint64_t* bar) {
+  tc_fence_after();  // order after the barrier that published the slices / freed TMEM
 #pragma unroll 1
   for (int l = 2; l <= kLevels; ++l) {
-    float acc[2][2][4];
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int b = 0; b < 2; ++b)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
     const int ilo = l - kS > 1 ? l - kS : 1;
     const int ihi = l - 1 < kS ? l - 1 : kS;
-#pragma unroll 2
+    uint32_t acc = 0;
+#pragma unroll 1
     for (int i = ilo; i <= ihi; ++i) {
       const int j = l - i;
-      const uint32_t ablk = ops_s + ((i - 1) * G::MT + mt0) * G::KT * 512 + lane * 16;
-      const uint32_t bblk =
-          slices_s + (j - 1) * G::SLICE_STRIDE + nt0 * G::KT * 256 + (lane & 15) * 16;
 #pragma unroll
       for (int kt = 0; kt < G::KT; ++kt) {
-        uint32_t a0[4], a1[4], b0[2], b1[2];
-        ldsm_x4(a0, ablk + kt * 512);
-        ldsm_x2(b0[0], b0[1], bblk + kt * 256);
-        mma16816(acc[0][0], a0, b0[0], b0[1]);
-        if (n2) {
-          ldsm_x2(b1[0], b1[1], bblk + (G::KT + kt) * 256);
-          mma16816(acc[0][1], a0, b1[0], b1[1]);
-        }
-        if (m2) {
-          ldsm_x4(a1, ablk + (G::KT + kt) * 512);
-          mma16816(acc[1][0], a1, b0[0], b0[1]);
-          if (n2) mma16816(acc[1][1], a1, b1[0], b1[1]);
-        }
-      }
-    }
-    const int sh = l <= 5 ? 7 * (5 - l) : 7 * (9 - l);
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int b = 0; b < 2; ++b)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const long long v = (long long)((unsigned long long)(long long)
-                                              f32_exact_int(acc[a][b][c]) << sh);
-          if (l <= 5) ghi[a][b][c] += v;
-          else glo[a][b][c] += v;
-        }
-  }
-  const int g = lane >> 2, tq = lane & 3;
-#pragma unroll
-  for (int a = 0; a < 2; ++a) {
-    if (a == 1 && !m2) break;
-#pragma unroll
-    for (int b = 0; b < 2; ++b) {
-      if (b == 1 && !n2) break;
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int row = (mt0 + a) * 16 + g + (c >= 2 ? 8 : 0);
-        const int col = (nt0 + b) * 8 + 2 * tq + (c & 1);
-        if (row < G::M && col < G::NC) {
-          const double r = fma(i64_exact_double(glo[a][b][c]), 0x1p-28,
-                               i64_exact_double(ghi[a][b][c]));
-          out[row * G::NC + col] = r * pow2(row_exp[row] + col_emax[col] - 1022 - 31);
-        }
+        const uint64_t da = smem_desc(a_s + (i - 1) * G::A_SLICE + kt * 256, 128, G::SBO);
+        const uint64_t db = smem_desc(b_s + (j - 1) * G::B_SLICE + kt * 256, 128, G::SBO);
+        tc_mma(tmem + (uint32_t)((l - 2) * G::NPAD), da, db, G::IDESC, acc);
+        acc = 1;
       }
     }
   }
+  tc_commit(bar);
 }
 
-// All units of one product, spread over the CTA's warps.
+// Read the level sums out of tensor memory and recombine them.  Warp w may
+// read tensor-memory lanes 32 (w % 4).. only; lanes (= rows) at or past M and
+// columns at or past NC are skipped (warp-uniformly), and the columns of a
+// lane quadrant are shared by the warps that can read it.  Per 8 columns the
+// 8 level loads are issued before one wait.  Writes C (FP64) into
+// out[row * NC + col].
 template <class G>
-__device__ __forceinline__ void gemm_all(uint32_t ops_s, const int* row_exp,
-                                         uint32_t slices_s, const int* col_emax,
-                                         double* out) {
-  for (int u = threadIdx.x >> 5; u < G::UNITS; u += kBlock / 32)
-    gemm_unit<G>(u, ops_s, row_exp, slices_s, col_emax, out);
+__device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
+                                             const int* col_emax, double* out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = warp & 3;
+  if (32 * q >= G::M) return;                    // no real rows in this quadrant
+  constexpr int NW = kBlock / 32 / 4;            // warps per lane quadrant
+  const int row = 32 * q + lane;
+  const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
+  const int e_row = row < G::M ? row_exp[row] : 0;
+  constexpr int CHUNKS = (G::NC + 7) / 8;
+#pragma unroll 1
+  for (int ch = warp >> 2; ch < CHUNKS; ch += NW) {
+    const int c0 = ch * 8;
+    uint32_t v[kLevels - 1][8];
+#pragma unroll
+    for (int l = 0; l < kLevels - 1; ++l)
+      tc_ld8(tq + (uint32_t)(l * G::NPAD + c0), v[l]);
+    tc_wait_ld();
+    long long ghi[8], glo[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      long long hi = 0, lo = 0;
+#pragma unroll
+      for (int l = 2; l <= kLevels; ++l) {
+        const int sh = l <= 5 ? 7 * (5 - l) : 7 * (9 - l);
+        const long long w = (long long)((unsigned long long)(long long)
+                                            f32_exact_int(__uint_as_float(v[l - 2][j])) << sh);
+        if (l <= 5) hi += w;
+        else lo += w;
+      }
+      ghi[j] = hi;
+      glo[j] = lo;
+    }
+    if (row < G::M) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int col = c0 + j;
+        if (col < G::NC) {
+          const double r = fma(i64_exact_double(glo[j]), 0x1p-28, i64_exact_double(ghi[j]));
+          out[row * G::NC + col] = r * pow2(e_row + col_emax[col] - 1022 - 31);
+        }
+      }
+    }
+  }
 }
 
 }  // namespace tc
@@ -377,11 +414,14 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
+  __shared__ uint64_t mma_bar;
+  __shared__ uint32_t tmem_base;
   __shared__ int ops_ok;
 
   const int t = threadIdx.x;
   if (t == 0) {
     mbar_init(&bar, 1);
+    mbar_init(&mma_bar, 1);
     mbar_arrive_expect_tx(&bar, a.ops_bytes);
     bulk_g2s(smem + P::SM_OPS, a.ops, a.ops_bytes, &bar);
     const bool ok = mbar_wait_bounded(&bar, 0);
@@ -393,6 +433,18 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   }
   __syncthreads();
   if (!ops_ok) return;
+  // tensor memory for the level accumulators, held until the CTA exits
+  if ((t >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(smem_u32(&tmem_base)), "r"(P::TMEM_ALLOC)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  uint32_t mma_phase = 0;
 
   const uint32_t ops_s = smem_u32(smem + P::SM_OPS);
   const int* rexp_v = reinterpret_cast<const int*>(smem + P::SM_OPS + P::OPS_GV + GV::DIGITS);
@@ -403,6 +455,17 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   double* sR2 = reinterpret_cast<double*>(smem + P::SM_R2);
   double* sG = reinterpret_cast<double*>(smem + P::SM_GEO);
   int* sExp = reinterpret_cast<int*>(smem + P::SM_EXP);
+  // products of one contraction: issue (thread 0), wait (bounded), fold
+  auto contract = [&](auto gtag, uint32_t a_s, const int* rexp, double* out) {
+    using G = decltype(gtag);
+    if (t == 0) tc::issue_products<G>(a_s, sR1_s, tmem, &mma_bar);
+    if (!mbar_wait_bounded(&mma_bar, mma_phase)) raise_status(a.status, DG_ERR_TIMEOUT);
+    mma_phase ^= 1u;
+    tc::tc_fence_after();
+    tc::fold_products<G>(tmem, rexp, sExp, out);
+    tc::tc_fence_before();
+    __syncthreads();
+  };
 
   const int el = t / NP;
   const int i = t - el * NP;
@@ -488,8 +551,7 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
       tc::split_columns<GV>(sR1, sExp, [&](int n, int k) { return sQ[n * NP + k]; });
     }
     __syncthreads();
-    tc::gemm_all<GV>(ops_s + P::OPS_GV, rexp_v, sR1_s, sExp, sR2);
-    __syncthreads();
+    contract(GV{}, ops_s + P::OPS_GV, rexp_v, sR2);
     // }}}
 
     // {{{ 5. volume term per node (registers)
@@ -547,8 +609,7 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
     tc::split_columns<GL>(sR1, sExp, [&](int n, int k) { return sF[n * NFPT + k]; });
     __syncthreads();
     double* sL = sR2 + NF * E * NFPT;            // Np x (NF E)
-    tc::gemm_all<GL>(ops_s + P::OPS_GL, rexp_l, sR1_s, sExp, sL);
-    __syncthreads();
+    contract(GL{}, ops_s + P::OPS_GL, rexp_l, sL);
     // }}}
 
     // {{{ 8. epilogue: store or fold into the RK stage
@@ -573,6 +634,12 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
     __syncthreads();
     // }}}
   }
+  tc::tc_fence_before();
+  __syncthreads();
+  if ((t >> 5) == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 ::"r"(tmem), "r"(P::TMEM_ALLOC)
+                 : "memory");
 }
 
 }  // namespace dg

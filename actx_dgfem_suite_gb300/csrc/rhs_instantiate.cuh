@@ -206,12 +206,11 @@ cudaError_t tc_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// orders 3 and 4 only (the tensor-core products need the work of high orders)
 template <int EQ>
 cudaError_t tc_shape_any(int order, int mode, LaunchShape* out) {
   if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
   switch (order) {
-    case 1: return tc_shape_n<1, EQ>(mode, out);
-    case 2: return tc_shape_n<2, EQ>(mode, out);
     case 3: return tc_shape_n<3, EQ>(mode, out);
     case 4: return tc_shape_n<4, EQ>(mode, out);
     default: return cudaErrorInvalidValue;
@@ -223,8 +222,6 @@ cudaError_t tc_launch_any(int order, int mode, const RhsArgs& a, int grid,
                           cudaStream_t s) {
   if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
   switch (order) {
-    case 1: return tc_launch_n<1, EQ>(mode, a, grid, s);
-    case 2: return tc_launch_n<2, EQ>(mode, a, grid, s);
     case 3: return tc_launch_n<3, EQ>(mode, a, grid, s);
     case 4: return tc_launch_n<4, EQ>(mode, a, grid, s);
     default: return cudaErrorInvalidValue;

@@ -33,7 +33,8 @@ def _gpu_rhs(problem, path="tc"):
                       "fp64-tc" if path == "tc" else "fp64")
     info = plan.info()
     assert info["face_shared"] == (path != "fused")
-    assert info["tensor_cores"] == (path == "tc")
+    # tensor-core products are built for orders 3 and 4 (FP64 FMAs below)
+    assert info["tensor_cores"] == (path == "tc" and problem.disc.order >= 3)
     q = torch.from_numpy(problem.fields).to("cuda:0")
     out = plan.rhs(q)
     plan.finish()
@@ -107,8 +108,12 @@ def test_paths_agree_and_launch_counts(equation):
     a, plan_s = _gpu_rhs(prob, "shared")
     b, plan_f = _gpu_rhs(prob, "fused")
     c, plan_t = _gpu_rhs(prob, "tc")
+    d4, plan_t4 = _gpu_rhs(make_problem(equation, jittered_box_mesh(4), 4, seed=5), "tc")
+    e4, _ = _gpu_rhs(make_problem(equation, jittered_box_mesh(4), 4, seed=5), "fused")
     assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(b)
     assert np.linalg.norm(c - b) <= 1e-13 * np.linalg.norm(b)
+    assert np.linalg.norm(d4 - e4) <= 1e-13 * np.linalg.norm(e4)
+    assert plan_t4.info()["tensor_cores"]
     assert plan_t.info()["launches_per_rhs"] == plan_s.info()["launches_per_rhs"]
     info_s, info_f = plan_s.info(), plan_f.info()
     assert info_s["launches_per_rhs"] == (3 if equation == "euler" else 2)
