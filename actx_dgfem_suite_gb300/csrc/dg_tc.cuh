@@ -54,6 +54,8 @@ namespace tc {
 constexpr int kS = 8;        // digits per value
 constexpr int kFix = 54;     // fixed-point bits
 constexpr int kLevels = 9;   // digit pairs with i + j <= kLevels are kept
+constexpr int kTcBlock = 512;  // threads per CTA (one CTA per SM)
+static_assert(kLevels == 9, "the recombination folds levels 2..9");
 
 constexpr int r16(int x) { return (x + 15) & ~15; }
 constexpr int r8(int x) { return (x + 7) & ~7; }
@@ -230,6 +232,47 @@ __device__ __forceinline__ double pow2(int e) {
   return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// RN(W) 2^s with W = T 2^28 + f (T: int64, |T| < 2^46; f in [0, 2^28)), built
+// from integer operations only (GB300 issues FP64 at 1/64 of the integer
+// rate).  Magnitude M = A 2^28 + B; M < 2^64 is normalised directly, larger
+// M keeps its top 64 bits with the dropped bits jammed into a sticky bit
+// (then M >= 2^54, so the sticky bit sits below the rounding bit).  Round to
+// nearest, ties to even; the carry of a round-up moves into the exponent.
+// Returns false (out untouched) when the result is not a normal double.
+__device__ __forceinline__ bool fixed_to_double(long long T, unsigned f, int s, double* out) {
+  const bool neg = T < 0;
+  unsigned long long A = (unsigned long long)(neg ? -T - (f != 0u) : T);
+  const unsigned B = neg && f != 0u ? (1u << 28) - f : f;
+  unsigned long long Z;
+  int zexp;
+  if (A < (1ull << 36)) {
+    Z = (A << 28) | B;
+    zexp = 0;
+  } else {
+    Z = (A << 18) | (B >> 10) | (unsigned long long)((B & 1023u) != 0u);
+    zexp = 10;
+  }
+  if (Z == 0) {
+    *out = 0.0;
+    return true;
+  }
+  const int n = 63 - __clzll((long long)Z);
+  const int eb = n + zexp + s + 1023;
+  if (eb < 1 || eb > 2045) return false;
+  unsigned long long mant, up = 0;
+  if (n <= 52) {
+    mant = Z << (52 - n);
+  } else {
+    const int sh = n - 52;
+    mant = Z >> sh;
+    const unsigned long long rem = Z & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    up = (rem > half || (rem == half && (mant & 1ull))) ? 1ull : 0ull;
+  }
+  const unsigned long long bits = ((unsigned long long)eb << 52) + (mant - (1ull << 52)) + up;
+  *out = __longlong_as_double((long long)(bits | ((unsigned long long)neg << 63)));
+  return true;
+}
+
 // biased exponent field of a double (0 for zero and subnormals)
 __device__ __forceinline__ int dexp(double x) {
   return (__double2hiint(x) >> 20) & 0x7ff;
@@ -283,7 +326,7 @@ __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_em
                                               Src src) {
   const int t = threadIdx.x, lane = t & 31;
   // column exponents: one warp per column, lanes split the rows
-  for (int n = t >> 5; n < G::NPAD; n += kBlock / 32) {
+  for (int n = t >> 5; n < G::NPAD; n += kTcBlock / 32) {
     int em = 0;
     if (n < G::NC)
       for (int k = lane; k < G::K; k += 32) {
@@ -301,7 +344,7 @@ __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_em
   // digits: each warp fills whole 8 x 16-byte core matrices, one 4-byte word
   // (rows k, k + 1 of one column) per lane: stores free of bank conflicts
   constexpr int ITEMS = (G::NPAD / 8) * G::KC * 32;
-  for (int idx = t; idx < ITEMS; idx += kBlock) {
+  for (int idx = t; idx < ITEMS; idx += kTcBlock) {
     const int kp4 = idx & 3, nr = (idx >> 2) & 7;
     const int blk = idx >> 5;                 // n-group * KC + k-chunk
     const int ng = blk / G::KC, kc = blk - ng * G::KC;
@@ -354,15 +397,15 @@ __device__ __forceinline__ void issue_products(uint32_t a_s, uint32_t b_s, uint3
 // read tensor-memory lanes 32 (w % 4).. only; lanes (= rows) at or past M and
 // columns at or past NC are skipped (warp-uniformly), and the columns of a
 // lane quadrant are shared by the warps that can read it.  Per 8 columns the
-// 8 level loads are issued before one wait.  Writes C (FP64) into
-// out[row * NC + col].
+// 8 level loads are issued before one wait; the recombination is integer
+// work.  Writes C (FP64) into out[row * NC + col].
 template <class G>
 __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
                                              const int* col_emax, double* out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q = warp & 3;
   if (32 * q >= G::M) return;                    // no real rows in this quadrant
-  constexpr int NW = kBlock / 32 / 4;            // warps per lane quadrant
+  constexpr int NW = kTcBlock / 32 / 4;            // warps per lane quadrant
   const int row = 32 * q + lane;
   const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
   const int e_row = row < G::M ? row_exp[row] : 0;
@@ -375,28 +418,30 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
     for (int l = 0; l < kLevels - 1; ++l)
       tc_ld8(tq + (uint32_t)(l * G::NPAD + c0), v[l]);
     tc_wait_ld();
-    long long ghi[8], glo[8];
+    // level sums (exact integers |v_l| < 2^22) -> W = G_hi 2^28 + G_lo with
+    // G_hi = ((v2 2^7 + v3) 2^14 + (v4 2^7 + v5)), G_lo likewise from v6..v9
+    long long wt[8];
+    unsigned wf[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      long long hi = 0, lo = 0;
+      int x[kLevels - 1];
 #pragma unroll
-      for (int l = 2; l <= kLevels; ++l) {
-        const int sh = l <= 5 ? 7 * (5 - l) : 7 * (9 - l);
-        const long long w = (long long)((unsigned long long)(long long)
-                                            f32_exact_int(__uint_as_float(v[l - 2][j])) << sh);
-        if (l <= 5) hi += w;
-        else lo += w;
-      }
-      ghi[j] = hi;
-      glo[j] = lo;
+      for (int l = 0; l < kLevels - 1; ++l) x[l] = f32_exact_int(__uint_as_float(v[l][j]));
+      const long long hi = (long long)(x[0] * 128 + x[1]) * 16384 + (x[2] * 128 + x[3]);
+      const long long lo = (long long)(x[4] * 128 + x[5]) * 16384 + (x[6] * 128 + x[7]);
+      wt[j] = hi + (lo >> 28);
+      wf[j] = (unsigned)(lo & 0x0fffffffLL);
     }
     if (row < G::M) {
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int col = c0 + j;
         if (col < G::NC) {
-          const double r = fma(i64_exact_double(glo[j]), 0x1p-28, i64_exact_double(ghi[j]));
-          out[row * G::NC + col] = r * pow2(e_row + col_emax[col] - 1022 - 31);
+          const int sc = e_row + col_emax[col] - 1022 - 31;
+          double r;
+          if (!fixed_to_double(wt[j], wf[j], sc - 28, &r))  // not a normal double
+            r = fma((double)wf[j], 0x1p-28, i64_exact_double(wt[j])) * pow2(sc);
+          out[row * G::NC + col] = r;
         }
       }
     }
@@ -406,7 +451,7 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
 }  // namespace tc
 
 template <int N, int EQ, int MODE>
-__global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
+__global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
   using P = tc::Plan<N, EQ>;
   using GV = typename P::GV;
   using GL = typename P::GL;
@@ -483,10 +528,10 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
       const double* qk = a.q + e0 * NP;
 #pragma unroll
       for (int k = 0; k < NF; ++k, qk += nelnp)
-        for (int rem = t; rem < E * NP; rem += kBlock)
+        for (int rem = t; rem < E * NP; rem += tc::kTcBlock)
           sQ[k * (E * NP) + rem] = rem < ecount * NP ? __ldg(qk + rem) : 0.0;
       const double* mt = a.metric + e0 * 9;
-      for (int idx = t; idx < 9 * E; idx += kBlock)
+      for (int idx = t; idx < 9 * E; idx += tc::kTcBlock)
         sG[idx] = idx < 9 * ecount ? __ldg(mt + idx) : 0.0;
     }
     __syncthreads();
@@ -602,7 +647,7 @@ __global__ void __launch_bounds__(kBlock, 1) dg_rhs_tc_kernel(const RhsArgs a) {
       const double* fk = a.flux_in + e0 * NFPT;
 #pragma unroll
       for (int k = 0; k < NF; ++k, fk += nfpt_all)
-        for (int rem = t; rem < E * NFPT; rem += kBlock)
+        for (int rem = t; rem < E * NFPT; rem += tc::kTcBlock)
           sF[k * (E * NFPT) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : 0.0;
     }
     __syncthreads();

@@ -182,7 +182,7 @@ cudaError_t tc_shape_impl(LaunchShape* out) {
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
   if (err != cudaSuccess) return err;
   int nb = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, P::SMEM_BYTES);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, tc::kTcBlock, P::SMEM_BYTES);
   out->smem_bytes = P::SMEM_BYTES;
   out->blocks_per_sm = nb;
   out->elems_per_tile = P::E;
@@ -200,9 +200,9 @@ template <int N, int EQ>
 cudaError_t tc_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
   using P = tc::Plan<N, EQ>;
   if (mode == 0)
-    dg_rhs_tc_kernel<N, EQ, MODE_SPLIT><<<grid, kBlock, P::SMEM_BYTES, s>>>(a);
+    dg_rhs_tc_kernel<N, EQ, MODE_SPLIT><<<grid, tc::kTcBlock, P::SMEM_BYTES, s>>>(a);
   else
-    dg_rhs_tc_kernel<N, EQ, MODE_SPLIT | MODE_STAGE><<<grid, kBlock, P::SMEM_BYTES, s>>>(a);
+    dg_rhs_tc_kernel<N, EQ, MODE_SPLIT | MODE_STAGE><<<grid, tc::kTcBlock, P::SMEM_BYTES, s>>>(a);
   return cudaGetLastError();
 }
 
