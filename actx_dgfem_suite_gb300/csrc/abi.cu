@@ -140,7 +140,8 @@ struct dg_plan {
   int grid = 0;
   int64_t ntiles = 0;      // tiles of the main kernel
   int grid_mtc = 0;        // mixed precision with tensor-core products
-  int variant = 0;         // bit 0: tensor-core products (mixed); bit 1: one CTA per tile
+  int variant = 0;         // bit 0: tensor-core products (mixed); bit 1: one CTA per
+                           // tile; 4: the mixed kernel on tcgen05
   dg::LaunchShape shape;
   int device = 0;
   int nsm = 0;
@@ -160,6 +161,12 @@ struct dg_plan {
   uint32_t tc_ops_bytes = 0;
   dg::LaunchShape tc_shape;
   int tc_grid = 0;
+  // mixed precision with tcgen05 contractions (variant 4)
+  bool tcm = false;
+  void* d_tcm_ops = nullptr;
+  uint32_t tcm_ops_bytes = 0;
+  dg::LaunchShape tcm_shape;
+  int tcm_grid = 0;
   // face-shared path and adjoint (wave, FP64): the mesh's face_partner
   const int32_t* face_partner = nullptr;
   void* d_adj_ops = nullptr;
@@ -443,6 +450,46 @@ int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
   pack_gemm(out + gv, np, nfpt, gl);
   return total;
 }
+
+// TF32 (round to nearest, ties away from zero) of a float, as a float
+static float tf32_host(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  b = (b + 0x1000u) & 0xffffe000u;
+  float r;
+  std::memcpy(&r, &b, 4);
+  return r;
+}
+
+int pack_tcm_ops(int order, const double* diff, const double* lift,
+                 const int32_t* face_nodes, unsigned char* out, int out_bytes) {
+  const int np = (order + 1) * (order + 2) * (order + 3) / 6;
+  const int nfpt = 2 * (order + 1) * (order + 2);
+  const int nb = (np + 15) & ~15, kv = (3 * np + 7) & ~7, kl = (nfpt + 7) & ~7;
+  const int sbo_v = (kv / 4) * 128, sbo_l = (kl / 4) * 128;
+  const int bs_v = (nb / 8) * sbo_v, bs_l = (nb / 8) * sbo_l;
+  const int ops_l = 2 * bs_v, ops_fn = ops_l + 2 * bs_l;
+  const int total = ops_fn + ((nfpt * 4 + 15) & ~15);
+  if (!out) return total;
+  if (out_bytes != total) return -1;
+  std::memset(out, 0, total);
+  auto put = [&](int base, int slice, int sbo, int n, int k, double x) {
+    const int off = base + (n / 8) * sbo + (k / 4) * 128 + (n % 8) * 16 + (k % 4) * 4;
+    const float hi = tf32_host((float)x);
+    const float lo = tf32_host((float)(x - (double)hi));
+    std::memcpy(out + off, &hi, 4);
+    std::memcpy(out + off + slice, &lo, 4);
+  };
+  for (int i = 0; i < np; ++i)
+    for (int r = 0; r < 3; ++r)
+      for (int j = 0; j < np; ++j)
+        put(0, bs_v, sbo_v, i, r * np + j, diff[((size_t)r * np + i) * np + j]);
+  for (int i = 0; i < np; ++i)
+    for (int fj = 0; fj < nfpt; ++fj)
+      put(ops_l, bs_l, sbo_l, i, fj, lift[(size_t)i * nfpt + fj]);
+  std::memcpy(out + ops_fn, face_nodes, (size_t)nfpt * 4);
+  return total;
+}
 }  // namespace dg
 
 namespace {
@@ -462,6 +509,25 @@ cudaError_t tc_launch_of(int eq, int order, int mode, const dg::RhsArgs& a, int 
     case DG_WAVE: return dg::tc_launch_wave(order, mode, a, grid, s);
     case DG_EULER: return dg::tc_launch_euler(order, mode, a, grid, s);
     case DG_MAXWELL: return dg::tc_launch_maxwell(order, mode, a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t tcm_shape_of(int eq, int order, int mode, dg::LaunchShape* out) {
+  switch (eq) {
+    case DG_WAVE: return dg::tcm_shape_wave(order, mode, out);
+    case DG_EULER: return dg::tcm_shape_euler(order, mode, out);
+    case DG_MAXWELL: return dg::tcm_shape_maxwell(order, mode, out);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t tcm_launch_of(int eq, int order, int mode, const dg::RhsArgs& a, int grid,
+                          cudaStream_t s) {
+  switch (eq) {
+    case DG_WAVE: return dg::tcm_launch_wave(order, mode, a, grid, s);
+    case DG_EULER: return dg::tcm_launch_euler(order, mode, a, grid, s);
+    case DG_MAXWELL: return dg::tcm_launch_maxwell(order, mode, a, grid, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -610,6 +676,34 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     const int bps = t1.blocks_per_sm < t0.blocks_per_sm ? t1.blocks_per_sm : t0.blocks_per_sm;
     const int64_t tfull = (int64_t)nsm * (bps > 0 ? bps : 1);
     p->grid_mtc = (int)(ntiles < tfull ? ntiles : tfull);
+    // the tcgen05 form (variant 4)
+    dg::LaunchShape m0, m1;
+    err = tcm_shape_of(equation, N, 0, &m0);
+    if (err == cudaSuccess) err = tcm_shape_of(equation, N, 1, &m1);
+    const int mbytes = dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0);
+    if (err != cudaSuccess || mbytes != m0.ops_bytes) {
+      dg_plan_destroy(p);
+      return err != cudaSuccess ? cuda_fail(err, "tcgen05 mixed kernel configuration")
+                                : fail(DG_ERR_CUDA, "tcgen05 operator layout mismatch");
+    }
+    if (m1.blocks_per_sm < m0.blocks_per_sm) m0.blocks_per_sm = m1.blocks_per_sm;
+    if (m0.blocks_per_sm >= 1) {
+      std::vector<unsigned char> mops(mbytes);
+      dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, mops.data(), mbytes);
+      err = cudaMalloc(&p->d_tcm_ops, mbytes);
+      if (err == cudaSuccess)
+        err = cudaMemcpy(p->d_tcm_ops, mops.data(), mbytes, cudaMemcpyHostToDevice);
+      if (err != cudaSuccess) {
+        dg_plan_destroy(p);
+        return cuda_fail(err, "tcgen05 operator buffer");
+      }
+      p->tcm = true;
+      p->tcm_ops_bytes = static_cast<uint32_t>(mbytes);
+      p->tcm_shape = m0;
+      const int64_t mtiles = (p->nel + m0.elems_per_tile - 1) / m0.elems_per_tile;
+      const int64_t mfull = (int64_t)nsm * m0.blocks_per_sm;
+      p->tcm_grid = (int)(mtiles < mfull ? mtiles : mfull);
+    }
   }
   p->face_partner = mesh->face_partner;
 
@@ -701,9 +795,11 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
 
 int dg_plan_set_variant(dg_plan* p, int32_t variant) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
-  if (variant < 0 || variant > 3) return fail(DG_ERR_ARGUMENT, "variant must be 0..3");
+  if (variant < 0 || variant > 4) return fail(DG_ERR_ARGUMENT, "variant must be 0..4");
   if ((variant & 1) && p->precision != DG_FP32_MIXED)
     return fail(DG_ERR_UNSUPPORTED, "tensor-core products are a mixed-precision variant");
+  if (variant == 4 && !p->tcm)
+    return fail(DG_ERR_UNSUPPORTED, "the tcgen05 kernel is a mixed-precision variant");
   if (p->tc) return fail(DG_ERR_UNSUPPORTED, "DG_FP64_TC plans have one variant");
   p->variant = variant;
   return DG_OK;
@@ -714,7 +810,7 @@ int dg_plan_autotune(dg_plan* p, const double* q, double* rhs, int32_t reps,
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (!q || !rhs || reps < 1) return fail(DG_ERR_ARGUMENT, "bad autotune arguments");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const int nvar = p->tc ? 1 : 4;
+  const int nvar = p->tc ? 1 : (p->tcm ? 5 : 4);
   cudaEvent_t e0, e1;
   cudaError_t err = cudaEventCreate(&e0);
   if (err == cudaSuccess) err = cudaEventCreate(&e1);
@@ -723,7 +819,7 @@ int dg_plan_autotune(dg_plan* p, const double* q, double* rhs, int32_t reps,
   int best = -1;
   float best_ms = 0.f;
   int code = DG_OK;
-  for (int v = 0; v < 4 && code == DG_OK; ++v) {
+  for (int v = 0; v < 5 && code == DG_OK; ++v) {
     float ms = -1.f;
     if (v < nvar && ((v & 1) == 0 || p->precision == DG_FP32_MIXED)) {
       p->variant = v;
@@ -855,6 +951,10 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     a.ops = p->d_tc_ops;
     a.ops_bytes = p->tc_ops_bytes;
     err = tc_launch_of(p->equation, p->order, 0, a, p->tc_grid, s);
+  } else if (p->variant == 4) {
+    a.ops = p->d_tcm_ops;
+    a.ops_bytes = p->tcm_ops_bytes;
+    err = tcm_launch_of(p->equation, p->order, 0, a, p->tcm_grid, s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
                     main_mode(p, p->split ? dg::MODE_SPLIT : dg::MODE_RHS), a,
@@ -897,6 +997,10 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     a.ops = p->d_tc_ops;
     a.ops_bytes = p->tc_ops_bytes;
     err = tc_launch_of(p->equation, p->order, 1, a, p->tc_grid, s);
+  } else if (p->variant == 4) {
+    a.ops = p->d_tcm_ops;
+    a.ops_bytes = p->tcm_ops_bytes;
+    err = tcm_launch_of(p->equation, p->order, 1, a, p->tcm_grid, s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
                     main_mode(p, dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0)), a,
@@ -988,7 +1092,7 @@ int dg_plan_destroy(dg_plan* p) {
   if (p->d_status && cudaFree(p->d_status) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
   for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux,
-                  (void*)p->d_tc_ops})
+                  (void*)p->d_tc_ops, (void*)p->d_tcm_ops})
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
@@ -1011,7 +1115,8 @@ int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* tensor_cores,
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (face_shared) *face_shared = p->split ? 1 : 0;
   if (tensor_cores)
-    *tensor_cores = (p->tc || ((p->variant & 1) && p->precision == DG_FP32_MIXED)) ? 1 : 0;
+    *tensor_cores =
+        (p->tc || p->variant == 4 || ((p->variant & 1) && p->precision == DG_FP32_MIXED)) ? 1 : 0;
   if (launches_per_rhs)
     *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : 1;
   if (owned_faces) *owned_faces = p->split ? p->nowned : 0;
@@ -1025,9 +1130,12 @@ int dg_plan_info(const dg_plan* p, int64_t* nelements, int32_t* order,
   if (nelements) *nelements = p->nel;
   if (order) *order = p->order;
   if (nfields) *nfields = p->nfields;
-  if (grid) *grid = p->tc ? p->tc_grid : main_grid(p);
-  if (block) *block = dg::kBlock;
-  if (smem_bytes) *smem_bytes = p->tc ? p->tc_shape.smem_bytes : p->shape.smem_bytes;
+  const bool m4 = !p->tc && p->variant == 4;
+  if (grid) *grid = p->tc ? p->tc_grid : (m4 ? p->tcm_grid : main_grid(p));
+  if (block) *block = p->tc ? p->tc_shape.threads : (m4 ? p->tcm_shape.threads : dg::kBlock);
+  if (smem_bytes)
+    *smem_bytes = p->tc ? p->tc_shape.smem_bytes
+                        : (m4 ? p->tcm_shape.smem_bytes : p->shape.smem_bytes);
   return DG_OK;
 }
 

@@ -18,6 +18,7 @@ struct LaunchShape {
   int blocks_per_sm = 0;   // resident CTAs per SM at that footprint
   int elems_per_tile = 0;  // elements per CTA tile
   int ops_bytes = 0;       // size of the staged operator block
+  int threads = 256;       // threads per CTA
 };
 
 // Byte layout of the operator block, shared by host packing and the kernels'
@@ -53,6 +54,8 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
 // (Euler: the per-node table, then) the face kernel of the face-shared path.
 // tc_shape_* / tc_launch_*: the face-shared volume/LIFT kernel with the
 // contractions on the tensor cores (mode 0 RHS, 1 RK stage).
+// tcm_shape_* / tcm_launch_*: the mixed-precision kernel with its
+// contractions on tcgen05 (3xTF32; mode 0 RHS, 1 RK stage).
 #define DG_DECLARE_EQ(name)                                                   \
   cudaError_t shape_##name(int order, int precision, int mode,               \
                            LaunchShape* out);                                \
@@ -63,7 +66,10 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
                                  int aux_grid, cudaStream_t s);              \
   cudaError_t tc_shape_##name(int order, int mode, LaunchShape* out);        \
   cudaError_t tc_launch_##name(int order, int mode, const RhsArgs& a,        \
-                               int grid, cudaStream_t s);
+                               int grid, cudaStream_t s);                    \
+  cudaError_t tcm_shape_##name(int order, int mode, LaunchShape* out);       \
+  cudaError_t tcm_launch_##name(int order, int mode, const RhsArgs& a,       \
+                                int grid, cudaStream_t s);
 DG_DECLARE_EQ(wave)
 DG_DECLARE_EQ(euler)
 DG_DECLARE_EQ(maxwell)
@@ -72,11 +78,18 @@ DG_DECLARE_EQ(maxwell)
 // Operator block of the tensor-core kernel (layout of tc::Plan<N, EQ> in
 // dg_tc.cuh): the volume product [A_0; A_1; A_2] (3 Np x Np, wave and
 // maxwell) or [A_0 A_1 A_2] (Np x 3 Np, euler), then LIFT (Np x 4 Nfp).
-// Each: 8 FP16 digit slices of 512-byte blocks (slice, m-tile, k-step) in
-// ldmatrix.x4 order, then one int32 exponent per padded row; blocks padded
-// to 16 bytes.  Returns the block size.
+// Each: 8 FP16 digit slices in the K-major no-swizzle layout of the tcgen05
+// descriptors, then one int32 exponent per padded row; blocks padded to 16
+// bytes.  Returns the block size (out == NULL: size only).
 int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
                 unsigned char* out, int out_bytes);
+
+// Operator block of the mixed tcgen05 kernel (tcm::MPlan<N, EQ> in
+// dg_tcm.cuh): [A_0 A_1 A_2] (Np x 3 Np) and LIFT (Np x 4 Nfp) as TF32 pairs
+// (hi slice, lo slice) in the K-major no-swizzle layout, then the int32 face
+// node table.  Returns the block size (out == NULL: size only).
+int pack_tcm_ops(int order, const double* diff, const double* lift,
+                 const int32_t* face_nodes, unsigned char* out, int out_bytes);
 
 // Record `msg` as the calling thread's last error (dg_last_error) and
 // return `code`; shared by the translation units behind the C ABI.

@@ -1,6 +1,6 @@
 // RHS kernels for the euler equation: orders 1..4, FP64 and mixed
 // precision, plain RHS and fused RK stage; face-shared FP64 forms with FP64
-// or tensor-core contractions.
+// or tensor-core contractions; mixed precision on tcgen05.
 #include "rhs_instantiate.cuh"
 
 namespace dg {
@@ -24,5 +24,12 @@ cudaError_t tc_shape_euler(int order, int mode, LaunchShape* out) {
 cudaError_t tc_launch_euler(int order, int mode, const RhsArgs& a, int grid,
                         cudaStream_t s) {
   return tc_launch_any<DG_EULER>(order, mode, a, grid, s);
+}
+cudaError_t tcm_shape_euler(int order, int mode, LaunchShape* out) {
+  return tcm_shape_any<DG_EULER>(order, mode, out);
+}
+cudaError_t tcm_launch_euler(int order, int mode, const RhsArgs& a, int grid,
+                        cudaStream_t s) {
+  return tcm_launch_any<DG_EULER>(order, mode, a, grid, s);
 }
 }  // namespace dg

@@ -1,13 +1,15 @@
 // Instantiates the RHS kernel of one equation for orders 1..4, FP64 and
 // mixed precision, plain RHS and fused RK stage (FP64 also in the
-// face-shared split form, with its face kernel), and defines the equation's
-// shape/launch entry points.  Included by exactly one .cu file per equation.
+// face-shared split form, with its face kernel; mixed precision also with
+// the contractions on tcgen05), and defines the equation's shape/launch
+// entry points.  Included by exactly one .cu file per equation.
 #pragma once
 
 #include <type_traits>
 
 #include "dg_face.cuh"
 #include "dg_tc.cuh"
+#include "dg_tcm.cuh"
 #include "dg_launch.h"
 #include "dg_rhs.cuh"
 
@@ -187,6 +189,7 @@ cudaError_t tc_shape_impl(LaunchShape* out) {
   out->blocks_per_sm = nb;
   out->elems_per_tile = P::E;
   out->ops_bytes = P::OPS_BYTES;
+  out->threads = tc::kTcBlock;
   return err;
 }
 
@@ -224,6 +227,69 @@ cudaError_t tc_launch_any(int order, int mode, const RhsArgs& a, int grid,
   switch (order) {
     case 3: return tc_launch_n<3, EQ>(mode, a, grid, s);
     case 4: return tc_launch_n<4, EQ>(mode, a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// }}}
+
+
+// {{{ mixed precision with tcgen05 contractions (fused face fluxes)
+
+template <int N, int EQ, int MODE>
+cudaError_t tcm_shape_impl(LaunchShape* out) {
+  using P = tcm::MPlan<N, EQ>;
+  auto kern = dg_rhs_tcm_kernel<N, EQ, MODE>;
+  cudaError_t err = cudaFuncSetAttribute(
+      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
+  if (err != cudaSuccess) return err;
+  int nb = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, tcm::kThreads, P::SMEM_BYTES);
+  out->smem_bytes = P::SMEM_BYTES;
+  out->blocks_per_sm = nb;
+  out->elems_per_tile = P::E;
+  out->ops_bytes = P::OPS_BYTES;
+  out->threads = tcm::kThreads;
+  return err;
+}
+
+template <int N, int EQ>
+cudaError_t tcm_shape_n(int mode, LaunchShape* out) {
+  return mode == 0 ? tcm_shape_impl<N, EQ, MODE_RHS>(out)
+                   : tcm_shape_impl<N, EQ, MODE_STAGE>(out);
+}
+
+template <int N, int EQ>
+cudaError_t tcm_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
+  using P = tcm::MPlan<N, EQ>;
+  if (mode == 0)
+    dg_rhs_tcm_kernel<N, EQ, MODE_RHS><<<grid, tcm::kThreads, P::SMEM_BYTES, s>>>(a);
+  else
+    dg_rhs_tcm_kernel<N, EQ, MODE_STAGE><<<grid, tcm::kThreads, P::SMEM_BYTES, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int EQ>
+cudaError_t tcm_shape_any(int order, int mode, LaunchShape* out) {
+  if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
+  switch (order) {
+    case 1: return tcm_shape_n<1, EQ>(mode, out);
+    case 2: return tcm_shape_n<2, EQ>(mode, out);
+    case 3: return tcm_shape_n<3, EQ>(mode, out);
+    case 4: return tcm_shape_n<4, EQ>(mode, out);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int EQ>
+cudaError_t tcm_launch_any(int order, int mode, const RhsArgs& a, int grid,
+                           cudaStream_t s) {
+  if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
+  switch (order) {
+    case 1: return tcm_launch_n<1, EQ>(mode, a, grid, s);
+    case 2: return tcm_launch_n<2, EQ>(mode, a, grid, s);
+    case 3: return tcm_launch_n<3, EQ>(mode, a, grid, s);
+    case 4: return tcm_launch_n<4, EQ>(mode, a, grid, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -228,7 +228,7 @@ class DevicePlan:
 
     #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per tile
     VARIANTS = {0: "persistent", 1: "tensor-core, persistent", 2: "one CTA per tile",
-                3: "tensor-core, one CTA per tile"}
+                3: "tensor-core, one CTA per tile", 4: "tcgen05, persistent"}
 
     def set_variant(self, variant: int) -> None:
         _lib.check(self._lib.dg_plan_set_variant(self._handle, int(variant)))
@@ -239,13 +239,13 @@ class DevicePlan:
         self._check_tensor(q, "state")
         out = torch.empty_like(q)
         chosen = ctypes.c_int32()
-        ms = (ctypes.c_float * 4)()
+        ms = (ctypes.c_float * 5)()
         _lib.check(self._lib.dg_plan_autotune(
             self._handle, ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(out.data_ptr()),
             int(reps), _stream_handle(stream), ctypes.byref(chosen), ms))
         return {"chosen": chosen.value,
                 "ms": {self.VARIANTS[v]: (float(ms[v]) if ms[v] >= 0 else None)
-                       for v in range(4)}}
+                       for v in range(5)}}
 
     def vjp(self, q: torch.Tensor, x: torch.Tensor, out: torch.Tensor | None = None,
             stream=None) -> torch.Tensor:

@@ -296,6 +296,7 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step) -> dict:
             "cases_ms": {f"{r['eq']}{r['order']}": t for r, t in zip(runs, times)},
             "autotuned_variant": {f"{r['eq']}{r['order']}": p.VARIANTS[tu["chosen"]]
                                   for r, p, tu in zip(runs, plans, tuned)},
+            "variant_ms": {f"{r['eq']}{r['order']}": tu["ms"] for r, tu in zip(runs, tuned)},
         }
         del outs
     except Exception as exc:  # report, keep the main line

@@ -208,14 +208,18 @@ int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 
 /* Launch variant of the plan's main kernel: bit 0 = contractions on the
  * tensor cores (DG_FP32_MIXED plans: 3xTF32 split with FP32 accumulation,
- * i.e. FP32 accuracy), bit 1 = one CTA per tile instead of the persistent
- * grid.  Default 0.  No counterpart in the reference. */
+ * i.e. FP32 accuracy, as warp-level mma.sync), bit 1 = one CTA per tile
+ * instead of the persistent grid; 4 = the DG_FP32_MIXED kernel with its
+ * volume and LIFT contractions as one tcgen05 product per tile (3xTF32,
+ * FP32 accumulators in tensor memory; persistent grid, one CTA per SM).
+ * Default 0.  No counterpart in the reference. */
 int dg_plan_set_variant(dg_plan* plan, int32_t variant);
 
 /* Time every variant the plan supports (after one warm-up launch, `reps`
  * launches of dg_rhs(q -> rhs) each, CUDA events on `stream`), keep the
  * fastest and report it in *chosen (may be NULL); ms_per_variant (may be
- * NULL) receives 4 floats, -1 for variants the plan does not support.
+ * NULL) receives 5 floats (variants 0..4), -1 for variants the plan does
+ * not support.
  * Writes rhs.  The autotuner of the batched (ensemble) path: the reference
  * fixes its loop-nest tiling in its loopy transforms instead
  * (actx_dgfem_suite/arraycontext/batched_einsum_loop_transforms.py:142). */
@@ -228,7 +232,8 @@ int dg_plan_destroy(dg_plan* plan);
 
 /* Which path the plan takes: face_shared 1 for the face-shared path, 0 for
  * the single fused launch; tensor_cores 1 when the contractions run on the
- * tensor cores (DG_FP64_TC on the face-shared path); launches_per_rhs = kernel launches of one dg_rhs
+ * tensor cores (DG_FP64_TC on the face-shared path, or a DG_FP32_MIXED plan
+ * under variant 1, 3 or 4); launches_per_rhs = kernel launches of one dg_rhs
  * or dg_rk_stage; owned_faces = faces whose flux the face kernel evaluates.
  * Any output pointer may be NULL. */
 int dg_plan_path(const dg_plan* plan, int32_t* face_shared, int32_t* tensor_cores,

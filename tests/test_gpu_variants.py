@@ -1,6 +1,7 @@
 """Launch variants and the autotuner: the mixed-precision kernel with its
-contractions on the tensor cores (3xTF32, FP32 accumulation) keeps the
-mixed path's accuracy; the one-CTA-per-tile grid gives identical results."""
+contractions on the tensor cores (3xTF32, FP32 accumulation; warp-level
+mma.sync or one tcgen05 product per tile) keeps the mixed path's accuracy;
+the one-CTA-per-tile grid gives identical results."""
 
 from __future__ import annotations
 
@@ -63,7 +64,7 @@ def test_autotune_picks_a_supported_variant():
     prob, ref, mixed = _plans("maxwell", 3)
     q = torch.from_numpy(prob.fields).cuda()
     res = mixed.autotune(q, reps=2)
-    assert res["chosen"] in (0, 1, 2, 3)
+    assert res["chosen"] in (0, 1, 2, 3, 4)
     assert all(v is not None and v > 0 for v in res["ms"].values())
     res64 = ref.autotune(q, reps=2)
     assert res64["chosen"] in (0, 2)
@@ -71,3 +72,63 @@ def test_autotune_picks_a_supported_variant():
     from actx_dgfem_suite_gb300._lib import DGError
     with pytest.raises(DGError):
         ref.set_variant(1)
+
+
+@pytest.mark.parametrize("equation", ["wave", "euler", "maxwell"])
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_tcgen05_mixed_matches_fp64(equation, order):
+    """Variant 4: [A_0 A_1 A_2 | LIFT] applied to the metric-combined inputs
+    and face values as one tcgen05 product per tile (partial last tile)."""
+    prob, ref, mixed = _plans(equation, order, seed=20 + order)
+    q = torch.from_numpy(prob.fields).cuda()
+    r64 = ref.rhs(q)
+    mixed.set_variant(0)
+    r0 = mixed.rhs(q)
+    mixed.set_variant(4)
+    assert mixed.info()["tensor_cores"]
+    r4 = mixed.rhs(q)
+    mixed.finish()
+    n64 = float(torch.linalg.norm(r64))
+    assert float(torch.linalg.norm(r4 - r64)) <= MIXED_RTOL * n64
+    assert float(torch.linalg.norm(r4 - r0)) <= MIXED_RTOL * n64
+
+
+@pytest.mark.parametrize("equation,order", [("maxwell", 3), ("euler", 2), ("wave", 4)])
+def test_tcgen05_mixed_many_tiles_per_cta(equation, order):
+    """More tiles than CTAs: every CTA runs the persistent loop several times."""
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem(equation, jittered_box_mesh(12), order, seed=3)
+    dm = DeviceMesh(prob.disc, "cuda:0")
+    ref = DevicePlan(dm, equation, prob.params, "fp64")
+    mixed = DevicePlan(dm, equation, prob.params, "fp32-mixed")
+    mixed.set_variant(4)
+    assert prob.disc.nelements > 2 * mixed.info()["grid"] * 21
+    q = torch.from_numpy(prob.fields).cuda()
+    r64 = ref.rhs(q)
+    r4 = mixed.rhs(q)
+    mixed.finish()
+    n64 = float(torch.linalg.norm(r64))
+    assert float(torch.linalg.norm(r4 - r64)) <= MIXED_RTOL * n64
+
+
+def test_tcgen05_mixed_rk_stage_and_element_scale():
+    prob, ref, mixed = _plans("wave", 3, seed=5)
+    q = torch.from_numpy(prob.fields).cuda()
+    nel = prob.disc.nelements
+    scale = torch.linspace(0.8, 1.2, nel, dtype=torch.float64, device="cuda:0")
+    res0 = torch.rand(q.shape, dtype=q.dtype, device=q.device,
+                      generator=torch.Generator(device=q.device).manual_seed(7))
+    outs = []
+    for plan, variant in ((ref, 0), (mixed, 4)):
+        plan.set_variant(variant)
+        plan.set_element_scale(scale)
+        res = res0.clone()
+        qo = torch.empty_like(q)
+        unscaled = torch.empty_like(q)
+        plan.rk_stage(q, qo, res, 0.3, 0.5, 1e-3, rhs_unscaled=unscaled)
+        plan.finish()
+        outs.append((qo, res, unscaled))
+    for k in range(3):
+        ref_k = outs[0][k]
+        assert float(torch.linalg.norm(outs[1][k] - ref_k)) <= \
+            MIXED_RTOL * float(torch.linalg.norm(ref_k))
