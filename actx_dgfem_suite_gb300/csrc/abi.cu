@@ -451,42 +451,48 @@ int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
   return total;
 }
 
-// TF32 (round to nearest, ties away from zero) of a float, as a float
-static float tf32_host(float x) {
-  uint32_t b;
-  std::memcpy(&b, &x, 4);
-  b = (b + 0x1000u) & 0xffffe000u;
-  float r;
-  std::memcpy(&r, &b, 4);
-  return r;
-}
-
+// Operator block of the mixed tcgen05 kernel: B_V = [A_0 A_1 A_2] and
+// B_L = LIFT as four FP16 digit slices each (layout: tcm::MPlan).
 int pack_tcm_ops(int order, const double* diff, const double* lift,
                  const int32_t* face_nodes, unsigned char* out, int out_bytes) {
   const int np = (order + 1) * (order + 2) * (order + 3) / 6;
   const int nfpt = 2 * (order + 1) * (order + 2);
-  const int nb = (np + 15) & ~15, kv = (3 * np + 7) & ~7, kl = (nfpt + 7) & ~7;
-  const int sbo_v = (kv / 4) * 128, sbo_l = (kl / 4) * 128;
+  const int nb = (np + 15) & ~15, kv = (3 * np + 15) & ~15, kl = (nfpt + 15) & ~15;
+  const int sbo_v = (kv / 8) * 128, sbo_l = (kl / 8) * 128;
   const int bs_v = (nb / 8) * sbo_v, bs_l = (nb / 8) * sbo_l;
-  const int ops_l = 2 * bs_v, ops_fn = ops_l + 2 * bs_l;
+  const int ops_l = 4 * bs_v, ops_ev = ops_l + 4 * bs_l, ops_el = ops_ev + nb * 4;
+  const int ops_fn = ops_el + nb * 4;
   const int total = ops_fn + ((nfpt * 4 + 15) & ~15);
   if (!out) return total;
   if (out_bytes != total) return -1;
-  std::memset(out, 0, total);
-  auto put = [&](int base, int slice, int sbo, int n, int k, double x) {
-    const int off = base + (n / 8) * sbo + (k / 4) * 128 + (n % 8) * 16 + (k % 4) * 4;
-    const float hi = tf32_host((float)x);
-    const float lo = tf32_host((float)(x - (double)hi));
-    std::memcpy(out + off, &hi, 4);
-    std::memcpy(out + off + slice, &lo, 4);
+  std::memset(out, 0, total);  // FP16 zero digits
+  // one block: rows i < np of at(i, k), k < kk, scaled per row to 31-bit
+  // integers (|x| <= 2^31) in four balanced base-256 digits, most significant
+  // first; row scales 2^e (FP32) with |at(i, k)| < 2^e
+  auto block = [&](int base, int slice, int sbo, int kk, int exp_off, auto at) {
+    float* rscale = reinterpret_cast<float*>(out + exp_off);
+    for (int i = 0; i < np; ++i) {
+      double mx = 0.0;
+      for (int k = 0; k < kk; ++k) mx = std::fmax(mx, std::fabs(at(i, k)));
+      int e = 0;
+      if (mx > 0.0) std::frexp(mx, &e);
+      rscale[i] = std::ldexp(1.0f, e);
+      for (int k = 0; k < kk; ++k) {
+        long long x = std::llrint(std::ldexp(at(i, k), 31 - e));
+        const int off = base + (i / 8) * sbo + (k / 8) * 128 + (i % 8) * 16 + (k % 8) * 2;
+        for (int d = 3; d >= 0; --d) {  // least significant digit first
+          const long long dig = d == 0 ? x : ((x + 128) & 255) - 128;
+          x = (x - dig) >> 8;
+          const uint16_t h = half_bits(static_cast<int>(dig));
+          std::memcpy(out + off + d * slice, &h, 2);
+        }
+      }
+    }
   };
-  for (int i = 0; i < np; ++i)
-    for (int r = 0; r < 3; ++r)
-      for (int j = 0; j < np; ++j)
-        put(0, bs_v, sbo_v, i, r * np + j, diff[((size_t)r * np + i) * np + j]);
-  for (int i = 0; i < np; ++i)
-    for (int fj = 0; fj < nfpt; ++fj)
-      put(ops_l, bs_l, sbo_l, i, fj, lift[(size_t)i * nfpt + fj]);
+  block(0, bs_v, sbo_v, 3 * np, ops_ev,
+        [&](int i, int k) { const int r = k / np; return diff[((size_t)r * np + i) * np + k - r * np]; });
+  block(ops_l, bs_l, sbo_l, nfpt, ops_el,
+        [&](int i, int k) { return lift[(size_t)i * nfpt + k]; });
   std::memcpy(out + ops_fn, face_nodes, (size_t)nfpt * 4);
   return total;
 }

@@ -85,9 +85,10 @@ int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
                 unsigned char* out, int out_bytes);
 
 // Operator block of the mixed tcgen05 kernel (tcm::MPlan<N, EQ> in
-// dg_tcm.cuh): [A_0 A_1 A_2] (Np x 3 Np) and LIFT (Np x 4 Nfp) as TF32 pairs
-// (hi slice, lo slice) in the K-major no-swizzle layout, then the int32 face
-// node table.  Returns the block size (out == NULL: size only).
+// dg_tcm.cuh): [A_0 A_1 A_2] (Np x 3 Np) and LIFT (Np x 4 Nfp), each row
+// scaled to 31-bit integers written as four FP16 digit slices in the K-major
+// no-swizzle layout, then the FP32 row scales 2^e of each, then the int32
+// face node table.  Returns the block size (out == NULL: size only).
 int pack_tcm_ops(int order, const double* diff, const double* lift,
                  const int32_t* face_nodes, unsigned char* out, int out_bytes);
 

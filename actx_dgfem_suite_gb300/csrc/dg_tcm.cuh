@@ -1,135 +1,220 @@
 // Mixed-precision RHS with the contractions on the tcgen05 tensor cores.
 //
 // The volume derivatives and LIFT of the mixed-precision path (FP32
-// arithmetic, FP64 state) as one product per tile, with the roles of data and
-// operator chosen for the tensor core's 128-row shape:
+// arithmetic, FP64 state) as tensor-core products per tile, with the roles
+// of data and operator chosen for the tensor core's 128-row shape:
 //
-//   D (128 x Np) = X (128 x K) B^T,   K = 3 Np + 4 Nfp (two phases)
+//   D (128 x Np) = X_V (128 x 3 Np) B_V^T + X_L (128 x 4 Nfp) B_L^T
 //
 // Each of the 128 rows of X is one (field c, element e) column of the tile's
-// data: the metric-combined inputs w_{c,r}(j) of the three reference
-// derivatives (r = 0, 1, 2; nodes j), then the field's lifted face values:
+// data.  X_V holds the metric-combined inputs w_{c,r}(j) of the three
+// reference derivatives (r = 0, 1, 2; nodes j), X_L the field's lifted face
+// values:
 //   wave    w_{0,r} = -c (G v)_r,  w_{1+x,r} = -c G_{r x} u;
 //   euler   w_{k,r} = sum_x G_{r x} F_{k x}(q);
 //   maxwell w_{c,r} from E_t = curl H, H_t = -curl E, e.g.
 //           w_{0,r} = G_{r 1} H_z - G_{r 2} H_y;
-// B is the operator [A_0 A_1 A_2 | LIFT] (Np rows; A_r the reference
-// derivative the equation uses).  So D holds vol + lift of every output node
-// directly: no per-node combination after the product.  X and B are split
-// into TF32 pairs x = x_hi + x_lo (cvt.rna) and multiplied as
-// x_hi b_hi + x_hi b_lo + x_lo b_hi with FP32 accumulation in tensor memory
-// (tcgen05.mma kind::tf32, M = 128, N = Np padded to 16, K = 8 per
-// instruction): FP32 accuracy, the error of the CUDA-core FP32 path.
+// B_V = [A_0 A_1 A_2] (A_r the reference derivative the equation uses) and
+// B_L = LIFT, Np rows each.  D holds vol + lift of every output node
+// directly: no per-node combination after the products.
 //
-// Per tile of E = 128 / NF elements:
-//   1. per node (8 elements x 4 nodes per warp, so the 4-byte stores into the
-//      K-major operand layout are free of bank conflicts): the FP64 state ->
-//      FP32 copy in shared memory, the metric-combined inputs (Euler: the
-//      pressure from total energy in FP64) -> X (volume phase);
-//   2. one thread issues the volume products (asynchronous, completion on an
+// Exact accumulation.  Every row of X and of B is scaled by a power of two
+// to 31-bit integers and written as four balanced base-256 digits
+// (|d| <= 128, exact in FP16): x = 2^(E - 31) sum_i d_i 2^(24 - 8 i).  The ten
+// digit-pair products with i + j <= 3 run as tcgen05.mma kind::f16 (M = 128,
+// N = Np padded to 16, K = 16) into one FP32 tensor-memory accumulator per
+// level l = i + j and phase; each level sum is an integer below 2^23, so the
+// tensor core adds it exactly whatever its internal rounding.  The fold
+// recombines L_0 + 2^-8 L_1 + 2^-16 L_2 + 2^-24 L_3 with three
+// round-to-nearest FP32 operations.  Row scaling with 31 bits keeps the
+// entries of a row that are up to 2^7 below its maximum at FP32's 24-bit
+// resolution (P4 operator rows span a factor 4-7 in rms), and the dropped
+// pairs weigh 2^-32: the result carries the error of FP32 arithmetic,
+// unbiased, where TF32 products accumulated by the tensor core lose accuracy
+// with every accumulation step.
+//
+// Per tile of E = 128 / NF elements (8 elements x 4 nodes or face points per
+// warp, so the digit stores into the K-major operand layout are free of bank
+// conflicts):
+//   1. per node: the FP64 state -> FP32 copy, metric, (Euler: pressure from
+//      total energy in FP64, 1/rho), the inputs w -> row maxima (shuffles +
+//      shared atomics);
+//   2. per node again: w -> digits of X_V;
+//   3. one thread issues the volume products (asynchronous, completion on an
 //      mbarrier); meanwhile every thread evaluates the numerical flux of its
-//      face points into registers;
-//   3. after the volume products have read X, the face values are written
-//      into X (LIFT phase) and the LIFT products accumulate into the same D;
-//   4. tcgen05.ld of D -> shared staging, then coalesced FP64 stores (RHS) or
-//      the fused low-storage RK stage.
+//      face points into registers and their row maxima; after the volume
+//      products have read X, the digits of X_L replace it and the LIFT
+//      products run;
+//   4. tcgen05.ld of the eight level sums -> FP32 staging, then coalesced FP64
+//      stores (RHS) or the fused low-storage RK stage.
 // Waits on the mbarriers are bounded (DG_ERR_TIMEOUT instead of spinning).
 //
 // Flux formulas as in dg_rhs.cuh (wave.py:80-114, grudge's Euler LF flux
 // with InviscidWallBC, MaxwellOperator alpha-flux with PEC).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "dg_tc.cuh"
 
 namespace dg {
 namespace tcm {
 
-constexpr int kThreads = 512;  // one CTA per SM
-
-constexpr int r8(int x) { return (x + 7) & ~7; }
 constexpr int r16(int x) { return (x + 15) & ~15; }
 constexpr int p16(int b) { return (b + 15) & ~15; }
-// row pitch (words) >= n with pitch % 32 == 4: 8 elements x 4 nodes of a warp
+// row pitch (words) >= n with pitch % 8 == 4: 8 elements x 4 nodes of a warp
 // hit 32 distinct banks
-constexpr int pitch_q(int n) { return n <= 4 ? 4 : ((n - 4 + 31) / 32) * 32 + 4; }
+constexpr int pitch_q(int n) { return ((n + 3) / 8) * 8 + 4; }
+constexpr int pow2_cols(int c) {
+  return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
+}
 
 template <int N, int EQ>
 struct MPlan {
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
   static constexpr int NF = EqInfo<EQ>::NF;
+  static constexpr int THREADS = N == 1 ? 128 : (N == 4 ? 512 : 256);
+  static constexpr int MIN_BLOCKS = N == 4 ? 1 : 2;
   static constexpr int E = 128 / NF;      // elements per tile
   static constexpr int NCOL = NF * E;     // rows of X in use (m = c E + e)
   static constexpr int NB = r16(NP);      // operator rows (MMA N)
-  static constexpr int KV = r8(3 * NP), KL = r8(NFPT);
-  // K-major, no swizzle: element (m, k) of a slice at
-  //   (m / 8) SBO + (k / 4) 128 + (m % 8) 16 + (k % 4) 4 bytes
-  static constexpr int SBO_V = (KV / 4) * 128, SBO_L = (KL / 4) * 128;
+  static constexpr int KV = r16(3 * NP), KL = r16(NFPT);
+  // K-major, no swizzle: element (m, k) of a digit slice at
+  //   (m / 8) SBO + (k / 8) 128 + (m % 8) 16 + (k % 8) 2 bytes
+  static constexpr int SBO_V = (KV / 8) * 128, SBO_L = (KL / 8) * 128;
   static constexpr int A_SLICE_V = 16 * SBO_V, A_SLICE_L = 16 * SBO_L;
-  static constexpr int A_BYTES = 2 * (A_SLICE_V > A_SLICE_L ? A_SLICE_V : A_SLICE_L);
-  // operator block (global and shared): vol hi | vol lo | lift hi | lift lo |
-  // int32 face nodes
+  static constexpr int NDIG = 4;  // digits per value
+  static constexpr int A_BYTES = NDIG * (A_SLICE_V > A_SLICE_L ? A_SLICE_V : A_SLICE_L);
+  // operator block (global and shared): B_V digits (4 slices) | B_L digits |
+  // FP32 row scales 2^e of B_V | of B_L (|B_ik| < 2^e) | int32 face nodes
   static constexpr int B_SLICE_V = (NB / 8) * SBO_V, B_SLICE_L = (NB / 8) * SBO_L;
-  static constexpr int OPS_V = 0, OPS_L = 2 * B_SLICE_V, OPS_FN = OPS_L + 2 * B_SLICE_L;
+  static constexpr int OPS_V = 0, OPS_L = NDIG * B_SLICE_V;
+  static constexpr int OPS_EV = OPS_L + NDIG * B_SLICE_L, OPS_EL = OPS_EV + NB * 4;
+  static constexpr int OPS_FN = OPS_EL + NB * 4;
   static constexpr int OPS_BYTES = OPS_FN + p16(NFPT * 4);
   static constexpr int QP = pitch_q(NP);  // FP32 state rows
   static constexpr int OP = NP | 1;       // FP32 result rows (odd pitch)
   static constexpr int SM_A = 0;
   static constexpr int SM_OPS = SM_A + A_BYTES;
   static constexpr int SM_Q = SM_OPS + OPS_BYTES;
-  static constexpr int SM_OUT = SM_Q + p16(NF * E * QP * 4);
-  static constexpr int SM_P = SM_OUT + p16(NCOL * OP * 4);
-  static constexpr int SMEM_BYTES = SM_P + (EQ == DG_EULER ? p16(E * NP * 8) : 0);
-  static constexpr int TMEM_COLS = NB <= 32 ? 32 : (NB <= 64 ? 64 : 128);
-  // instruction descriptor: D FP32, A and B TF32, both K-major, N, M = 128
-  static constexpr uint32_t IDESC =
-      (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NB >> 3) << 17) | (8u << 24);
+  static constexpr int SM_G = SM_Q + p16(NF * E * QP * 4);
+  static constexpr int SM_OUT = SM_G + p16(9 * E * 4);
+  static constexpr int SM_RMAX = SM_OUT + p16(NCOL * OP * 4);  // [2 tiles][2 phases][128]
+  static constexpr int SM_P = SM_RMAX + 4 * 128 * 4;
+  static constexpr int SM_R = SM_P + (EQ == DG_EULER ? p16(E * NP * 8) : 0);
+  static constexpr int SMEM_BYTES = SM_R + (EQ == DG_EULER ? p16(E * NP * 4) : 0);
+  // accumulators: levels 0..3 of the volume phase, then of the LIFT phase
+  static constexpr int ACC_L = 4 * NB;
+  static constexpr int TMEM_COLS = pow2_cols(8 * NB);
+  // instruction descriptor: D FP32, A and B FP16, both K-major, N, M = 128
+  static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(NB >> 3) << 17) | (8u << 24);
   static_assert(NCOL <= 128, "one 128-row product per tile");
   static_assert(NB >= 16 && NB <= 256, "MMA N range");
+  static_assert(KV <= 128 && KL <= 128, "level sums (4 pairs) below 2^23 need K <= 128");
+  static_assert(TMEM_COLS <= 512, "accumulators fit in tensor memory");
   static_assert(SMEM_BYTES <= 227 * 1024, "tile does not fit in shared memory");
 };
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
-      ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
+// FP32 copies of the equation constants, converted once per CTA (on the
+// integer ALU: conversions that touch FP64 issue at GB300's FP64 rate)
+struct FluxConsts {
+  float p0;      // wave speed c / gamma / maxwell alpha
+  float z, y;    // maxwell impedance and admittance
+  float ce, ch;  // maxwell flux factors -1/(2z), 1/(2y)
+  float ie, im;  // maxwell 1/eps, 1/mu
+};
 
-// x -> (hi, lo) TF32 pair stored at byte offset `off` of both slices
-__device__ __forceinline__ void put_split(unsigned char* base, int slice_bytes, int off,
-                                          float x) {
-  uint32_t hi, lo;
-  tf32_split(x, hi, lo);
-  *reinterpret_cast<uint32_t*>(base + off) = hi;
-  *reinterpret_cast<uint32_t*>(base + slice_bytes + off) = lo;
+__device__ __forceinline__ FluxConsts flux_consts(const RhsArgs& a) {
+  FluxConsts f;
+  f.p0 = d2f_alu(a.p0);
+  f.z = d2f_alu(a.k[0]);
+  f.y = d2f_alu(a.k[1]);
+  f.ce = d2f_alu(a.k[2]);
+  f.ch = d2f_alu(a.k[3]);
+  f.ie = d2f_alu(a.k[4]);
+  f.im = d2f_alu(a.k[5]);
+  return f;
 }
 
 __device__ __forceinline__ int kmajor_off(int m, int k, int sbo) {
-  return (m >> 3) * sbo + (k >> 2) * 128 + (m & 7) * 16 + (k & 3) * 4;
+  return (m >> 3) * sbo + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2;
 }
 
-// One K phase: per k-step of 8, x_hi b_hi, x_hi b_lo, x_lo b_hi into D.
-template <int K, int SBO, int A_SLICE, int B_SLICE>
-__device__ __forceinline__ void issue_phase(uint32_t a_s, uint32_t b_s, uint32_t tmem,
-                                            uint32_t idesc, bool first) {
+// 2^s as a float for s in [-126, 127]
+__device__ __forceinline__ float pow2f(int s) {
+  s = s < -126 ? -126 : (s > 127 ? 127 : s);
+  return __uint_as_float((uint32_t)(s + 127) << 23);
+}
+
+// biased exponent of a row maximum (float bits of |x|), clamped so that the
+// scale 2^(157 - e) stays a normal float: |x| < 2^(e - 126)
+__device__ __forceinline__ int row_exp_bits(uint32_t maxbits) {
+  const int e = (int)(maxbits >> 23);
+  return e < 30 ? 30 : e;
+}
+
+// x (|x| < 2^(e - 126)) -> four FP16 digits of v = round(x 2^(157 - e)),
+// |v| <= 2^31, at byte offset `off` of the four slices.  FP32 arithmetic is
+// exact here: v has at most 24 significant bits, and every remainder is a
+// multiple of ulp(v) below 2^24 ulp(v).
+__device__ __forceinline__ void put_digits(unsigned char* base, int slice, int off, float x,
+                                           int e) {
+  const float v = rintf(x * __uint_as_float((uint32_t)(284 - e) << 23));
+  const float d0 = rintf(v * 0x1p-24f);
+  const float r1 = fmaf(-d0, 0x1p24f, v);
+  const float d1 = rintf(r1 * 0x1p-16f);
+  const float r2 = fmaf(-d1, 65536.f, r1);
+  const float d2 = rintf(r2 * 0x1p-8f);
+  const float d3 = fmaf(-d2, 256.f, r2);
+  const __half2 h01 = __floats2half2_rn(d0, d1), h23 = __floats2half2_rn(d2, d3);
+  *reinterpret_cast<__half*>(base + off) = __low2half(h01);
+  *reinterpret_cast<__half*>(base + slice + off) = __high2half(h01);
+  *reinterpret_cast<__half*>(base + 2 * slice + off) = __low2half(h23);
+  *reinterpret_cast<__half*>(base + 3 * slice + off) = __high2half(h23);
+}
+
+// max over the four lanes of a warp that share lane & 7 (elements), then one
+// shared atomic per element row
+__device__ __forceinline__ void row_max(unsigned* rmax, int m, float a, bool lead) {
+  a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, 8));
+  a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, 16));
+  if (lead) atomicMax(rmax + m, __float_as_uint(a));
+}
+
+// One phase: per k-step of 16 the ten digit pairs (i, j), i + j <= 3, into the
+// level accumulators acc + (i + j) NB.
+template <int K, int SBO, int A_SLICE, int B_SLICE, int NB>
+__device__ __forceinline__ void issue_phase(uint32_t a_s, uint32_t b_s, uint32_t acc,
+                                            uint32_t idesc) {
   tc::tc_fence_after();
 #pragma unroll 1
-  for (int kt = 0; kt < K / 8; ++kt) {
-    const uint32_t ka = a_s + kt * 256, kb = b_s + kt * 256;
-    const uint64_t ah = tc::smem_desc(ka, 128, SBO), al = tc::smem_desc(ka + A_SLICE, 128, SBO);
-    const uint64_t bh = tc::smem_desc(kb, 128, SBO), bl = tc::smem_desc(kb + B_SLICE, 128, SBO);
-    mma_tf32(tmem, al, bh, idesc, (first && kt == 0) ? 0u : 1u);
-    mma_tf32(tmem, ah, bl, idesc, 1u);
-    mma_tf32(tmem, ah, bh, idesc, 1u);
+  for (int kt = 0; kt < K / 16; ++kt) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4 - i; ++j) {
+        const uint64_t da = tc::smem_desc(a_s + i * A_SLICE + kt * 256, 128, SBO);
+        const uint64_t db = tc::smem_desc(b_s + j * B_SLICE + kt * 256, 128, SBO);
+        // the first product of each level (kt = 0, i = 0) starts it
+        tc::tc_mma(acc + (uint32_t)((i + j) * NB), da, db, idesc,
+                   (kt == 0 && i == 0) ? 0u : 1u);
+      }
   }
+}
+
+// L_0 + 2^-8 L_1 + 2^-16 L_2 + 2^-24 L_3 (exact integer level sums), three
+// roundings, smallest terms first
+__device__ __forceinline__ float levels4(const uint32_t* l, int jj) {
+  const float t2 = fmaf(__uint_as_float(l[24 + jj]), 0x1p-8f, __uint_as_float(l[16 + jj]));
+  const float t1 = fmaf(t2, 0x1p-8f, __uint_as_float(l[8 + jj]));
+  return fmaf(t1, 0x1p-8f, __uint_as_float(l[jj]));
 }
 
 // Numerical flux of one face point in FP32 (FP64 exterior state, FP64
 // Euler pressures); out[c] = the lifted face value of field c.
 template <int EQ, int NF>
-__device__ __forceinline__ void face_point_flux(const RhsArgs& a, const float* qi,
+__device__ __forceinline__ void face_point_flux(const RhsArgs& a, const FluxConsts& fc,
+                                                const float* qi,
                                                 const double* qed, bool bdry, float nx,
                                                 float ny, float nz, float scale,
                                                 double pi_d, float* out) {
@@ -145,7 +230,7 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const float* q
       qe[2] = qi[2];
       qe[3] = qi[3];
     }
-    const float c = (float)a.p0;
+    const float c = fc.p0;
     const float vavg_n = 0.5f * (qi[1] + qe[1]) * nx + 0.5f * (qi[2] + qe[2]) * ny +
                          0.5f * (qi[3] + qe[3]) * nz;
     const float uavg = 0.5f * (qi[0] + qe[0]);
@@ -157,7 +242,7 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const float* q
     out[2] = scale * (fv * ny);
     out[3] = scale * (fv * nz);
   } else if constexpr (EQ == DG_EULER) {
-    const float gamma = (float)a.p0;
+    const float gamma = fc.p0;
     double pe_d;
     if (bdry) {
       pe_d = pi_d;  // the wall mirror keeps rho, |m| and E
@@ -203,8 +288,8 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const float* q
       qe[4] = qi[4];
       qe[5] = qi[5];
     }
-    const float alpha = (float)a.p0;
-    const float z = (float)a.k[0], y = (float)a.k[1];
+    const float alpha = fc.p0;
+    const float z = fc.z, y = fc.y;
     const float je[3] = {qe[0] - qi[0], qe[1] - qi[1], qe[2] - qi[2]};
     const float jh[3] = {qe[3] - qi[3], qe[4] - qi[4], qe[5] - qi[5]};
     const float n[3] = {nx, ny, nz};
@@ -223,7 +308,7 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const float* q
     }
     cross(n, te, fe);
     cross(n, th, fh);
-    const float ce = (float)a.k[2], ch = (float)a.k[3];
+    const float ce = fc.ce, ch = fc.ch;
 #pragma unroll
     for (int x = 0; x < 3; ++x) {
       out[x] = -scale * (ce * fe[x]);
@@ -235,12 +320,13 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const float* q
 }  // namespace tcm
 
 template <int N, int EQ, int MODE>
-__global__ void __launch_bounds__(tcm::kThreads, 1) dg_rhs_tcm_kernel(const RhsArgs a) {
+__global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>::MIN_BLOCKS)
+    dg_rhs_tcm_kernel(const RhsArgs a) {
   using P = tcm::MPlan<N, EQ>;
   constexpr int NP = P::NP, NFP = P::NFP, NFPT = P::NFPT, NF = P::NF, E = P::E;
-  constexpr int QP = P::QP, OP = P::OP;
+  constexpr int QP = P::QP, OP = P::OP, NB = P::NB, THREADS = P::THREADS;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
-  constexpr int NWARP = tcm::kThreads / 32;
+  constexpr int NWARP = THREADS / 32;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar;
   __shared__ uint64_t mma_bar;
@@ -250,9 +336,15 @@ __global__ void __launch_bounds__(tcm::kThreads, 1) dg_rhs_tcm_kernel(const RhsA
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   unsigned char* sA = smem + P::SM_A;
   const int* sFN = reinterpret_cast<const int*>(smem + P::SM_OPS + P::OPS_FN);
+  const float* sEV = reinterpret_cast<const float*>(smem + P::SM_OPS + P::OPS_EV);
+  const float* sEL = reinterpret_cast<const float*>(smem + P::SM_OPS + P::OPS_EL);
   float* sq = reinterpret_cast<float*>(smem + P::SM_Q);
+  float* sG = reinterpret_cast<float*>(smem + P::SM_G);
   float* sOut = reinterpret_cast<float*>(smem + P::SM_OUT);
+  unsigned* sRmax = reinterpret_cast<unsigned*>(smem + P::SM_RMAX);
   double* sP = reinterpret_cast<double*>(smem + P::SM_P);
+  float* sR = reinterpret_cast<float*>(smem + P::SM_R);
+  const tcm::FluxConsts fc = tcm::flux_consts(a);
   if (t == 0) {
     mbar_init(&bar, 1);
     mbar_init(&mma_bar, 1);
@@ -265,10 +357,11 @@ __global__ void __launch_bounds__(tcm::kThreads, 1) dg_rhs_tcm_kernel(const RhsA
     }
     ops_ok = ok ? 1 : 0;
   }
-  // the data operand's padding (k past 3 Np or 4 Nfp) meets zero operator
-  // columns; it must hold finite values, so clear the region once
-  for (int idx = t; idx < P::A_BYTES / 16; idx += tcm::kThreads)
+  // digit padding (k past 3 Np or 4 Nfp, rows past NF E) meets zero operator
+  // columns or unused rows; it must hold finite values, so clear X once
+  for (int idx = t; idx < P::A_BYTES / 16; idx += THREADS)
     reinterpret_cast<uint4*>(sA)[idx] = make_uint4(0u, 0u, 0u, 0u);
+  for (int idx = t; idx < 4 * 128; idx += THREADS) sRmax[idx] = 0u;
   __syncthreads();
   if (!ops_ok) return;
   if (warp == 0) {
@@ -297,166 +390,236 @@ __global__ void __launch_bounds__(tcm::kThreads, 1) dg_rhs_tcm_kernel(const RhsA
     tc::tc_fence_after();
   };
 
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  // metric-combined volume inputs of node j of element e from FP32 values
+  auto vol_inputs = [&](const float* qf, const float* G, float p, float rinv, float (*w)[3]) {
+    if constexpr (EQ == DG_WAVE) {
+      const float c = fc.p0;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        w[0][r] = -c * fmaf(G[r * 3 + 0], qf[1], fmaf(G[r * 3 + 1], qf[2], G[r * 3 + 2] * qf[3]));
+#pragma unroll
+        for (int x = 0; x < 3; ++x) w[1 + x][r] = -c * (G[r * 3 + x] * qf[0]);
+      }
+    } else if constexpr (EQ == DG_EULER) {
+      const float u3[3] = {qf[2] * rinv, qf[3] * rinv, qf[4] * rinv};
+      float F[5][3];
+#pragma unroll
+      for (int x = 0; x < 3; ++x) {
+        F[0][x] = qf[2 + x];
+        F[1][x] = u3[x] * (qf[1] + p);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) F[2 + c][x] = qf[2 + c] * u3[x] + (c == x ? p : 0.f);
+      }
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          w[k][r] = fmaf(G[r * 3 + 0], F[k][0], fmaf(G[r * 3 + 1], F[k][1], G[r * 3 + 2] * F[k][2]));
+    } else {  // maxwell: E_t = curl H, H_t = -curl E (strong derivatives)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const float g0 = G[r * 3 + 0], g1 = G[r * 3 + 1], g2 = G[r * 3 + 2];
+        w[0][r] = g1 * qf[5] - g2 * qf[4];
+        w[1][r] = g2 * qf[3] - g0 * qf[5];
+        w[2][r] = g0 * qf[4] - g1 * qf[3];
+        w[3][r] = g2 * qf[1] - g1 * qf[2];
+        w[4][r] = g0 * qf[2] - g2 * qf[0];
+        w[5][r] = g1 * qf[0] - g0 * qf[1];
+      }
+    }
+  };
+
+  int it = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
     const int64_t e0 = tile * E;
     const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
+    unsigned* rmaxV = sRmax + (it & 1) * 256;  // this tile's row maxima
+    unsigned* rmaxL = rmaxV + 128;
+    {  // the other buffer was last read before the previous tile's final barrier
+      unsigned* other = sRmax + ((it + 1) & 1) * 256;
+      for (int idx = t; idx < 256; idx += THREADS) other[idx] = 0u;
+    }
 
-    // {{{ 1. state -> FP32 copy, metric-combined volume inputs -> X
+    // {{{ 1. state -> FP32 copies, volume inputs -> row maxima
     for (int u = warp; u < EG * JG; u += NWARP) {
       const int e = (u % EG) * 8 + (lane & 7);
       const int j = (u / EG) * 4 + (lane >> 3);
-      if (e >= E || j >= NP) continue;
-      const bool valid = e < ecount;
+      const bool item = e < E && j < NP;
+      const bool valid = item && e < ecount;
+      float qf[NF], G[9];
+      float p = 0.f, rinv = 1.f;
       const int64_t gnode = (e0 + e) * NP + j;
       double qd[NF];
-      float qf[NF];
 #pragma unroll
       for (int k = 0; k < NF; ++k) {
         qd[k] = valid ? __ldg(a.q + k * nelnp + gnode) : (k == 0 ? 1.0 : 0.0);
         qf[k] = d2f_alu(qd[k]);
-        sq[(k * E + e) * QP + j] = qf[k];
+        if (item) sq[(k * E + e) * QP + j] = qf[k];
       }
-      float G[9];
 #pragma unroll
-      for (int x = 0; x < 9; ++x) G[x] = valid ? d2f_alu(__ldg(a.metric + (e0 + e) * 9 + x)) : 0.f;
-      float w[NF][3];
-      if constexpr (EQ == DG_WAVE) {
-        const float c = (float)a.p0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          w[0][r] = -c * fmaf(G[r * 3 + 0], qf[1], fmaf(G[r * 3 + 1], qf[2], G[r * 3 + 2] * qf[3]));
-#pragma unroll
-          for (int x = 0; x < 3; ++x) w[1 + x][r] = -c * (G[r * 3 + x] * qf[0]);
-        }
-      } else if constexpr (EQ == DG_EULER) {
+      for (int x = 0; x < 9; ++x) {
+        G[x] = valid ? d2f_alu(__ldg(a.metric + (e0 + e) * 9 + x)) : 0.f;
+        if (item && j == 0) sG[e * 9 + x] = G[x];
+      }
+      if constexpr (EQ == DG_EULER) {
         const double rinv_d = rcp64_fast(qd[0]);
         const double p_d =
             (a.p0 - 1.0) *
             (qd[1] - 0.5 * (qd[2] * qd[2] + qd[3] * qd[3] + qd[4] * qd[4]) * rinv_d);
-        sP[e * NP + j] = p_d;
-        const float p = d2f_alu(p_d), rinv = d2f_alu(rinv_d);
-        const float u3[3] = {qf[2] * rinv, qf[3] * rinv, qf[4] * rinv};
-        float F[5][3];
-#pragma unroll
-        for (int x = 0; x < 3; ++x) {
-          F[0][x] = qf[2 + x];
-          F[1][x] = u3[x] * (qf[1] + p);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) F[2 + c][x] = qf[2 + c] * u3[x] + (c == x ? p : 0.f);
-        }
-#pragma unroll
-        for (int k = 0; k < 5; ++k)
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-            w[k][r] = fmaf(G[r * 3 + 0], F[k][0], fmaf(G[r * 3 + 1], F[k][1], G[r * 3 + 2] * F[k][2]));
-      } else {  // maxwell: E_t = curl H, H_t = -curl E (strong derivatives)
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          const float g0 = G[r * 3 + 0], g1 = G[r * 3 + 1], g2 = G[r * 3 + 2];
-          w[0][r] = g1 * qf[5] - g2 * qf[4];
-          w[1][r] = g2 * qf[3] - g0 * qf[5];
-          w[2][r] = g0 * qf[4] - g1 * qf[3];
-          w[3][r] = g2 * qf[1] - g1 * qf[2];
-          w[4][r] = g0 * qf[2] - g2 * qf[0];
-          w[5][r] = g1 * qf[0] - g0 * qf[1];
+        p = d2f_alu(p_d);
+        rinv = d2f_alu(rinv_d);
+        if (item) {
+          sP[e * NP + j] = p_d;
+          sR[e * NP + j] = rinv;
         }
       }
+      float w[NF][3];
+      vol_inputs(qf, G, p, rinv, w);
 #pragma unroll
-      for (int c = 0; c < NF; ++c)
+      for (int c = 0; c < NF; ++c) {
+        const float m = item ? fmaxf(fabsf(w[c][0]), fmaxf(fabsf(w[c][1]), fabsf(w[c][2]))) : 0.f;
+        tcm::row_max(rmaxV, c * E + (e < E ? e : 0), m, (lane >> 3) == 0 && e < E);
+      }
+    }
+    __syncthreads();
+    // }}}
+
+    // {{{ 2. volume inputs -> digits of X_V
+    for (int u = warp; u < EG * JG; u += NWARP) {
+      const int e = (u % EG) * 8 + (lane & 7);
+      const int j = (u / EG) * 4 + (lane >> 3);
+      if (e >= E || j >= NP) continue;
+      float qf[NF];
+#pragma unroll
+      for (int k = 0; k < NF; ++k) qf[k] = sq[(k * E + e) * QP + j];
+      float p = 0.f, rinv = 1.f;
+      if constexpr (EQ == DG_EULER) {
+        p = d2f_alu(sP[e * NP + j]);
+        rinv = sR[e * NP + j];
+      }
+      float w[NF][3];
+      vol_inputs(qf, sG + e * 9, p, rinv, w);
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const int m = c * E + e;
+        const int ex = tcm::row_exp_bits(rmaxV[m]);
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-          tcm::put_split(sA, P::A_SLICE_V, tcm::kmajor_off(c * E + e, r * NP + j, P::SBO_V),
-                         w[c][r]);
+          tcm::put_digits(sA, P::A_SLICE_V, tcm::kmajor_off(m, r * NP + j, P::SBO_V), w[c][r], ex);
+      }
     }
     tc::fence_async_smem();
     __syncthreads();
     // }}}
 
-    // {{{ 2. volume products (one thread), face fluxes (registers)
+    // {{{ 3. volume products (one thread); face fluxes (registers) and their
+    //        row maxima; then X_L and the LIFT products
     if (t == 0) {
-      tcm::issue_phase<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V>(
-          a_s, b_s + P::OPS_V, tmem, P::IDESC, true);
+      tcm::issue_phase<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V, NB>(a_s, b_s + P::OPS_V,
+                                                                       tmem, P::IDESC);
       tc::tc_commit(&mma_bar);
     }
     float fv[FROUNDS][NF];
-    int fm[FROUNDS];  // kmajor offset of (row c = 0, k = fj), -1: none
+    int fm[FROUNDS];  // e | fj << 8, or -1
 #pragma unroll
     for (int rd = 0; rd < FROUNDS; ++rd) {
       fm[rd] = -1;
       const int u = warp + rd * NWARP;
-      if (u >= EG * FG) continue;
       const int e = (u % EG) * 8 + (lane & 7);
       const int fj = (u / EG) * 4 + (lane >> 3);
-      if (e >= ecount || fj >= NFPT) continue;
-      const int f = fj / NFP;
-      const int node = sFN[fj];
-      const uint32_t g = __ldg(a.gather + (e0 + e) * NFPT + fj);
-      const bool bdry = (g >> 31) != 0u;
-      uint32_t gi = g & 0x7fffffffu;
-      if (gi >= (uint32_t)nelnp) {  // never read out of bounds
-        raise_status(a.status, DG_ERR_INDEX);
-        gi = (uint32_t)((e0 + e) * NP + node);
-      }
-      const double* fg = a.face_geom + (e0 + e) * 16 + f * 4;
-      const float nx = d2f_alu(__ldg(fg + 0)), ny = d2f_alu(__ldg(fg + 1)),
-                  nz = d2f_alu(__ldg(fg + 2)), scale = d2f_alu(__ldg(fg + 3));
-      float qi[NF];
-      double qed[NF];
+      const bool item = u < EG * FG && e < E && fj < NFPT;
 #pragma unroll
-      for (int k = 0; k < NF; ++k) {
-        qi[k] = sq[(k * E + e) * QP + node];
-        qed[k] = bdry ? 0.0 : __ldg(a.q + k * nelnp + gi);
+      for (int c = 0; c < NF; ++c) fv[rd][c] = 0.f;
+      if (item && e < ecount) {
+        const int f = fj / NFP;
+        const int node = sFN[fj];
+        const uint32_t g = __ldg(a.gather + (e0 + e) * NFPT + fj);
+        const bool bdry = (g >> 31) != 0u;
+        uint32_t gi = g & 0x7fffffffu;
+        if (gi >= (uint32_t)nelnp) {  // never read out of bounds
+          raise_status(a.status, DG_ERR_INDEX);
+          gi = (uint32_t)((e0 + e) * NP + node);
+        }
+        const double* fg = a.face_geom + (e0 + e) * 16 + f * 4;
+        const float nx = d2f_alu(__ldg(fg + 0)), ny = d2f_alu(__ldg(fg + 1)),
+                    nz = d2f_alu(__ldg(fg + 2)), scale = d2f_alu(__ldg(fg + 3));
+        float qi[NF];
+        double qed[NF];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+          qi[k] = sq[(k * E + e) * QP + node];
+          qed[k] = bdry ? 0.0 : __ldg(a.q + k * nelnp + gi);
+        }
+        const double pi_d = EQ == DG_EULER ? sP[e * NP + node] : 0.0;
+        tcm::face_point_flux<EQ, NF>(a, fc, qi, qed, bdry, nx, ny, nz, scale, pi_d, fv[rd]);
+        fm[rd] = e | (fj << 8);
       }
-      const double pi_d = EQ == DG_EULER ? sP[e * NP + node] : 0.0;
-      tcm::face_point_flux<EQ, NF>(a, qi, qed, bdry, nx, ny, nz, scale, pi_d, fv[rd]);
-      fm[rd] = e | (fj << 8);
+      if (u < EG * FG) {  // warp-uniform: every lane joins the shuffles
+#pragma unroll
+        for (int c = 0; c < NF; ++c)
+          tcm::row_max(rmaxL, c * E + (e < E ? e : 0), fabsf(fv[rd][c]),
+                       (lane >> 3) == 0 && e < E);
+      }
     }
-    wait_mma();  // the volume products have read X
-    // }}}
-
-    // {{{ 3. face values -> X, LIFT products into the same accumulator
+    __syncthreads();  // row maxima of X_L complete
+    wait_mma();       // the volume products have read X
 #pragma unroll
     for (int rd = 0; rd < FROUNDS; ++rd) {
       if (fm[rd] < 0) continue;
       const int e = fm[rd] & 0xff, fj = fm[rd] >> 8;
 #pragma unroll
-      for (int c = 0; c < NF; ++c)
-        tcm::put_split(sA, P::A_SLICE_L, tcm::kmajor_off(c * E + e, fj, P::SBO_L), fv[rd][c]);
+      for (int c = 0; c < NF; ++c) {
+        const int m = c * E + e;
+        tcm::put_digits(sA, P::A_SLICE_L, tcm::kmajor_off(m, fj, P::SBO_L), fv[rd][c],
+                        tcm::row_exp_bits(rmaxL[m]));
+      }
     }
     tc::fence_async_smem();
     __syncthreads();
     if (t == 0) {
-      tcm::issue_phase<P::KL, P::SBO_L, P::A_SLICE_L, P::B_SLICE_L>(
-          a_s, b_s + P::OPS_L, tmem, P::IDESC, false);
+      tcm::issue_phase<P::KL, P::SBO_L, P::A_SLICE_L, P::B_SLICE_L, NB>(
+          a_s, b_s + P::OPS_L, tmem + P::ACC_L, P::IDESC);
       tc::tc_commit(&mma_bar);
     }
     wait_mma();
     // }}}
 
-    // {{{ 4. D -> staging (warp w reads lanes 32 (w % 4)..), then the epilogue
+    // {{{ 4. level sums -> staging (warp w reads lanes 32 (w % 4)..), epilogue
     {
       const int qd = warp & 3;
       const int row = 32 * qd + lane;
       const uint32_t tq = tmem + ((uint32_t)(32 * qd) << 16);
       float sc = 1.f;
-      if constexpr (EQ == DG_MAXWELL) sc = (row / E) < 3 ? (float)a.k[4] : (float)a.k[5];
+      if constexpr (EQ == DG_MAXWELL) sc = (row / E) < 3 ? fc.ie : fc.im;
+      // row factors 2^(E_m - 14), E_m = e - 126 (the column factors 2^e_B
+      // come with the operator); products of powers of two are exact
+      const float rsv = tcm::pow2f(tcm::row_exp_bits(rmaxV[row]) - 140);
+      const float rsl = tcm::pow2f(tcm::row_exp_bits(rmaxL[row]) - 140);
 #pragma unroll 1
-      for (int ch = warp >> 2; ch < P::NB / 8; ch += NWARP / 4) {
-        uint32_t v[8];
-        tc::tc_ld8(tq + (uint32_t)(ch * 8), v);
+      for (int ch = warp >> 2; ch < NB / 8; ch += NWARP / 4) {
+        uint32_t v[32], l[32];  // levels 0..3 x 8 columns
+#pragma unroll
+        for (int lv = 0; lv < 4; ++lv) {
+          tc::tc_ld8(tq + (uint32_t)(lv * NB + ch * 8), v + 8 * lv);
+          tc::tc_ld8(tq + (uint32_t)(P::ACC_L + lv * NB + ch * 8), l + 8 * lv);
+        }
         tc::tc_wait_ld();
         if (row < P::NCOL) {
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const int col = ch * 8 + jj;
-            if (col < NP) sOut[row * OP + col] = sc * __uint_as_float(v[jj]);
+            if (col < NP) {
+              const float vol = tcm::levels4(v, jj) * (rsv * sEV[col]);
+              const float lift = tcm::levels4(l, jj) * (rsl * sEL[col]);
+              sOut[row * OP + col] = sc * (vol + lift);
+            }
           }
         }
       }
     }
     tc::tc_fence_before();
     __syncthreads();
-    for (int idx = t; idx < ecount * NP; idx += tcm::kThreads) {
+    for (int idx = t; idx < ecount * NP; idx += THREADS) {
       const int e = idx / NP, i = idx - e * NP;
       int64_t gidx = e0 * NP + idx;
       const double es = a.elem_scale ? __ldg(a.elem_scale + e0 + e) : 1.0;
@@ -475,8 +638,9 @@ __global__ void __launch_bounds__(tcm::kThreads, 1) dg_rhs_tcm_kernel(const RhsA
         }
       }
     }
-    // no barrier: the next tile writes X and the state copy, which no thread
-    // reads any more, and its first tensor-memory use follows a barrier
+    // no barrier: the next tile writes the state copies, X and the other
+    // row-maxima buffer, none of which a thread still reads; its first
+    // tensor-memory use follows two barriers
     // }}}
   }
   tc::tc_fence_before();

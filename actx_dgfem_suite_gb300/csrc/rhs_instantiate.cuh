@@ -243,13 +243,30 @@ cudaError_t tcm_shape_impl(LaunchShape* out) {
   cudaError_t err = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
   if (err != cudaSuccess) return err;
-  int nb = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, tcm::kThreads, P::SMEM_BYTES);
+  // resident CTAs per SM from the kernel's registers and shared memory (the
+  // occupancy query reports one CTA for kernels that allocate tensor
+  // memory), capped by the SM's 512 tensor-memory columns
+  cudaFuncAttributes fa;
+  err = cudaFuncGetAttributes(&fa, kern);
+  if (err != cudaSuccess) return err;
+  int dev = 0, regs_sm = 0, smem_sm = 0, smem_rsv = 0, thr_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  const int warps = P::THREADS / 32;
+  const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;  // 256-register units
+  int nb = regs_sm / (regs_warp * warps);
+  const int smem_blk = P::SMEM_BYTES + (int)fa.sharedSizeBytes + smem_rsv;
+  if (smem_sm / smem_blk < nb) nb = smem_sm / smem_blk;
+  if (thr_sm / P::THREADS < nb) nb = thr_sm / P::THREADS;
+  if (nb > 512 / P::TMEM_COLS) nb = 512 / P::TMEM_COLS;
   out->smem_bytes = P::SMEM_BYTES;
   out->blocks_per_sm = nb;
   out->elems_per_tile = P::E;
   out->ops_bytes = P::OPS_BYTES;
-  out->threads = tcm::kThreads;
+  out->threads = P::THREADS;
   return err;
 }
 
@@ -263,9 +280,9 @@ template <int N, int EQ>
 cudaError_t tcm_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
   using P = tcm::MPlan<N, EQ>;
   if (mode == 0)
-    dg_rhs_tcm_kernel<N, EQ, MODE_RHS><<<grid, tcm::kThreads, P::SMEM_BYTES, s>>>(a);
+    dg_rhs_tcm_kernel<N, EQ, MODE_RHS><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
   else
-    dg_rhs_tcm_kernel<N, EQ, MODE_STAGE><<<grid, tcm::kThreads, P::SMEM_BYTES, s>>>(a);
+    dg_rhs_tcm_kernel<N, EQ, MODE_STAGE><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -97,12 +97,13 @@ def test_tcgen05_mixed_matches_fp64(equation, order):
 def test_tcgen05_mixed_many_tiles_per_cta(equation, order):
     """More tiles than CTAs: every CTA runs the persistent loop several times."""
     from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
-    prob = make_problem(equation, jittered_box_mesh(12), order, seed=3)
+    prob = make_problem(equation, jittered_box_mesh(20), order, seed=3)
     dm = DeviceMesh(prob.disc, "cuda:0")
     ref = DevicePlan(dm, equation, prob.params, "fp64")
     mixed = DevicePlan(dm, equation, prob.params, "fp32-mixed")
     mixed.set_variant(4)
-    assert prob.disc.nelements > 2 * mixed.info()["grid"] * 21
+    tile = 128 // prob.fields.shape[0]   # elements per tile
+    assert prob.disc.nelements > 2 * mixed.info()["grid"] * tile
     q = torch.from_numpy(prob.fields).cuda()
     r64 = ref.rhs(q)
     r4 = mixed.rhs(q)
