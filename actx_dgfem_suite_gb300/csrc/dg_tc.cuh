@@ -91,11 +91,12 @@ struct Gemm {
 };
 
 // Elements per CTA tile: at most 64 data columns per contraction so the 8
-// level accumulators fit the 512 tensor-memory columns, and shared memory
-// for the FP16 operator digits at order 4.
+// level accumulators fit the 512 tensor-memory columns, filling the columns
+// the products pad to 16 anyway (wave 4 E, euler and maxwell NF E), within
+// the shared memory left beside the FP16 operator digits at order 4.
 constexpr int tile_elems(int N, int EQ) {
-  return N == 3 ? (EQ == DG_MAXWELL ? 10 : 12)
-                : (EQ == DG_EULER ? 5 : (EQ == DG_MAXWELL ? 6 : 7));
+  return N == 3 ? (EQ == DG_MAXWELL ? 10 : (EQ == DG_EULER ? 12 : 16))
+                : (EQ == DG_EULER ? 6 : (EQ == DG_MAXWELL ? 7 : 8));
 }
 
 constexpr int pow2_cols(int c) {
