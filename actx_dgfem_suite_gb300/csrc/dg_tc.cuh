@@ -133,15 +133,26 @@ struct Plan {
                                                NF * E * NFPT + GL::M * GL::NC));
   static constexpr int NCOLS = cmax(GV::NPAD, GL::NPAD);
   static constexpr int TMEM_ALLOC = pow2_cols(cmax(GV::TMEM_COLS, GL::TMEM_COLS));
+  // a tile's inputs: state, face values, metric (FP64)
+  static constexpr int IN_Q = p16(NF * E * NP * 8), IN_F = p16(NF * E * NFPT * 8);
+  static constexpr int IN_G = p16(9 * E * 8);
+  static constexpr int IN_BYTES = IN_Q + IN_F + IN_G;
+  // where shared memory allows (order 3), two input buffers: the next tile's
+  // inputs arrive by TMA bulk copies while the current tile computes
+  static constexpr bool PREFETCH =
+      p16(OPS_BYTES) + R1_BYTES + R2_BYTES + p16(NCOLS * 4) + 2 * IN_BYTES <= 227 * 1024;
   // shared memory: ops | state (FP64) | R1 (slices) | R2 (FP64 scratch) |
-  // metric | column exponents
+  // metric | column exponents | (PREFETCH: two input buffers, which then
+  // hold the state and metric)
   static constexpr int SM_OPS = 0;
   static constexpr int SM_Q = p16(OPS_BYTES);
-  static constexpr int SM_R1 = SM_Q + p16(NF * E * NP * 8);
+  static constexpr int SM_R1 = SM_Q + (PREFETCH ? 0 : IN_Q);
   static constexpr int SM_R2 = SM_R1 + R1_BYTES;
   static constexpr int SM_GEO = SM_R2 + R2_BYTES;
-  static constexpr int SM_EXP = SM_GEO + p16(9 * E * 8);
-  static constexpr int SMEM_USED = SM_EXP + p16(NCOLS * 4);
+  static constexpr int SM_EXP = SM_GEO + (PREFETCH ? 0 : IN_G);
+  static constexpr int SM_IN = SM_EXP + p16(NCOLS * 4);
+  static constexpr int SMEM_USED = SM_IN + (PREFETCH ? 2 * IN_BYTES : 0);
+  static_assert(!PREFETCH || (E * NP) % 2 == 0, "bulk-copy destinations 16-byte aligned");
   // a CTA that takes all 512 tensor-memory columns must be alone on its SM
   static constexpr int SMEM_BYTES =
       TMEM_ALLOC == 512 && SMEM_USED < 120 * 1024 ? 120 * 1024 : SMEM_USED;
@@ -463,11 +474,20 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
   __shared__ uint64_t mma_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int ops_ok;
+  __shared__ uint64_t in_bar[2];  // PREFETCH: input buffer b complete
+  __shared__ int in_bulk[2];      // PREFETCH: buffer b's tile came by bulk copies
+  constexpr bool PF = P::PREFETCH;
 
   const int t = threadIdx.x;
+  if constexpr (PF) {  // rows past a partial tile's elements stay finite
+    for (int idx = t; idx < 2 * P::IN_BYTES / 16; idx += tc::kTcBlock)
+      reinterpret_cast<uint4*>(smem + P::SM_IN)[idx] = make_uint4(0u, 0u, 0u, 0u);
+  }
   if (t == 0) {
     mbar_init(&bar, 1);
     mbar_init(&mma_bar, 1);
+    mbar_init(&in_bar[0], 1);
+    mbar_init(&in_bar[1], 1);
     mbar_arrive_expect_tx(&bar, a.ops_bytes);
     bulk_g2s(smem + P::SM_OPS, a.ops, a.ops_bytes, &bar);
     const bool ok = mbar_wait_bounded(&bar, 0);
@@ -520,12 +540,62 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
   const int64_t nelnp = nel * NP;
   const int64_t ntiles = (nel + E - 1) / E;
 
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  // PREFETCH: (thread 0) the inputs of tile `tl` into buffer b by 1D bulk
+  // copies: 1 when issued, 0 when a size or source address is not 16-byte
+  // aligned (the tile then loads with plain loads)
+  auto issue_in = [&](int64_t tl, int b) -> int {
+    const int64_t e0n = tl * E;
+    const int ec = (nel - e0n) < (int64_t)E ? (int)(nel - e0n) : E;
+    const uint32_t bq = (uint32_t)ec * NP * 8, bf = (uint32_t)ec * NFPT * 8,
+                   bg = (uint32_t)ec * 9 * 8;
+    bool ok = (bq % 16u) == 0u && (bf % 16u) == 0u && (bg % 16u) == 0u &&
+              ((uintptr_t)(a.metric + e0n * 9) & 15u) == 0u;
+#pragma unroll
+    for (int k = 0; k < NF; ++k)
+      ok = ok && ((uintptr_t)(a.q + k * nelnp + e0n * NP) & 15u) == 0u &&
+           ((uintptr_t)(a.flux_in + (k * nel + e0n) * NFPT) & 15u) == 0u;
+    if (!ok) return 0;
+    unsigned char* buf = smem + P::SM_IN + b * P::IN_BYTES;
+    mbar_arrive_expect_tx(&in_bar[b], (uint32_t)NF * (bq + bf) + bg);
+#pragma unroll
+    for (int k = 0; k < NF; ++k) {
+      bulk_g2s(buf + k * (E * NP * 8), a.q + k * nelnp + e0n * NP, bq, &in_bar[b]);
+      bulk_g2s(buf + P::IN_Q + k * (E * NFPT * 8), a.flux_in + (k * nel + e0n) * NFPT, bf,
+               &in_bar[b]);
+    }
+    bulk_g2s(buf + P::IN_Q + P::IN_F, a.metric + e0n * 9, bg, &in_bar[b]);
+    return 1;
+  };
+  uint32_t in_phase[2] = {0u, 0u};
+  if constexpr (PF) {
+    if (t == 0) in_bulk[0] = blockIdx.x < ntiles ? issue_in(blockIdx.x, 0) : 0;
+    __syncthreads();
+  }
+
+  int it = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
     const int64_t e0 = tile * E;
     const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
+    const int ib = it & 1;
+    double* sF = sR2;  // face values (PREFETCH: in the input buffer)
+    if constexpr (PF) {
+      unsigned char* buf = smem + P::SM_IN + ib * P::IN_BYTES;
+      sQ = reinterpret_cast<double*>(buf);
+      sF = reinterpret_cast<double*>(buf + P::IN_Q);
+      sG = reinterpret_cast<double*>(buf + P::IN_Q + P::IN_F);
+      // the other buffer's last reader was the previous tile, before its
+      // final barrier
+      if (t == 0) {
+        const int64_t nx = tile + gridDim.x;
+        in_bulk[ib ^ 1] = nx < ntiles ? issue_in(nx, ib ^ 1) : 0;
+      }
+    }
 
-    // {{{ 1. state and metric -> shared memory
-    {
+    // {{{ 1. state and metric (PREFETCH: and face values) -> shared memory
+    if (PF && in_bulk[ib]) {
+      if (!mbar_wait_bounded(&in_bar[ib], in_phase[ib])) raise_status(a.status, DG_ERR_TIMEOUT);
+      in_phase[ib] ^= 1u;
+    } else {
       const double* qk = a.q + e0 * NP;
 #pragma unroll
       for (int k = 0; k < NF; ++k, qk += nelnp)
@@ -534,6 +604,14 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
       const double* mt = a.metric + e0 * 9;
       for (int idx = t; idx < 9 * E; idx += tc::kTcBlock)
         sG[idx] = idx < 9 * ecount ? __ldg(mt + idx) : 0.0;
+      if constexpr (PF) {
+        const int64_t nfpt_all = nel * NFPT;
+        const double* fk = a.flux_in + e0 * NFPT;
+#pragma unroll
+        for (int k = 0; k < NF; ++k, fk += nfpt_all)
+          for (int rem = t; rem < E * NFPT; rem += tc::kTcBlock)
+            sF[k * (E * NFPT) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : 0.0;
+      }
     }
     __syncthreads();
     // }}}
@@ -641,17 +719,17 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
     __syncthreads();
     // }}}
 
-    // {{{ 6. face values of the tile -> R2, digit slices, 7. LIFT product
-    double* sF = sR2;                            // (NF, E, 4 Nfp)
-    {
+    // {{{ 6. face values of the tile (NF, E, 4 Nfp) -> R2 (PREFETCH: already
+    //        in the input buffer), digit slices, 7. LIFT product
+    if constexpr (!PF) {
       const int64_t nfpt_all = nel * NFPT;
       const double* fk = a.flux_in + e0 * NFPT;
 #pragma unroll
       for (int k = 0; k < NF; ++k, fk += nfpt_all)
         for (int rem = t; rem < E * NFPT; rem += tc::kTcBlock)
           sF[k * (E * NFPT) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : 0.0;
+      __syncthreads();
     }
-    __syncthreads();
     tc::split_columns<GL>(sR1, sExp, [&](int n, int k) { return sF[n * NFPT + k]; });
     __syncthreads();
     double* sL = sR2 + NF * E * NFPT;            // Np x (NF E)
