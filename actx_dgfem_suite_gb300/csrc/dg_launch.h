@@ -55,7 +55,7 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
 // tc_shape_* / tc_launch_*: the face-shared volume/LIFT kernel with the
 // contractions on the tensor cores (mode 0 RHS, 1 RK stage).
 // tcm_shape_* / tcm_launch_*: the mixed-precision kernel with its
-// contractions on tcgen05 (3xTF32; mode 0 RHS, 1 RK stage).
+// contractions on tcgen05 (exact digit-pair products; mode 0 RHS, 1 RK stage).
 #define DG_DECLARE_EQ(name)                                                   \
   cudaError_t shape_##name(int order, int precision, int mode,               \
                            LaunchShape* out);                                \

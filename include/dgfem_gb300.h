@@ -51,9 +51,11 @@ enum dg_equation { DG_WAVE = 0, DG_EULER = 1, DG_MAXWELL = 2 };
  * DG_FP32_MIXED: FP32 derivative/flux/LIFT arithmetic, FP64 state, FP64
  *   Euler pressure recovery and FP64 RK accumulation.
  * DG_FP64_TC: FP64 state and results with the volume and LIFT contractions
- *   on the tensor cores as an exact FP64 emulation by FP16 digit slices
- *   (error ~2^-53 of sum |A||x|, the size of FP64 rounding); needs the
- *   face-shared path (see dg_plan_create), else it falls back to DG_FP64. */
+ *   on the tcgen05 tensor cores as an exact FP64 emulation by FP16 digit
+ *   slices (54-bit row/column scaling, exact FP32 level sums in tensor
+ *   memory; error of the order of FP64's own accumulation error); orders 3
+ *   and 4 on the face-shared path (see dg_plan_create), other plans fall
+ *   back to DG_FP64 arithmetic. */
 enum dg_precision { DG_FP64 = 0, DG_FP32_MIXED = 1, DG_FP64_TC = 2 };
 
 typedef struct dg_plan dg_plan;
@@ -210,8 +212,10 @@ int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
  * tensor cores (DG_FP32_MIXED plans: 3xTF32 split with FP32 accumulation,
  * i.e. FP32 accuracy, as warp-level mma.sync), bit 1 = one CTA per tile
  * instead of the persistent grid; 4 = the DG_FP32_MIXED kernel with its
- * volume and LIFT contractions as one tcgen05 product per tile (3xTF32,
- * FP32 accumulators in tensor memory; persistent grid, one CTA per SM).
+ * volume and LIFT contractions as one tcgen05 product per tile (rows scaled
+ * to 31-bit integers in four FP16 digits, digit-pair products accumulated
+ * exactly in tensor memory: the most accurate mixed variant; persistent
+ * grid).
  * Default 0.  No counterpart in the reference. */
 int dg_plan_set_variant(dg_plan* plan, int32_t variant);
 
