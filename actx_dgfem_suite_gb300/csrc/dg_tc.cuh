@@ -23,9 +23,12 @@
 //   G_lo = sum_{l>=6} v_l 2^(7(9-l)) in 64-bit integers (exact), read out of
 //   tensor memory with tcgen05.ld.
 //
-// Dropped digit pairs (l > 9) and the 54-bit rounding of the inputs bound the
-// error by ~2^-53 of sum_k |A_mk| |X_kn| -- the size of FP64's own
-// rounding.  Splitting and recombination are integer work (no FP64 pipe).
+// Error: the 54-bit rounding of the inputs (2^-55 of the row or column
+// maximum) and the dropped digit pairs (l > 9, below ~2^-51 K max_k |A_mk|
+// max_k |X_kn|) -- the order of FP64's own accumulation error.  Splitting
+// and recombination are integer work (no FP64 pipe): the level sums are
+// folded by 64-bit Horner sums and converted to FP64 with round-to-nearest-
+// even built from the bits.
 //
 // One thread issues all products of a contraction (asynchronous, completion
 // signalled on an mbarrier through tcgen05.commit; the wait is bounded);
@@ -37,8 +40,11 @@
 // The kernel is the volume/LIFT half of the face-shared path: face values
 // come from dg_face_flux_kernel (and, for Euler, pressure and 1/rho from
 // dg_euler_aux_kernel), pointwise work (Euler fluxes, metric terms, curl,
-// RK epilogue) stays in FP64.  Orders 3 and 4 (lower orders have too little
-// contraction work for the digit splitting to pay).
+// RK epilogue) stays in FP64.  One 512-thread CTA per SM (the order-4
+// operator digits take 126 KB of shared memory); at order 3 the next tile's
+// inputs arrive by 1D TMA bulk copies into a second buffer while the current
+// tile computes.  Orders 3 and 4 (lower orders have too little contraction
+// work for the digit splitting to pay).
 #pragma once
 
 #include <cuda_fp16.h>
