@@ -161,6 +161,9 @@ struct dg_plan {
   uint32_t tc_ops_bytes = 0;
   dg::LaunchShape tc_shape;
   int tc_grid = 0;
+  // mixed-precision Euler: per-node FP32 pressure table, filled before each RHS
+  float* d_pres = nullptr;
+  int pres_grid = 0;
   // mixed precision with tcgen05 contractions (variant 4)
   bool tcm = false;
   void* d_tcm_ops = nullptr;
@@ -193,6 +196,7 @@ dg::RhsArgs base_args(const dg_plan* p) {
   a.elem_scale = p->elem_scale;
   a.flux_in = p->split ? p->d_flux : nullptr;
   a.aux = p->split ? p->d_aux : nullptr;
+  a.pres = p->d_pres;
   return a;
 }
 
@@ -713,6 +717,17 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   }
   p->face_partner = mesh->face_partner;
 
+  if (kprec == 1 && equation == DG_EULER) {
+    err = cudaMalloc(&p->d_pres, (size_t)p->nel * np * sizeof(float));
+    if (err != cudaSuccess) {
+      dg_plan_destroy(p);
+      return cuda_fail(err, "pressure table");
+    }
+    const int64_t pblocks = (p->nel * np + dg::kFaceBlock - 1) / dg::kFaceBlock;
+    const int64_t pfull = (int64_t)nsm * 8;
+    p->pres_grid = (int)(pblocks < pfull ? pblocks : pfull);
+  }
+
   if (split) {
     p->d_face_nodes = reinterpret_cast<const int32_t*>(
         static_cast<const unsigned char*>(p->d_ops) + off.fn);
@@ -952,6 +967,11 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     cudaError_t err = launch_faces(p, q, s);
     if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
   }
+  if (p->d_pres) {
+    cudaError_t err = dg::pressure_launch_euler(q, p->d_pres, p->nel * p->np,
+                                                p->params[0], p->pres_grid, s);
+    if (err != cudaSuccess) return cuda_fail(err, "pressure kernel launch");
+  }
   cudaError_t err;
   if (p->tc) {
     a.ops = p->d_tc_ops;
@@ -997,6 +1017,11 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
   if (p->split) {
     cudaError_t err = launch_faces(p, q_in, s);
     if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
+  }
+  if (p->d_pres) {
+    cudaError_t err = dg::pressure_launch_euler(q_in, p->d_pres, p->nel * p->np,
+                                                p->params[0], p->pres_grid, s);
+    if (err != cudaSuccess) return cuda_fail(err, "pressure kernel launch");
   }
   cudaError_t err;
   if (p->tc) {
@@ -1098,7 +1123,7 @@ int dg_plan_destroy(dg_plan* p) {
   if (p->d_status && cudaFree(p->d_status) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
   for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux,
-                  (void*)p->d_tc_ops, (void*)p->d_tcm_ops})
+                  (void*)p->d_tc_ops, (void*)p->d_tcm_ops, (void*)p->d_pres})
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
@@ -1124,7 +1149,7 @@ int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* tensor_cores,
     *tensor_cores =
         (p->tc || p->variant == 4 || ((p->variant & 1) && p->precision == DG_FP32_MIXED)) ? 1 : 0;
   if (launches_per_rhs)
-    *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : 1;
+    *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : (p->d_pres ? 2 : 1);
   if (owned_faces) *owned_faces = p->split ? p->nowned : 0;
   return DG_OK;
 }

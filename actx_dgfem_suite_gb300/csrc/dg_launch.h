@@ -103,6 +103,12 @@ cudaError_t adjoint_shape_wave(int order, LaunchShape* out);
 cudaError_t adjoint_launch_wave(int order, const AdjArgs& a, int grid, int nsm,
                                 cudaStream_t s);
 
+// Mixed-precision Euler: the per-node pressure table (FP64 recovery from
+// total energy, stored as FP32) that the mixed kernels read; one launch
+// before each mixed Euler RHS or RK stage.
+cudaError_t pressure_launch_euler(const double* q, float* pres, int64_t nelnp,
+                                  double gamma, int grid, cudaStream_t s);
+
 // Transposed Jacobian of the FP64 Euler RHS (dg_adjoint_euler.cuh): shape of
 // the volume kernel, and the launches (node table, volume, face, node gather).
 cudaError_t vjp_shape_euler(int order, LaunchShape* out);

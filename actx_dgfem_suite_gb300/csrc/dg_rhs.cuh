@@ -71,6 +71,8 @@ struct RhsArgs {
   double k[6];             // maxwell: z, 1/z, -1/(2z), 1/(2/z), 1/eps, 1/mu
   const double* flux_in;   // MODE_SPLIT: (NF, Nel, 4 Nfp) face values
   const double* aux;       // MODE_SPLIT euler: (3, Nel, Np) p, 1/rho, |u| + c
+  const float* pres;       // mixed-precision euler: (Nel, Np) pressure, recovered
+                           // from total energy in FP64 once per node, as FP32
 };
 
 template <int N>
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
   Real* sFlux = reinterpret_cast<Real*>(smem + T::FLUX);
   Real* sG = reinterpret_cast<Real*>(smem + T::GEO);
   Real* sFG = reinterpret_cast<Real*>(smem + T::FGEO);
-  double* sP = reinterpret_cast<double*>(smem + T::PRES);
+  float* sPf = reinterpret_cast<float*>(smem + T::PRES);  // mixed euler: node pressures
   float* sTC = reinterpret_cast<float*>(smem + T::TC);  // MODE_TC outputs
 
   const int t = threadIdx.x;
@@ -364,27 +366,37 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     } else if constexpr (EQ == DG_EULER) {
       if (active && el < ecount) {
         const Real* G = sG + el * 9;
-        // pressure recovery from total energy in FP64
-        const double rho_d = sQ[(0 * E + el) * NP + i];
-        const double en_d = sQ[(1 * E + el) * NP + i];
-        const double md[3] = {sQ[(2 * E + el) * NP + i], sQ[(3 * E + el) * NP + i],
-                              sQ[(4 * E + el) * NP + i]};
-        double rinv_d, p_d;
-        if constexpr (SPLIT) {
-          const int64_t gidx = e0 * NP + (el * NP + i);
-          p_d = __ldg(a.aux + gidx);
-          rinv_d = __ldg(a.aux + nelnp + gidx);
+        Real p, en, m[3], rinv;
+        if constexpr (T::MIXED) {
+          // the pressure from the per-node table (recovered from total
+          // energy in FP64 by dg_euler_pressure_f32_kernel)
+          p = __ldg(a.pres + e0 * NP + (el * NP + i));
+          sPf[el * NP + i] = p;
+          en = sQr[(1 * E + el) * ROW + i];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) m[c] = sQr[((2 + c) * E + el) * ROW + i];
+          rinv = __frcp_rn(sQr[(0 * E + el) * ROW + i]);
         } else {
-          if constexpr (T::MIXED) rinv_d = rcp64_fast(rho_d);
-          else rinv_d = 1.0 / rho_d;
-          p_d = (a.p0 - 1.0) *
-                (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
+          const double rho_d = sQ[(0 * E + el) * NP + i];
+          const double en_d = sQ[(1 * E + el) * NP + i];
+          const double md[3] = {sQ[(2 * E + el) * NP + i], sQ[(3 * E + el) * NP + i],
+                                sQ[(4 * E + el) * NP + i]};
+          double rinv_d, p_d;
+          if constexpr (SPLIT) {
+            const int64_t gidx = e0 * NP + (el * NP + i);
+            p_d = __ldg(a.aux + gidx);
+            rinv_d = __ldg(a.aux + nelnp + gidx);
+          } else {
+            rinv_d = 1.0 / rho_d;
+            p_d = (a.p0 - 1.0) *
+                  (en_d - 0.5 * (md[0] * md[0] + md[1] * md[1] + md[2] * md[2]) * rinv_d);
+          }
+          p = p_d;
+          en = en_d;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) m[c] = md[c];
+          rinv = rinv_d;
         }
-        if constexpr (T::MIXED) sP[el * NP + i] = p_d;
-        const Real p = to_real<Real>(p_d), en = to_real<Real>(en_d);
-        const Real m[3] = {to_real<Real>(md[0]), to_real<Real>(md[1]),
-                           to_real<Real>(md[2])};
-        const Real rinv = to_real<Real>(rinv_d);
         const Real u[3] = {m[0] * rinv, m[1] * rinv, m[2] * rinv};
         Real F[5][3];
 #pragma unroll
@@ -650,18 +662,13 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
         out[3 * FS] = scale * (fv * nz);
       } else if constexpr (EQ == DG_EULER) {
         const Real gamma = p0;
-        double pi_d = 0.0, pe_d = 0.0;
+        Real pi_m = zero, pe_m = zero;
         if constexpr (T::MIXED) {
-          // FP64 pressures: interior from the pre-pass, exterior recovered here
-          pi_d = sP[elp * NP + node];
-          if (bdry) {
-            pe_d = pi_d;  // the wall mirror keeps rho, |m| and E
-          } else {
-            const double rinv_e = rcp64_fast(qed[0]);
-            pe_d = (a.p0 - 1.0) *
-                   (qed[1] - 0.5 * (qed[2] * qed[2] + qed[3] * qed[3] + qed[4] * qed[4]) *
-                                 rinv_e);
-          }
+          // pressures from the per-node table: interior through the pre-pass
+          // copy, exterior at the gathered node (the wall mirror keeps rho,
+          // |m| and E, so its pressure)
+          pi_m = sPf[elp * NP + node];
+          pe_m = bdry ? pi_m : __ldg(a.pres + gi);
         }
         if (bdry) {  // InviscidWallBC: mirror the normal momentum
           if constexpr (T::MIXED) {
@@ -683,10 +690,10 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           }
         }
         Real fn_i[5], fn_e[5], lam_i, lam_e;
-        auto side = [&](const Real* q, double p_mixed, Real* fn, Real& lam) {
+        auto side = [&](const Real* q, Real p_mixed, Real* fn, Real& lam) {
           Real p, rinv;
           if constexpr (T::MIXED) {
-            p = to_real<Real>(p_mixed);
+            p = p_mixed;
             rinv = (Real)1 / q[0];
           } else {
             const double rinv_d = 1.0 / q[0];
@@ -703,8 +710,8 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           fn[4] = q[4] * un + p * nz;
           lam = sqrt(ux * ux + uy * uy + uz * uz) + sqrt(gamma * (p * rinv));
         };
-        side(qi, pi_d, fn_i, lam_i);
-        side(qe, pe_d, fn_e, lam_e);
+        side(qi, pi_m, fn_i, lam_i);
+        side(qe, pe_m, fn_e, lam_e);
         const Real lam = fmax(lam_i, lam_e);
         const Real nn = nx * nx + ny * ny + nz * nz;
 #pragma unroll

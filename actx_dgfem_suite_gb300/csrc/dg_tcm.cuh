@@ -36,9 +36,10 @@
 // Per tile of E = 128 / NF elements (8 elements x 4 nodes or face points per
 // warp, so the digit stores into the K-major operand layout are free of bank
 // conflicts):
-//   1. per node: the FP64 state -> FP32 copy, metric, (Euler: pressure from
-//      total energy in FP64, 1/rho), the inputs w -> row maxima (shuffles +
-//      shared atomics);
+//   1. per node: the FP64 state -> FP32 copy, metric, (Euler: the pressure
+//      from the per-node table, which dg_euler_pressure_f32_kernel fills by
+//      the FP64 recovery from total energy), the inputs w -> row maxima
+//      (shuffles + shared atomics);
 //   2. per node again: w -> digits of X_V;
 //   3. one thread issues the volume products (asynchronous, completion on an
 //      mbarrier); meanwhile every thread evaluates the numerical flux of its
@@ -100,9 +101,8 @@ struct MPlan {
   static constexpr int SM_G = SM_Q + p16(NF * E * QP * 4);
   static constexpr int SM_OUT = SM_G + p16(9 * E * 4);
   static constexpr int SM_RMAX = SM_OUT + p16(NCOL * OP * 4);  // [2 tiles][2 phases][128]
-  static constexpr int SM_P = SM_RMAX + 4 * 128 * 4;
-  static constexpr int SM_R = SM_P + (EQ == DG_EULER ? p16(E * NP * 8) : 0);
-  static constexpr int SMEM_BYTES = SM_R + (EQ == DG_EULER ? p16(E * NP * 4) : 0);
+  static constexpr int SM_P = SM_RMAX + 4 * 128 * 4;  // euler: node pressures (FP32)
+  static constexpr int SMEM_BYTES = SM_P + (EQ == DG_EULER ? p16(E * NP * 4) : 0);
   // accumulators: levels 0..3 of the volume phase, then of the LIFT phase
   static constexpr int ACC_L = 4 * NB;
   static constexpr int TMEM_COLS = pow2_cols(8 * NB);
@@ -210,14 +210,14 @@ __device__ __forceinline__ float levels4(const uint32_t* l, int jj) {
   return fmaf(t1, 0x1p-8f, __uint_as_float(l[jj]));
 }
 
-// Numerical flux of one face point in FP32 (FP64 exterior state, FP64
-// Euler pressures); out[c] = the lifted face value of field c.
+// Numerical flux of one face point in FP32 (FP64 exterior state; Euler:
+// interior and exterior pressures from the per-node table); out[c] = the
+// lifted face value of field c.
 template <int EQ, int NF>
-__device__ __forceinline__ void face_point_flux(const RhsArgs& a, const FluxConsts& fc,
-                                                const float* qi,
+__device__ __forceinline__ void face_point_flux(const FluxConsts& fc, const float* qi,
                                                 const double* qed, bool bdry, float nx,
                                                 float ny, float nz, float scale,
-                                                double pi_d, float* out) {
+                                                float pi, float pe, float* out) {
   float qe[NF];
   if (!bdry) {
 #pragma unroll
@@ -243,23 +243,16 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const FluxCons
     out[3] = scale * (fv * nz);
   } else if constexpr (EQ == DG_EULER) {
     const float gamma = fc.p0;
-    double pe_d;
-    if (bdry) {
-      pe_d = pi_d;  // the wall mirror keeps rho, |m| and E
+    if (bdry) {  // the wall mirror keeps rho, |m| and E (so the pressure)
       const float mn = qi[2] * nx + qi[3] * ny + qi[4] * nz;
       qe[0] = qi[0];
       qe[1] = qi[1];
       qe[2] = qi[2] - 2.f * nx * mn;
       qe[3] = qi[3] - 2.f * ny * mn;
       qe[4] = qi[4] - 2.f * nz * mn;
-    } else {
-      const double rinv_e = rcp64_fast(qed[0]);
-      pe_d = (a.p0 - 1.0) *
-             (qed[1] - 0.5 * (qed[2] * qed[2] + qed[3] * qed[3] + qed[4] * qed[4]) * rinv_e);
     }
     float fn_i[5], fn_e[5], lam_i, lam_e;
-    auto side = [&](const float* q, double p_d, float* fn, float& lam) {
-      const float p = d2f_alu(p_d);
+    auto side = [&](const float* q, float p, float* fn, float& lam) {
       const float rinv = 1.f / q[0];
       const float ux = q[2] * rinv, uy = q[3] * rinv, uz = q[4] * rinv;
       const float un = ux * nx + uy * ny + uz * nz;
@@ -270,8 +263,8 @@ __device__ __forceinline__ void face_point_flux(const RhsArgs& a, const FluxCons
       fn[4] = q[4] * un + p * nz;
       lam = sqrtf(ux * ux + uy * uy + uz * uz) + sqrtf(gamma * (p * rinv));
     };
-    side(qi, pi_d, fn_i, lam_i);
-    side(qe, pe_d, fn_e, lam_e);
+    side(qi, pi, fn_i, lam_i);
+    side(qe, bdry ? pi : pe, fn_e, lam_e);
     const float lam = fmaxf(lam_i, lam_e);
     const float nn = nx * nx + ny * ny + nz * nz;
 #pragma unroll
@@ -342,8 +335,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
   float* sG = reinterpret_cast<float*>(smem + P::SM_G);
   float* sOut = reinterpret_cast<float*>(smem + P::SM_OUT);
   unsigned* sRmax = reinterpret_cast<unsigned*>(smem + P::SM_RMAX);
-  double* sP = reinterpret_cast<double*>(smem + P::SM_P);
-  float* sR = reinterpret_cast<float*>(smem + P::SM_R);
+  float* sP = reinterpret_cast<float*>(smem + P::SM_P);  // euler: node pressures
   const tcm::FluxConsts fc = tcm::flux_consts(a);
   if (t == 0) {
     mbar_init(&bar, 1);
@@ -461,17 +453,10 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
         G[x] = valid ? d2f_alu(__ldg(a.metric + (e0 + e) * 9 + x)) : 0.f;
         if (item && j == 0) sG[e * 9 + x] = G[x];
       }
-      if constexpr (EQ == DG_EULER) {
-        const double rinv_d = rcp64_fast(qd[0]);
-        const double p_d =
-            (a.p0 - 1.0) *
-            (qd[1] - 0.5 * (qd[2] * qd[2] + qd[3] * qd[3] + qd[4] * qd[4]) * rinv_d);
-        p = d2f_alu(p_d);
-        rinv = d2f_alu(rinv_d);
-        if (item) {
-          sP[e * NP + j] = p_d;
-          sR[e * NP + j] = rinv;
-        }
+      if constexpr (EQ == DG_EULER) {  // pressure table: FP64 recovery once per node
+        p = valid ? __ldg(a.pres + gnode) : 0.f;
+        rinv = __frcp_rn(qf[0]);
+        if (item) sP[e * NP + j] = p;
       }
       float w[NF][3];
       vol_inputs(qf, G, p, rinv, w);
@@ -494,8 +479,8 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
       for (int k = 0; k < NF; ++k) qf[k] = sq[(k * E + e) * QP + j];
       float p = 0.f, rinv = 1.f;
       if constexpr (EQ == DG_EULER) {
-        p = d2f_alu(sP[e * NP + j]);
-        rinv = sR[e * NP + j];
+        p = sP[e * NP + j];
+        rinv = __frcp_rn(qf[0]);
       }
       float w[NF][3];
       vol_inputs(qf, sG + e * 9, p, rinv, w);
@@ -550,8 +535,12 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
           qi[k] = sq[(k * E + e) * QP + node];
           qed[k] = bdry ? 0.0 : __ldg(a.q + k * nelnp + gi);
         }
-        const double pi_d = EQ == DG_EULER ? sP[e * NP + node] : 0.0;
-        tcm::face_point_flux<EQ, NF>(a, fc, qi, qed, bdry, nx, ny, nz, scale, pi_d, fv[rd]);
+        float pi = 0.f, pe = 0.f;
+        if constexpr (EQ == DG_EULER) {
+          pi = sP[e * NP + node];
+          pe = bdry ? pi : __ldg(a.pres + gi);
+        }
+        tcm::face_point_flux<EQ, NF>(fc, qi, qed, bdry, nx, ny, nz, scale, pi, pe, fv[rd]);
         fm[rd] = e | (fj << 8);
       }
       if (u < EG * FG) {  // warp-uniform: every lane joins the shuffles

@@ -32,4 +32,31 @@ cudaError_t tcm_launch_euler(int order, int mode, const RhsArgs& a, int grid,
                         cudaStream_t s) {
   return tcm_launch_any<DG_EULER>(order, mode, a, grid, s);
 }
+
+// Mixed-precision Euler: the pressure of every node, recovered from total
+// energy in FP64 with the mixed kernels' reciprocal (FP32 estimate refined
+// by one Newton step) and stored as FP32, the flux arithmetic's type.  Once
+// per node, where the kernels would otherwise recover it for every node and
+// again for the exterior side of every face point on the FP64 pipe.
+__global__ void __launch_bounds__(kFaceBlock)
+    dg_euler_pressure_f32_kernel(const double* __restrict__ q, float* __restrict__ pres,
+                                 int64_t nelnp, double gamma) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nelnp;
+       idx += stride) {
+    const double rho = __ldg(q + idx);
+    const double en = __ldg(q + nelnp + idx);
+    const double m0 = __ldg(q + 2 * nelnp + idx);
+    const double m1 = __ldg(q + 3 * nelnp + idx);
+    const double m2 = __ldg(q + 4 * nelnp + idx);
+    const double rinv = rcp64_fast(rho);
+    pres[idx] = d2f_alu((gamma - 1.0) * (en - 0.5 * (m0 * m0 + m1 * m1 + m2 * m2) * rinv));
+  }
+}
+
+cudaError_t pressure_launch_euler(const double* q, float* pres, int64_t nelnp,
+                                  double gamma, int grid, cudaStream_t s) {
+  dg_euler_pressure_f32_kernel<<<grid, kFaceBlock, 0, s>>>(q, pres, nelnp, gamma);
+  return cudaGetLastError();
+}
 }  // namespace dg
