@@ -146,3 +146,24 @@ def test_inconsistent_partner_rejected():
     dm.partner = torch.from_numpy(bad2.reshape(part.shape)).to("cuda:0")
     with pytest.raises(DGError, match="face_partner"):
         DevicePlan(dm, "wave", prob.params)
+
+
+@pytest.mark.parametrize("equation", EQUATIONS)
+@pytest.mark.parametrize("order", (3, 4))
+@pytest.mark.parametrize("drop", (1, 7))
+def test_parity_odd_element_count(equation, order, drop):
+    """A box mesh with ``drop`` elements removed (their faces become walls):
+    an odd element count leaves partial tiles whose sizes are no multiple of
+    16 bytes, which the order-3 tensor-core kernel loads with plain loads
+    instead of its bulk-copy prefetch; both paths against the oracle."""
+    from actx_dgfem_suite_gb300.mesh import TetMesh
+    box = jittered_box_mesh(4)
+    keep = np.ones(box.nelements, dtype=bool)
+    keep[np.linspace(0, box.nelements - 1, drop).astype(int)] = False
+    mesh = TetMesh(box.vertices, box.elements[keep])
+    assert mesh.nelements % 2 == 1
+    prob = make_problem(equation, mesh, order, seed=order + drop)
+    ref, scale = oracle_rhs(prob, parts=True)
+    for path in ("tc", "shared"):
+        got, _ = _gpu_rhs(prob, path)
+        assert parity_error(got, ref, scale) <= FP64_RTOL
