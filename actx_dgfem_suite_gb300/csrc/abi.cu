@@ -461,7 +461,8 @@ int pack_tcm_ops(int order, const double* diff, const double* lift,
                  const int32_t* face_nodes, unsigned char* out, int out_bytes) {
   const int np = (order + 1) * (order + 2) * (order + 3) / 6;
   const int nfpt = 2 * (order + 1) * (order + 2);
-  const int nb = (np + 15) & ~15, kv = (3 * np + 15) & ~15, kl = (nfpt + 15) & ~15;
+  const int npp = np + (np & 1);  // node pitch of the volume columns (even)
+  const int nb = (np + 15) & ~15, kv = (3 * npp + 15) & ~15, kl = (nfpt + 15) & ~15;
   const int sbo_v = (kv / 8) * 128, sbo_l = (kl / 8) * 128;
   const int bs_v = (nb / 8) * sbo_v, bs_l = (nb / 8) * sbo_l;
   const int ops_l = 4 * bs_v, ops_ev = ops_l + 4 * bs_l, ops_el = ops_ev + nb * 4;
@@ -493,8 +494,10 @@ int pack_tcm_ops(int order, const double* diff, const double* lift,
       }
     }
   };
-  block(0, bs_v, sbo_v, 3 * np, ops_ev,
-        [&](int i, int k) { const int r = k / np; return diff[((size_t)r * np + i) * np + k - r * np]; });
+  block(0, bs_v, sbo_v, 3 * npp, ops_ev, [&](int i, int k) {
+    const int r = k / npp, j = k - r * npp;  // column r npp + j; j = np is padding
+    return j < np ? diff[((size_t)r * np + i) * np + j] : 0.0;
+  });
   block(ops_l, bs_l, sbo_l, nfpt, ops_el,
         [&](int i, int k) { return lift[(size_t)i * nfpt + k]; });
   std::memcpy(out + ops_fn, face_nodes, (size_t)nfpt * 4);

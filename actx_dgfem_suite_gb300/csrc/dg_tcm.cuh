@@ -33,9 +33,9 @@
 // unbiased, where TF32 products accumulated by the tensor core lose accuracy
 // with every accumulation step.
 //
-// Per tile of E = 128 / NF elements (8 elements x 4 nodes or face points per
-// warp, so the digit stores into the K-major operand layout are free of bank
-// conflicts):
+// Per tile of E = 128 / NF elements (8 elements x 4 pairs of nodes or face
+// points per warp; a pair's digits are one 4-byte word per digit slice, and
+// the 32 words a warp stores fall in 32 distinct banks):
 //   1. per node: the FP64 state -> FP32 copy, metric, (Euler: the pressure
 //      from the per-node table, which dg_euler_pressure_f32_kernel fills by
 //      the FP64 recovery from total energy), the inputs w -> row maxima
@@ -79,7 +79,10 @@ struct MPlan {
   static constexpr int E = 128 / NF;      // elements per tile
   static constexpr int NCOL = NF * E;     // rows of X in use (m = c E + e)
   static constexpr int NB = r16(NP);      // operator rows (MMA N)
-  static constexpr int KV = r16(3 * NP), KL = r16(NFPT);
+  // X_V column of derivative r and node j: k = r NPP + j, NPP = Np rounded up
+  // to even, so the two nodes a lane writes share one 4-byte word
+  static constexpr int NPP = NP + (NP & 1);
+  static constexpr int KV = r16(3 * NPP), KL = r16(NFPT);
   // K-major, no swizzle: element (m, k) of a digit slice at
   //   (m / 8) SBO + (k / 8) 128 + (m % 8) 16 + (k % 8) 2 bytes
   static constexpr int SBO_V = (KV / 8) * 128, SBO_L = (KL / 8) * 128;
@@ -153,28 +156,38 @@ __device__ __forceinline__ int row_exp_bits(uint32_t maxbits) {
   return e < 30 ? 30 : e;
 }
 
-// x (|x| < 2^(e - 126)) -> four FP16 digits of v = round(x 2^(157 - e)),
-// |v| <= 2^31, at byte offset `off` of the four slices.  FP32 arithmetic is
-// exact here: v has at most 24 significant bits, and every remainder is a
-// multiple of ulp(v) below 2^24 ulp(v).
-__device__ __forceinline__ void put_digits(unsigned char* base, int slice, int off, float x,
-                                           int e) {
-  const float v = rintf(x * __uint_as_float((uint32_t)(284 - e) << 23));
-  const float d0 = rintf(v * 0x1p-24f);
-  const float r1 = fmaf(-d0, 0x1p24f, v);
-  const float d1 = rintf(r1 * 0x1p-16f);
-  const float r2 = fmaf(-d1, 65536.f, r1);
-  const float d2 = rintf(r2 * 0x1p-8f);
-  const float d3 = fmaf(-d2, 256.f, r2);
-  const __half2 h01 = __floats2half2_rn(d0, d1), h23 = __floats2half2_rn(d2, d3);
-  *reinterpret_cast<__half*>(base + off) = __low2half(h01);
-  *reinterpret_cast<__half*>(base + slice + off) = __high2half(h01);
-  *reinterpret_cast<__half*>(base + 2 * slice + off) = __low2half(h23);
-  *reinterpret_cast<__half*>(base + 3 * slice + off) = __high2half(h23);
+// x (|x| < 2^(e - 126)) -> four digits of v = round(x 2^(157 - e)),
+// |v| <= 2^31, most significant first.  FP32 arithmetic is exact here: v has
+// at most 24 significant bits, and every remainder is a multiple of ulp(v)
+// below 2^24 ulp(v).
+__device__ __forceinline__ void digits4(float x, float scale, float* d) {
+  const float v = rintf(x * scale);
+  d[0] = rintf(v * 0x1p-24f);
+  const float r1 = fmaf(-d[0], 0x1p24f, v);
+  d[1] = rintf(r1 * 0x1p-16f);
+  const float r2 = fmaf(-d[1], 65536.f, r1);
+  d[2] = rintf(r2 * 0x1p-8f);
+  d[3] = fmaf(-d[2], 256.f, r2);
 }
 
-// max over the four lanes of a warp that share lane & 7 (elements), then one
-// shared atomic per element row
+// two values of one row at columns k, k + 1 (k even: one 4-byte word per
+// slice) -> their FP16 digits in the four slices at byte offset `off`
+__device__ __forceinline__ void put_digits2(unsigned char* base, int slice, int off,
+                                            float x0, float x1, int e) {
+  const float scale = __uint_as_float((uint32_t)(284 - e) << 23);
+  float a[4], b[4];
+  digits4(x0, scale, a);
+  digits4(x1, scale, b);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const __half2 h = __floats2half2_rn(a[i], b[i]);  // low half: column k
+    *reinterpret_cast<__half2*>(base + i * slice + off) = h;
+  }
+}
+
+// max over the four lanes of a warp that share lane & 7 (elements; the
+// lanes differ in their pair of nodes or face points), then one shared
+// atomic per element row
 __device__ __forceinline__ void row_max(unsigned* rmax, int m, float a, bool lead) {
   a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, 8));
   a = fmaxf(a, __shfl_xor_sync(0xffffffffu, a, 16));
@@ -373,8 +386,12 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
   const int64_t nel = a.nel;
   const int64_t nelnp = nel * NP;
   const int64_t ntiles = (nel + E - 1) / E;
-  constexpr int EG = (E + 7) / 8, JG = (NP + 3) / 4, FG = (NFPT + 3) / 4;
+  // warp items: 8 elements x 4 pairs of nodes (face points); a lane takes
+  // nodes (face points) 2 p and 2 p + 1
+  constexpr int NPP = P::NPP;
+  constexpr int EG = (E + 7) / 8, JG = (NPP / 2 + 3) / 4, FG = (NFPT / 2 + 3) / 4;
   constexpr int FROUNDS = (EG * FG + NWARP - 1) / NWARP;  // face items per thread
+  static_assert(NFPT % 2 == 0, "face points come in pairs");
 
   auto wait_mma = [&]() {
     if (!mbar_wait_bounded(&mma_bar, mma_phase)) raise_status(a.status, DG_ERR_TIMEOUT);
@@ -435,62 +452,81 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
     // {{{ 1. state -> FP32 copies, volume inputs -> row maxima
     for (int u = warp; u < EG * JG; u += NWARP) {
       const int e = (u % EG) * 8 + (lane & 7);
-      const int j = (u / EG) * 4 + (lane >> 3);
-      const bool item = e < E && j < NP;
-      const bool valid = item && e < ecount;
-      float qf[NF], G[9];
-      float p = 0.f, rinv = 1.f;
-      const int64_t gnode = (e0 + e) * NP + j;
-      double qd[NF];
-#pragma unroll
-      for (int k = 0; k < NF; ++k) {
-        qd[k] = valid ? __ldg(a.q + k * nelnp + gnode) : (k == 0 ? 1.0 : 0.0);
-        qf[k] = d2f_alu(qd[k]);
-        if (item) sq[(k * E + e) * QP + j] = qf[k];
-      }
+      const int j0 = 2 * ((u / EG) * 4 + (lane >> 3));
+      const bool ein = e < E;
+      const bool valid_e = ein && e < ecount;
+      float G[9];
 #pragma unroll
       for (int x = 0; x < 9; ++x) {
-        G[x] = valid ? d2f_alu(__ldg(a.metric + (e0 + e) * 9 + x)) : 0.f;
-        if (item && j == 0) sG[e * 9 + x] = G[x];
+        G[x] = valid_e ? d2f_alu(__ldg(a.metric + (e0 + e) * 9 + x)) : 0.f;
+        if (ein && j0 == 0) sG[e * 9 + x] = G[x];
       }
-      if constexpr (EQ == DG_EULER) {  // pressure table: FP64 recovery once per node
-        p = valid ? __ldg(a.pres + gnode) : 0.f;
-        rinv = __frcp_rn(qf[0]);
-        if (item) sP[e * NP + j] = p;
-      }
-      float w[NF][3];
-      vol_inputs(qf, G, p, rinv, w);
+      float m[NF];
 #pragma unroll
-      for (int c = 0; c < NF; ++c) {
-        const float m = item ? fmaxf(fabsf(w[c][0]), fmaxf(fabsf(w[c][1]), fabsf(w[c][2]))) : 0.f;
-        tcm::row_max(rmaxV, c * E + (e < E ? e : 0), m, (lane >> 3) == 0 && e < E);
+      for (int c = 0; c < NF; ++c) m[c] = 0.f;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int j = j0 + h;
+        const bool item = ein && j < NP;
+        const bool valid = item && e < ecount;
+        const int64_t gnode = (e0 + e) * NP + j;
+        float qf[NF];
+        float p = 0.f, rinv = 1.f;
+#pragma unroll
+        for (int k = 0; k < NF; ++k) {
+          const double qd = valid ? __ldg(a.q + k * nelnp + gnode) : (k == 0 ? 1.0 : 0.0);
+          qf[k] = d2f_alu(qd);
+          if (item) sq[(k * E + e) * QP + j] = qf[k];
+        }
+        if constexpr (EQ == DG_EULER) {  // pressure table: FP64 recovery once per node
+          p = valid ? __ldg(a.pres + gnode) : 0.f;
+          rinv = __frcp_rn(qf[0]);
+          if (item) sP[e * NP + j] = p;
+        }
+        float w[NF][3];
+        vol_inputs(qf, G, p, rinv, w);
+        if (item) {
+#pragma unroll
+          for (int c = 0; c < NF; ++c)
+            m[c] = fmaxf(m[c], fmaxf(fabsf(w[c][0]), fmaxf(fabsf(w[c][1]), fabsf(w[c][2]))));
+        }
       }
+#pragma unroll
+      for (int c = 0; c < NF; ++c)
+        tcm::row_max(rmaxV, c * E + (ein ? e : 0), m[c], (lane >> 3) == 0 && ein);
     }
     __syncthreads();
     // }}}
 
-    // {{{ 2. volume inputs -> digits of X_V
+    // {{{ 2. volume inputs -> digits of X_V (node pairs; a node past Np is the
+    //        zero padding column)
     for (int u = warp; u < EG * JG; u += NWARP) {
       const int e = (u % EG) * 8 + (lane & 7);
-      const int j = (u / EG) * 4 + (lane >> 3);
-      if (e >= E || j >= NP) continue;
-      float qf[NF];
+      const int j0 = 2 * ((u / EG) * 4 + (lane >> 3));
+      if (e >= E || j0 >= NP) continue;
+      const bool two = j0 + 1 < NP;
+      float w0[NF][3], w1[NF][3];
 #pragma unroll
-      for (int k = 0; k < NF; ++k) qf[k] = sq[(k * E + e) * QP + j];
-      float p = 0.f, rinv = 1.f;
-      if constexpr (EQ == DG_EULER) {
-        p = sP[e * NP + j];
-        rinv = __frcp_rn(qf[0]);
+      for (int h = 0; h < 2; ++h) {
+        const int j = two ? j0 + h : j0;
+        float qf[NF];
+#pragma unroll
+        for (int k = 0; k < NF; ++k) qf[k] = sq[(k * E + e) * QP + j];
+        float p = 0.f, rinv = 1.f;
+        if constexpr (EQ == DG_EULER) {
+          p = sP[e * NP + j];
+          rinv = __frcp_rn(qf[0]);
+        }
+        vol_inputs(qf, sG + e * 9, p, rinv, h == 0 ? w0 : w1);
       }
-      float w[NF][3];
-      vol_inputs(qf, sG + e * 9, p, rinv, w);
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
         const int m = c * E + e;
         const int ex = tcm::row_exp_bits(rmaxV[m]);
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-          tcm::put_digits(sA, P::A_SLICE_V, tcm::kmajor_off(m, r * NP + j, P::SBO_V), w[c][r], ex);
+          tcm::put_digits2(sA, P::A_SLICE_V, tcm::kmajor_off(m, r * NPP + j0, P::SBO_V),
+                           w0[c][r], two ? w1[c][r] : 0.f, ex);
       }
     }
     tc::fence_async_smem();
@@ -504,49 +540,57 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
                                                                        tmem, P::IDESC);
       tc::tc_commit(&mma_bar);
     }
-    float fv[FROUNDS][NF];
-    int fm[FROUNDS];  // e | fj << 8, or -1
+    float fv[FROUNDS][2][NF];
+    int fm[FROUNDS];  // e | fj0 << 8 (fj0 even), or -1
 #pragma unroll
     for (int rd = 0; rd < FROUNDS; ++rd) {
       fm[rd] = -1;
       const int u = warp + rd * NWARP;
       const int e = (u % EG) * 8 + (lane & 7);
-      const int fj = (u / EG) * 4 + (lane >> 3);
-      const bool item = u < EG * FG && e < E && fj < NFPT;
+      const int fj0 = 2 * ((u / EG) * 4 + (lane >> 3));
+      const bool item = u < EG * FG && e < E && fj0 < NFPT;
 #pragma unroll
-      for (int c = 0; c < NF; ++c) fv[rd][c] = 0.f;
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int c = 0; c < NF; ++c) fv[rd][h][c] = 0.f;
       if (item && e < ecount) {
-        const int f = fj / NFP;
-        const int node = sFN[fj];
-        const uint32_t g = __ldg(a.gather + (e0 + e) * NFPT + fj);
-        const bool bdry = (g >> 31) != 0u;
-        uint32_t gi = g & 0x7fffffffu;
-        if (gi >= (uint32_t)nelnp) {  // never read out of bounds
-          raise_status(a.status, DG_ERR_INDEX);
-          gi = (uint32_t)((e0 + e) * NP + node);
-        }
-        const double* fg = a.face_geom + (e0 + e) * 16 + f * 4;
-        const float nx = d2f_alu(__ldg(fg + 0)), ny = d2f_alu(__ldg(fg + 1)),
-                    nz = d2f_alu(__ldg(fg + 2)), scale = d2f_alu(__ldg(fg + 3));
-        float qi[NF];
-        double qed[NF];
 #pragma unroll
-        for (int k = 0; k < NF; ++k) {
-          qi[k] = sq[(k * E + e) * QP + node];
-          qed[k] = bdry ? 0.0 : __ldg(a.q + k * nelnp + gi);
+        for (int h = 0; h < 2; ++h) {
+          const int fj = fj0 + h;
+          const int f = fj / NFP;
+          const int node = sFN[fj];
+          const uint32_t g = __ldg(a.gather + (e0 + e) * NFPT + fj);
+          const bool bdry = (g >> 31) != 0u;
+          uint32_t gi = g & 0x7fffffffu;
+          if (gi >= (uint32_t)nelnp) {  // never read out of bounds
+            raise_status(a.status, DG_ERR_INDEX);
+            gi = (uint32_t)((e0 + e) * NP + node);
+          }
+          const double* fg = a.face_geom + (e0 + e) * 16 + f * 4;
+          const float nx = d2f_alu(__ldg(fg + 0)), ny = d2f_alu(__ldg(fg + 1)),
+                      nz = d2f_alu(__ldg(fg + 2)), scale = d2f_alu(__ldg(fg + 3));
+          float qi[NF];
+          double qed[NF];
+#pragma unroll
+          for (int k = 0; k < NF; ++k) {
+            qi[k] = sq[(k * E + e) * QP + node];
+            qed[k] = bdry ? 0.0 : __ldg(a.q + k * nelnp + gi);
+          }
+          float pi = 0.f, pe = 0.f;
+          if constexpr (EQ == DG_EULER) {
+            pi = sP[e * NP + node];
+            pe = bdry ? pi : __ldg(a.pres + gi);
+          }
+          tcm::face_point_flux<EQ, NF>(fc, qi, qed, bdry, nx, ny, nz, scale, pi, pe,
+                                       fv[rd][h]);
         }
-        float pi = 0.f, pe = 0.f;
-        if constexpr (EQ == DG_EULER) {
-          pi = sP[e * NP + node];
-          pe = bdry ? pi : __ldg(a.pres + gi);
-        }
-        tcm::face_point_flux<EQ, NF>(fc, qi, qed, bdry, nx, ny, nz, scale, pi, pe, fv[rd]);
-        fm[rd] = e | (fj << 8);
+        fm[rd] = e | (fj0 << 8);
       }
       if (u < EG * FG) {  // warp-uniform: every lane joins the shuffles
 #pragma unroll
         for (int c = 0; c < NF; ++c)
-          tcm::row_max(rmaxL, c * E + (e < E ? e : 0), fabsf(fv[rd][c]),
+          tcm::row_max(rmaxL, c * E + (e < E ? e : 0),
+                       fmaxf(fabsf(fv[rd][0][c]), fabsf(fv[rd][1][c])),
                        (lane >> 3) == 0 && e < E);
       }
     }
@@ -555,12 +599,12 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
 #pragma unroll
     for (int rd = 0; rd < FROUNDS; ++rd) {
       if (fm[rd] < 0) continue;
-      const int e = fm[rd] & 0xff, fj = fm[rd] >> 8;
+      const int e = fm[rd] & 0xff, fj0 = fm[rd] >> 8;
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
         const int m = c * E + e;
-        tcm::put_digits(sA, P::A_SLICE_L, tcm::kmajor_off(m, fj, P::SBO_L), fv[rd][c],
-                        tcm::row_exp_bits(rmaxL[m]));
+        tcm::put_digits2(sA, P::A_SLICE_L, tcm::kmajor_off(m, fj0, P::SBO_L), fv[rd][0][c],
+                         fv[rd][1][c], tcm::row_exp_bits(rmaxL[m]));
       }
     }
     tc::fence_async_smem();
