@@ -56,6 +56,25 @@ def _dist():
     return rank, world, local
 
 
+def max_over_ranks(value: float, device) -> float:
+    """The maximum of a per-rank time over all ranks of the initialised
+    process group (the replica that finished last sets the job's time);
+    ``value`` itself for a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank: float, seconds: float, world: int) -> float:
+    """Whole-job rate of ``world`` independent replicas that each process
+    ``units_per_rank`` in at most ``seconds`` (the max over ranks)."""
+    return world * units_per_rank / seconds
+
+
 # {{{ clocks sampling
 
 
@@ -460,13 +479,9 @@ def our_arm(args) -> None:
     total_ms = t_all0.elapsed_time(t_all1)
     case_ms = [statistics.mean(events[s][k][0].elapsed_time(events[s][k][1])
                                for s in range(K)) for k in range(len(runs))]
-    ms_step = total_ms / K
-    if world > 1:
-        t = torch.tensor([ms_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(total_ms / K, dev)
     dofs_step = sum(r["cost"].dofs for r in runs)
-    value = world * dofs_step / (ms_step * 1e-3)
+    value = replica_rate(dofs_step, ms_step * 1e-3, world)
     flops_step = sum(r["cost"].flops for r in runs)
 
     # {{{ e2e through the public API with host buffers
@@ -501,16 +516,12 @@ def our_arm(args) -> None:
     for _ in range(ke):
         host_out = e2e_step()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / ke
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, dev)
     # sanity: the host result equals the device-resident result
     ok = all(np.array_equal(np.stack([d[0] for d in leaves(h)]),
                             r["out"].cpu().numpy())
              for h, r in zip(host_out[:1], runs[:1]))
-    e2e_value = world * dofs_step / e2e_s
+    e2e_value = replica_rate(dofs_step, e2e_s, world)
     # }}}
 
     # {{{ roofline of the dominant launch
