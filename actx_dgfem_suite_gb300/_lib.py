@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc", "dg_rhs_vjp",
                     "dg_box_mesh_build",
                     "dg_plan_path", "dg_plan_info", "dg_plan_set_variant",
-                    "dg_plan_autotune", "dg_fp64_fma_probe",
+                    "dg_plan_autotune", "dg_fp64_fma_probe", "dg_wait_probe",
                     "dg_last_error",
                     "dg_abi_version")
 
@@ -139,6 +139,8 @@ def lib() -> ctypes.CDLL:
     L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, vp]
     L.dg_fp64_fma_probe.restype = ctypes.c_int
+    L.dg_wait_probe.argtypes = [ctypes.POINTER(ctypes.c_int32), vp]
+    L.dg_wait_probe.restype = ctypes.c_int
     L.dg_last_error.argtypes = []
     L.dg_last_error.restype = ctypes.c_char_p
     L.dg_abi_version.argtypes = []

@@ -102,6 +102,15 @@ bool overlap2(const void* a, int64_t na, const void* b, int64_t nb) {
   return x < y + nb && y < x + na;
 }
 
+// one thread waits on an mbarrier whose single expected arrival never comes
+__global__ void wait_probe_kernel(int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    dg::mbar_init(&bar, 1);
+    if (!dg::mbar_wait_bounded(&bar, 0)) dg::raise_status(status, DG_ERR_TIMEOUT);
+  }
+}
+
 __global__ void fp64_fma_probe_kernel(double* out, int iters) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double v[8];
@@ -1130,6 +1139,25 @@ int dg_plan_destroy(dg_plan* p) {
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
+  return DG_OK;
+}
+
+int dg_wait_probe(int32_t* status, void* stream) {
+  if (!status) return fail(DG_ERR_ARGUMENT, "status is NULL");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int* d = nullptr;
+  cudaError_t err = cudaMalloc(&d, sizeof(int));
+  if (err == cudaSuccess) err = cudaMemsetAsync(d, 0, sizeof(int), s);
+  if (err == cudaSuccess) {
+    wait_probe_kernel<<<1, 32, 0, s>>>(d);
+    err = cudaGetLastError();
+  }
+  int h = 0;
+  if (err == cudaSuccess) err = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (d) cudaFree(d);
+  if (err != cudaSuccess) return cuda_fail(err, "wait probe");
+  *status = h;
   return DG_OK;
 }
 

@@ -257,6 +257,14 @@ int dg_plan_info(const dg_plan* plan, int64_t* nelements, int32_t* order,
 int dg_fp64_fma_probe(double* out, int64_t iters, int32_t grid, int32_t block,
                       void* stream);
 
+/* Failure-detection check (no counterpart in the reference): one thread
+ * waits on an mbarrier that nothing arrives at, through the same bounded
+ * wait the kernels use (1 s), and reports through *status the code that
+ * wait raises (DG_ERR_TIMEOUT), read back to the host after the launch.
+ * The context stays usable.  Returns DG_OK when the launch and the read
+ * succeeded. */
+int dg_wait_probe(int32_t* status, void* stream);
+
 /* Thread-local message for the last failing call, "" if none. */
 const char* dg_last_error(void);
 
