@@ -512,9 +512,12 @@ def our_arm(args) -> None:
     if world > 1:
         dist.barrier()
     ke = max(1, min(K, 5))
+    e2e_step_ms = []
     t0 = time.perf_counter()
     for _ in range(ke):
-        host_out = e2e_step()
+        ts = time.perf_counter()
+        host_out = e2e_step()   # ends in a synchronous device->host copy
+        e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, dev)
     # sanity: the host result equals the device-resident result
@@ -598,7 +601,8 @@ def our_arm(args) -> None:
                        "scale_divisor": args.scale},
             "gflops_suite": world * flops_step / (ms_step * 1e-3) / 1e9,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "host_matches_device": bool(ok)},
+                    "d2h_bytes_per_step": d2h, "host_matches_device": bool(ok),
+                    "step_ms": [round(x, 1) for x in e2e_step_ms]},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clock_info,
