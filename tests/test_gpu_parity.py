@@ -167,3 +167,32 @@ def test_parity_odd_element_count(equation, order, drop):
     for path in ("tc", "shared"):
         got, _ = _gpu_rhs(prob, path)
         assert parity_error(got, ref, scale) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("equation", EQUATIONS)
+@pytest.mark.parametrize("order", (3, 4))
+def test_tc_rk_stage_matches_fma_path(equation, order):
+    """The fused RK stage of the tensor-core kernel (at order 3 its state
+    comes from the prefetched input buffer) against the FP64-FMA kernel, with
+    a nonzero residual, a per-element scale and the unscaled RHS output."""
+    import torch
+
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem(equation, jittered_box_mesh(4), order, seed=11 + order)
+    dm = DeviceMesh(prob.disc, "cuda:0", with_partner=True)
+    q = torch.from_numpy(prob.fields).to("cuda:0")
+    nel = prob.disc.nelements
+    scale = torch.linspace(0.9, 1.1, nel, dtype=torch.float64, device="cuda:0")
+    res0 = torch.rand(q.shape, dtype=q.dtype, device=q.device,
+                      generator=torch.Generator(device=q.device).manual_seed(3))
+    outs = []
+    for prec in ("fp64-tc", "fp64"):
+        plan = DevicePlan(dm, equation, prob.params, prec)
+        assert plan.info()["tensor_cores"] == (prec == "fp64-tc")
+        plan.set_element_scale(scale)
+        res, qo, un = res0.clone(), torch.empty_like(q), torch.empty_like(q)
+        plan.rk_stage(q, qo, res, 0.4, 0.3, 2e-3, rhs_unscaled=un)
+        plan.finish()
+        outs.append((qo, res, un))
+    for a, b in zip(outs[0], outs[1]):
+        assert float(torch.linalg.norm(a - b)) <= FP64_RTOL * float(torch.linalg.norm(b))
