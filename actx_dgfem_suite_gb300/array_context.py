@@ -15,6 +15,7 @@ device, or without the compiled library, raises.
 
 from __future__ import annotations
 
+import weakref
 from typing import Any
 
 import numpy as np
@@ -103,6 +104,45 @@ class CompiledRHS:
         return from_stacked(self.actx, state, res)
 
 
+class PinnedResultPool:
+    """Page-locked host buffers for results, reused by exact size.
+
+    ``take`` returns a new array backed by a free buffer of that byte size
+    (allocating one only when every buffer of that size is in use); when the
+    array and all its views have been garbage-collected, the buffer goes back
+    to the pool.  Page-locking a fresh block costs about as much as copying
+    it several times over, and a copy into freshly allocated pageable memory
+    is limited by first-touch page faults, so steady-state transfers need
+    resident, reused buffers; callers still get independent arrays."""
+
+    def __init__(self, pin: bool = True):
+        self.pin = pin                  # page-locked (False: plain host memory)
+        self._free: dict[int, list[torch.Tensor]] = {}
+        self.allocated_bytes = 0
+
+    def _give(self, nbytes: int, buf: torch.Tensor) -> None:
+        self._free.setdefault(nbytes, []).append(buf)
+
+    def take(self, shape, dtype: torch.dtype) -> tuple[np.ndarray, torch.Tensor]:
+        view_t = torch.empty((), dtype=dtype)
+        nbytes = int(np.prod(shape, dtype=np.int64)) * view_t.element_size()
+        free = self._free.get(nbytes)
+        if free:
+            buf = free.pop()
+        else:
+            buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=self.pin)
+            self.allocated_bytes += nbytes
+        t = buf.view(dtype).view(shape)
+        arr = t.numpy()
+        weakref.finalize(arr, self._give, nbytes, buf)
+        return arr, t
+
+    def release(self) -> None:
+        """Drop the free buffers (buffers of live arrays stay with them)."""
+        self.allocated_bytes -= sum(b.numel() for lst in self._free.values() for b in lst)
+        self._free.clear()
+
+
 class GB300DGArrayContext:
     """Array context running the suite's RHS operators on one GB300."""
 
@@ -120,6 +160,7 @@ class GB300DGArrayContext:
             self.device = torch.device("cuda", torch.cuda.current_device())
         _lib.lib()  # load the kernels now, so a missing library fails here
         self.pinned_results = bool(pinned_results)
+        self.host_pool = PinnedResultPool()
         self.np = _ActxNumpy(self)
         self._meshes: dict[int, DeviceMesh] = {}
 
@@ -139,21 +180,25 @@ class GB300DGArrayContext:
         return map_leaves(x, lambda d: DOFArray(self, [self.from_numpy(np.asarray(a)) for a in d]))
 
     def _host(self, t: torch.Tensor) -> np.ndarray:
-        """A new host array holding ``t``.  Device tensors are copied into
-        page-locked blocks of torch's caching host allocator: a fresh
-        pageable array would be faulted in page by page during the copy
-        (~25 GB/s on a Grace host against ~190 GB/s into resident memory),
-        while a cached block is already resident and returns to the cache
-        when the caller drops the array.  ``pinned_results=False`` keeps
-        plain pageable arrays."""
+        """A new host array holding ``t``.  Device tensors are copied into a
+        page-locked buffer of ``host_pool``: a fresh pageable array would be
+        faulted in page by page during the copy (~25 GB/s on a Grace host
+        against ~190 GB/s into resident memory), and page-locking a fresh
+        block costs more than the copy, so buffers are reused by size and
+        return to the pool when the caller drops the array.
+        ``pinned_results=False`` keeps plain pageable arrays."""
         t = t.detach()
         if not t.is_cuda:
             return t.numpy()
         if not self.pinned_results:
             return t.cpu().numpy()
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        arr, h = self.host_pool.take(tuple(t.shape), t.dtype)
         h.copy_(t)
-        return h.numpy()
+        return arr
+
+    def release_host_buffers(self) -> None:
+        """Return the pool's free page-locked result buffers to the system."""
+        self.host_pool.release()
 
     def to_numpy(self, x):
         if isinstance(x, torch.Tensor):
