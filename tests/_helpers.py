@@ -8,7 +8,7 @@ from actx_dgfem_suite_gb300.discretization import make_discretization
 from actx_dgfem_suite_gb300.equations.common import Problem
 from actx_dgfem_suite_gb300.mesh import TetMesh, generate_box_tet_mesh
 
-#: relative L2 parity bound for the FP64 path (spec tolerance)
+#: relative L2 parity bound for the FP64 path against the CPU oracle
 FP64_RTOL = 1e-12
 
 

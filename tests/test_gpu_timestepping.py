@@ -11,7 +11,7 @@ from tests._helpers import (FP64_RTOL, jittered_box_mesh, make_problem,
 
 pytestmark = pytest.mark.gpu
 
-#: spec bound for the mixed-precision RHS against FP64
+#: relative L2 bound for the mixed-precision RHS against FP64
 MIXED_RTOL = 1e-5
 
 
