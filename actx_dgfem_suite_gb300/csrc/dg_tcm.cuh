@@ -23,8 +23,9 @@
 // (|d| <= 128, exact in FP16): x = 2^(E - 31) sum_i d_i 2^(24 - 8 i).  The ten
 // digit-pair products with i + j <= 3 run as tcgen05.mma kind::f16 (M = 128,
 // N = Np padded to 16, K = 16) into one FP32 tensor-memory accumulator per
-// level l = i + j and phase; each level sum is an integer below 2^23, so the
-// tensor core adds it exactly whatever its internal rounding.  The fold
+// level l = i + j and phase; each level sum is an integer of magnitude at
+// most 2^23 (FP32 holds integers exactly up to 2^24), so the tensor core adds
+// it exactly whatever its internal rounding.  The fold
 // recombines L_0 + 2^-8 L_1 + 2^-16 L_2 + 2^-24 L_3 with three
 // round-to-nearest FP32 operations.  Row scaling with 31 bits keeps the
 // entries of a row that are up to 2^7 below its maximum at FP32's 24-bit
@@ -113,7 +114,7 @@ struct MPlan {
   static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(NB >> 3) << 17) | (8u << 24);
   static_assert(NCOL <= 128, "one 128-row product per tile");
   static_assert(NB >= 16 && NB <= 256, "MMA N range");
-  static_assert(KV <= 128 && KL <= 128, "level sums (4 pairs) below 2^23 need K <= 128");
+  static_assert(KV <= 128 && KL <= 128, "level sums (4 pairs) of at most 2^23 need K <= 128");
   static_assert(TMEM_COLS <= 512, "accumulators fit in tensor memory");
   static_assert(SMEM_BYTES <= 227 * 1024, "tile does not fit in shared memory");
 };
