@@ -64,8 +64,8 @@ namespace tcm {
 
 constexpr int r16(int x) { return (x + 15) & ~15; }
 constexpr int p16(int b) { return (b + 15) & ~15; }
-// row pitch (words) >= n with pitch % 8 == 4: 8 elements x 4 nodes of a warp
-// hit 32 distinct banks
+// row pitch (words) >= n with pitch % 8 == 4: a warp's 8 elements x 4 node
+// pairs reach 16 distinct banks with one node of each pair (two lanes per bank)
 constexpr int pitch_q(int n) { return ((n + 3) / 8) * 8 + 4; }
 constexpr int pow2_cols(int c) {
   return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
