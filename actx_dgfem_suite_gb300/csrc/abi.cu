@@ -562,7 +562,7 @@ extern "C" {
 
 const char* dg_last_error(void) { return g_last_error.c_str(); }
 
-int32_t dg_abi_version(void) { return 2; }
+int32_t dg_abi_version(void) { return 3; }
 
 int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,

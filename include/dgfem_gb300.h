@@ -268,7 +268,8 @@ int dg_wait_probe(int32_t* status, void* stream);
 /* Thread-local message for the last failing call, "" if none. */
 const char* dg_last_error(void);
 
-/* ABI version, bumped on any incompatible change. */
+/* ABI version, bumped on any incompatible change (3: dg_plan_autotune
+ * writes 5 floats to ms_per_variant, variant 4 added). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus
