@@ -12,6 +12,9 @@ from pathlib import Path
 _LIB_PATH = Path(__file__).resolve().parent / "libdgfem_gb300.so"
 _lib = None
 
+#: ABI version this binding is written for (dg_abi_version() of the library)
+ABI_VERSION = 4
+
 DG_OK = 0
 DG_ERR_ARGUMENT = 1
 DG_ERR_UNSUPPORTED = 2
@@ -33,7 +36,8 @@ EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc", "dg_rhs_vjp",
                     "dg_box_mesh_build",
                     "dg_plan_path", "dg_plan_info", "dg_plan_set_variant",
-                    "dg_plan_autotune", "dg_fp64_fma_probe", "dg_wait_probe",
+                    "dg_plan_autotune", "dg_plan_autotune_bounded",
+                    "dg_fp64_fma_probe", "dg_wait_probe",
                     "dg_last_error",
                     "dg_abi_version")
 
@@ -90,17 +94,27 @@ def lib() -> ctypes.CDLL:
     if _lib is not None:
         return _lib
     from actx_dgfem_suite_gb300.csrc import build as _build
+    rebuild_error = None
     if _build.is_stale():
         try:
             _build.build()
-        except Exception as exc:  # no nvcc: fall through to the load error
+        except Exception as exc:  # no nvcc: the version check below decides
             if not _LIB_PATH.exists():
                 raise RuntimeError(
                     f"{_LIB_PATH.name} is missing and could not be built: {exc}"
                 ) from exc
+            rebuild_error = exc
     if not _LIB_PATH.exists():
         raise RuntimeError(f"{_LIB_PATH} is missing; run __graft_entry__.build()")
     L = ctypes.CDLL(str(_LIB_PATH))
+    L.dg_abi_version.argtypes = []
+    L.dg_abi_version.restype = ctypes.c_int32
+    found = int(L.dg_abi_version())
+    if found != ABI_VERSION:
+        why = f" (rebuilding the stale library failed: {rebuild_error})" if rebuild_error else ""
+        raise RuntimeError(
+            f"{_LIB_PATH.name} has ABI version {found}, this binding needs "
+            f"{ABI_VERSION}{why}; run __graft_entry__.build()")
     vp = ctypes.c_void_p
     L.dg_plan_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int32,
                                  ctypes.c_int32, ctypes.POINTER(MeshDesc),
@@ -135,6 +149,11 @@ def lib() -> ctypes.CDLL:
     L.dg_plan_autotune.argtypes = [vp, vp, vp, ctypes.c_int32, vp, i32p,
                                    ctypes.POINTER(ctypes.c_float)]
     L.dg_plan_autotune.restype = ctypes.c_int
+    L.dg_plan_autotune_bounded.argtypes = [vp, vp, vp, vp, ctypes.c_double,
+                                           ctypes.c_int32, vp, i32p,
+                                           ctypes.POINTER(ctypes.c_float),
+                                           ctypes.POINTER(ctypes.c_double)]
+    L.dg_plan_autotune_bounded.restype = ctypes.c_int
     L.dg_plan_path.restype = ctypes.c_int
     L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, vp]
@@ -143,8 +162,6 @@ def lib() -> ctypes.CDLL:
     L.dg_wait_probe.restype = ctypes.c_int
     L.dg_last_error.argtypes = []
     L.dg_last_error.restype = ctypes.c_char_p
-    L.dg_abi_version.argtypes = []
-    L.dg_abi_version.restype = ctypes.c_int32
     _lib = L
     return L
 

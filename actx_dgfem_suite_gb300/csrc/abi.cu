@@ -111,6 +111,35 @@ __global__ void wait_probe_kernel(int* status) {
   }
 }
 
+// Per block: sum (a - b)^2 and sum b^2 over a grid-stride range, reduced in a
+// fixed order (deterministic); partial[2 * block + {0, 1}].
+constexpr int kNormBlocks = 512;
+__global__ void __launch_bounds__(256) diff_norm_kernel(const double* a, const double* b,
+                                                        int64_t n, double* partial) {
+  __shared__ double s_d[256], s_b[256];
+  double d2 = 0.0, b2 = 0.0;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const double bv = b[k], dv = a[k] - bv;
+    d2 = fma(dv, dv, d2);
+    b2 = fma(bv, bv, b2);
+  }
+  s_d[threadIdx.x] = d2;
+  s_b[threadIdx.x] = b2;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s_d[threadIdx.x] += s_d[threadIdx.x + w];
+      s_b[threadIdx.x] += s_b[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = s_d[0];
+    partial[2 * blockIdx.x + 1] = s_b[0];
+  }
+}
+
 __global__ void fp64_fma_probe_kernel(double* out, int iters) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double v[8];
@@ -562,7 +591,7 @@ extern "C" {
 
 const char* dg_last_error(void) { return g_last_error.c_str(); }
 
-int32_t dg_abi_version(void) { return 3; }
+int32_t dg_abi_version(void) { return 4; }
 
 int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,
@@ -838,22 +867,70 @@ int dg_plan_set_variant(dg_plan* p, int32_t variant) {
   return DG_OK;
 }
 
-int dg_plan_autotune(dg_plan* p, const double* q, double* rhs, int32_t reps,
-                     void* stream, int32_t* chosen, float* ms_per_variant) {
-  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
-  if (!q || !rhs || reps < 1) return fail(DG_ERR_ARGUMENT, "bad autotune arguments");
+}  // extern "C"
+
+namespace {
+
+// Relative L2 distance ||a - b|| / ||b|| of two device arrays of n doubles
+// (deterministic: fixed grid, fixed-order block and host sums).
+int rel_l2_device(const double* a, const double* b, int64_t n, cudaStream_t s,
+                  double* out) {
+  double* d_part = nullptr;
+  cudaError_t err = cudaMalloc(&d_part, 2 * kNormBlocks * sizeof(double));
+  std::vector<double> part(2 * kNormBlocks, 0.0);
+  if (err == cudaSuccess) {
+    diff_norm_kernel<<<kNormBlocks, 256, 0, s>>>(a, b, n, d_part);
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(part.data(), d_part, part.size() * sizeof(double),
+                          cudaMemcpyDeviceToHost, s);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  if (d_part) cudaFree(d_part);
+  if (err != cudaSuccess) return cuda_fail(err, "autotune error check");
+  double d2 = 0.0, b2 = 0.0;
+  for (int k = 0; k < kNormBlocks; ++k) {
+    d2 += part[2 * k];
+    b2 += part[2 * k + 1];
+  }
+  *out = b2 > 0.0 ? std::sqrt(d2 / b2) : std::sqrt(d2);
+  return DG_OK;
+}
+
+// Read and clear the plan's device status word (after the stream drained).
+int take_status(dg_plan* p, cudaStream_t s, int* status) {
+  cudaError_t err = cudaStreamSynchronize(s);
+  if (err == cudaSuccess)
+    err = cudaMemcpy(status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (err == cudaSuccess && *status != 0) err = cudaMemset(p->d_status, 0, sizeof(int));
+  if (err != cudaSuccess) return cuda_fail(err, "status read");
+  return DG_OK;
+}
+
+// Shared by dg_plan_autotune and dg_plan_autotune_bounded: time every
+// supported variant; a variant whose launches raised a device status
+// (timeout, bad index) is dropped and reported as -1; with `ref`, a
+// variant whose result differs from ref by more than max_rel_l2 (relative
+// L2) is not chosen unless none meets the bound, in which case the most
+// accurate variant is kept.
+int autotune_impl(dg_plan* p, const double* q, double* rhs, const double* ref,
+                  double max_rel_l2, int32_t reps, void* stream, int32_t* chosen,
+                  float* ms_per_variant, double* err_per_variant) {
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int nvar = p->tc ? 1 : (p->tcm ? 5 : 4);
+  const int64_t n = (int64_t)p->nfields * p->nel * p->np;
   cudaEvent_t e0, e1;
   cudaError_t err = cudaEventCreate(&e0);
   if (err == cudaSuccess) err = cudaEventCreate(&e1);
   if (err != cudaSuccess) return cuda_fail(err, "autotune events");
   const int saved = p->variant;
-  int best = -1;
+  int best = -1, best_acc = -1, first_status = 0;
   float best_ms = 0.f;
+  double best_err = 0.0;
   int code = DG_OK;
   for (int v = 0; v < 5 && code == DG_OK; ++v) {
     float ms = -1.f;
+    double rel = -1.0;
     if (v < nvar && ((v & 1) == 0 || p->precision == DG_FP32_MIXED)) {
       p->variant = v;
       code = dg_rhs(p, q, rhs, stream);  // warm-up
@@ -864,21 +941,63 @@ int dg_plan_autotune(dg_plan* p, const double* q, double* rhs, int32_t reps,
       if (code == DG_OK && err == cudaSuccess) err = cudaEventSynchronize(e1);
       if (code == DG_OK && err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
       if (code == DG_OK && err != cudaSuccess) code = cuda_fail(err, "autotune timing");
-      if (code == DG_OK) {
+      int status = 0;
+      if (code == DG_OK) code = take_status(p, s, &status);
+      if (code == DG_OK && status != 0) {  // the variant failed on the device
+        if (!first_status) first_status = status;
+        ms = -1.f;
+      } else if (code == DG_OK) {
         ms /= (float)reps;
-        if (best < 0 || ms < best_ms) {
+        if (ref) code = rel_l2_device(rhs, ref, n, s, &rel);
+      }
+      if (code == DG_OK && ms >= 0.f) {
+        const bool within = !ref || rel <= max_rel_l2;
+        if (within && (best < 0 || ms < best_ms)) {
           best = v;
           best_ms = ms;
+        }
+        if (ref && (best_acc < 0 || rel < best_err)) {
+          best_acc = v;
+          best_err = rel;
         }
       }
     }
     if (ms_per_variant) ms_per_variant[v] = ms;
+    if (err_per_variant) err_per_variant[v] = rel;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (best < 0) best = best_acc;
   p->variant = code == DG_OK && best >= 0 ? best : saved;
   if (chosen) *chosen = p->variant;
+  if (code == DG_OK && best < 0 && first_status)
+    return fail(first_status, "every autotuned variant raised a device-side error");
   return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dg_plan_autotune(dg_plan* p, const double* q, double* rhs, int32_t reps,
+                     void* stream, int32_t* chosen, float* ms_per_variant) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!q || !rhs || reps < 1) return fail(DG_ERR_ARGUMENT, "bad autotune arguments");
+  return autotune_impl(p, q, rhs, nullptr, 0.0, reps, stream, chosen, ms_per_variant,
+                       nullptr);
+}
+
+int dg_plan_autotune_bounded(dg_plan* p, const double* q, double* rhs,
+                             const double* ref, double max_rel_l2, int32_t reps,
+                             void* stream, int32_t* chosen, float* ms_per_variant,
+                             double* err_per_variant) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!q || !rhs || !ref || reps < 1 || !(max_rel_l2 >= 0.0))
+    return fail(DG_ERR_ARGUMENT, "bad autotune arguments");
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  if (overlap(ref, rhs, bytes)) return fail(DG_ERR_ARGUMENT, "ref and rhs overlap");
+  return autotune_impl(p, q, rhs, ref, max_rel_l2, reps, stream, chosen, ms_per_variant,
+                       err_per_variant);
 }
 
 int dg_plan_set_element_scale(dg_plan* p, const double* scale) {
@@ -1065,18 +1184,44 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
+// the scratch's device address per device, and the context it belongs to
 double* g_noalloc_addr[kMaxDevices] = {};
+void* g_noalloc_ctx[kMaxDevices] = {};
 
-// Device address of the static scratch on `device` (which must be current),
-// looked up on the first call for that device and cached.
+// The calling thread's current CUDA context (driver handle), or NULL.  The
+// driver entry point is looked up through the runtime, so the library does
+// not link libcuda directly.
+void* current_context() {
+  using CtxGetCurrent = int (*)(void**);
+  static CtxGetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrent>(f);
+  }();
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
+
+// Device address of the static scratch on `device` (which must be current).
+// The address belongs to the context it was looked up in: a context that is
+// destroyed and created again (cudaDeviceReset) loads the library's device
+// code anew, possibly elsewhere, so the cache is keyed by the current
+// context and looked up again when that changes.
 int noalloc_scratch(int device, double** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[device]) {
+  void* ctx = current_context();
+  if (!g_noalloc_addr[device] || !ctx || ctx != g_noalloc_ctx[device]) {
     void* ptr = nullptr;
     cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (err != cudaSuccess)
       return cuda_fail(err, "looking up the static adjoint scratch");
     g_noalloc_addr[device] = static_cast<double*>(ptr);
+    g_noalloc_ctx[device] = current_context();  // current once the lookup ran
   }
   *out = g_noalloc_addr[device];
   return DG_OK;

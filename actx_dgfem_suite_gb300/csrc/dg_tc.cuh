@@ -52,6 +52,7 @@
 #include <type_traits>
 
 #include "dg_face.cuh"
+#include "dg_ledger.h"
 #include "dg_rhs.cuh"
 
 namespace dg {
@@ -516,7 +517,10 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
-  uint32_t mma_phase = 0;
+  // barriers 0: products, 1 + b: input buffer b (PREFETCH)
+  constexpr int kMma = 0, kIn0 = 1;
+  AsyncLedger<3> led;
+  led.init();
 
   const uint32_t ops_s = smem_u32(smem + P::SM_OPS);
   const int* rexp_v = reinterpret_cast<const int*>(smem + P::SM_OPS + P::OPS_GV + GV::DIGITS);
@@ -527,16 +531,23 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
   double* sR2 = reinterpret_cast<double*>(smem + P::SM_R2);
   double* sG = reinterpret_cast<double*>(smem + P::SM_GEO);
   int* sExp = reinterpret_cast<int*>(smem + P::SM_EXP);
-  // products of one contraction: issue (thread 0), wait (bounded), fold
-  auto contract = [&](auto gtag, uint32_t a_s, const int* rexp, double* out) {
+  // products of one contraction: issue (thread 0), wait (bounded), fold.
+  // false (uniformly) when some thread's wait gave up: the CTA then stops
+  // reading tensor memory and leaves its tile loop
+  auto contract = [&](auto gtag, uint32_t a_s, const int* rexp, double* out) -> bool {
     using G = decltype(gtag);
-    if (t == 0) tc::issue_products<G>(a_s, sR1_s, tmem, &mma_bar);
-    if (!mbar_wait_bounded(&mma_bar, mma_phase)) raise_status(a.status, DG_ERR_TIMEOUT);
-    mma_phase ^= 1u;
+    if (t == 0) {
+      tc::issue_products<G>(a_s, sR1_s, tmem, &mma_bar);
+      led.issue(kMma);
+    }
+    const bool ok = led.complete(kMma, mbar_wait_bounded(&mma_bar, led.phase[kMma]));
+    if (!ok) raise_status(a.status, DG_ERR_TIMEOUT);
+    if (__syncthreads_or(!ok)) return false;
     tc::tc_fence_after();
     tc::fold_products<G>(tmem, rexp, sExp, out);
     tc::tc_fence_before();
     __syncthreads();
+    return true;
   };
 
   const int el = t / NP;
@@ -562,6 +573,7 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
            ((uintptr_t)(a.flux_in + (k * nel + e0n) * NFPT) & 15u) == 0u;
     if (!ok) return 0;
     unsigned char* buf = smem + P::SM_IN + b * P::IN_BYTES;
+    led.issue(kIn0 + b);
     mbar_arrive_expect_tx(&in_bar[b], (uint32_t)NF * (bq + bf) + bg);
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
@@ -572,7 +584,6 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
     bulk_g2s(buf + P::IN_Q + P::IN_F, a.metric + e0n * 9, bg, &in_bar[b]);
     return 1;
   };
-  uint32_t in_phase[2] = {0u, 0u};
   if constexpr (PF) {
     if (t == 0) in_bulk[0] = blockIdx.x < ntiles ? issue_in(blockIdx.x, 0) : 0;
     __syncthreads();
@@ -598,9 +609,11 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
     }
 
     // {{{ 1. state and metric (PREFETCH: and face values) -> shared memory
+    bool in_ok = true;
     if (PF && in_bulk[ib]) {
-      if (!mbar_wait_bounded(&in_bar[ib], in_phase[ib])) raise_status(a.status, DG_ERR_TIMEOUT);
-      in_phase[ib] ^= 1u;
+      in_ok = led.complete(kIn0 + ib,
+                           mbar_wait_bounded(&in_bar[ib], led.phase[kIn0 + ib]));
+      if (!in_ok) raise_status(a.status, DG_ERR_TIMEOUT);
     } else {
       const double* qk = a.q + e0 * NP;
 #pragma unroll
@@ -619,7 +632,7 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
             sF[k * (E * NFPT) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : 0.0;
       }
     }
-    __syncthreads();
+    if (__syncthreads_or(!in_ok)) break;  // an input copy never arrived
     // }}}
 
     // {{{ 2. pointwise pre-pass (FP64): inputs of the weak divergence
@@ -681,7 +694,7 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
       tc::split_columns<GV>(sR1, sExp, [&](int n, int k) { return sQ[n * NP + k]; });
     }
     __syncthreads();
-    contract(GV{}, ops_s + P::OPS_GV, rexp_v, sR2);
+    if (!contract(GV{}, ops_s + P::OPS_GV, rexp_v, sR2)) break;
     // }}}
 
     // {{{ 5. volume term per node (registers)
@@ -739,7 +752,7 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
     tc::split_columns<GL>(sR1, sExp, [&](int n, int k) { return sF[n * NFPT + k]; });
     __syncthreads();
     double* sL = sR2 + NF * E * NFPT;            // Np x (NF E)
-    contract(GL{}, ops_s + P::OPS_GL, rexp_l, sL);
+    if (!contract(GL{}, ops_s + P::OPS_GL, rexp_l, sL)) break;
     // }}}
 
     // {{{ 8. epilogue: store or fold into the RK stage
@@ -763,6 +776,15 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
     }
     __syncthreads();
     // }}}
+  }
+  // after a wait gave up: before shared and tensor memory are released, the
+  // issuing thread waits (bounded) for the copies and products it still owes.
+  // If one of them never completes, the status already reads DG_ERR_TIMEOUT
+  // and the tensor memory is released with that product outstanding.
+  if (t == 0 && led.owes_any()) {
+    if (led.owes(kMma)) mbar_wait_bounded(&mma_bar, led.phase[kMma]);
+    for (int b = 0; b < 2; ++b)
+      if (led.owes(kIn0 + b)) mbar_wait_bounded(&in_bar[b], led.phase[kIn0 + b]);
   }
   tc::tc_fence_before();
   __syncthreads();

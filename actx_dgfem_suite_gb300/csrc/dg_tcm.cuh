@@ -380,7 +380,8 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = tmem_base;
-  uint32_t mma_phase = 0;
+  AsyncLedger<1> led;  // barrier 0: the tensor-core products
+  led.init();
   const uint32_t a_s = smem_u32(sA);
   const uint32_t b_s = smem_u32(smem + P::SM_OPS);
 
@@ -394,10 +395,12 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
   constexpr int FROUNDS = (EG * FG + NWARP - 1) / NWARP;  // face items per thread
   static_assert(NFPT % 2 == 0, "face points come in pairs");
 
-  auto wait_mma = [&]() {
-    if (!mbar_wait_bounded(&mma_bar, mma_phase)) raise_status(a.status, DG_ERR_TIMEOUT);
-    mma_phase ^= 1u;
+  // bounded wait for the products; false if it gave up
+  auto wait_mma = [&]() -> bool {
+    const bool ok = led.complete(0, mbar_wait_bounded(&mma_bar, led.phase[0]));
+    if (!ok) raise_status(a.status, DG_ERR_TIMEOUT);
     tc::tc_fence_after();
+    return ok;
   };
 
   // metric-combined volume inputs of node j of element e from FP32 values
@@ -540,6 +543,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
       tcm::issue_phase<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V, NB>(a_s, b_s + P::OPS_V,
                                                                        tmem, P::IDESC);
       tc::tc_commit(&mma_bar);
+      led.issue(0);
     }
     float fv[FROUNDS][2][NF];
     int fm[FROUNDS];  // e | fj0 << 8 (fj0 even), or -1
@@ -595,8 +599,8 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
                        (lane >> 3) == 0 && e < E);
       }
     }
-    __syncthreads();  // row maxima of X_L complete
-    wait_mma();       // the volume products have read X
+    const bool vol_ok = wait_mma();        // the volume products have read X
+    if (__syncthreads_or(!vol_ok)) break;  // (and the row maxima of X_L are complete)
 #pragma unroll
     for (int rd = 0; rd < FROUNDS; ++rd) {
       if (fm[rd] < 0) continue;
@@ -614,8 +618,9 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
       tcm::issue_phase<P::KL, P::SBO_L, P::A_SLICE_L, P::B_SLICE_L, NB>(
           a_s, b_s + P::OPS_L, tmem + P::ACC_L, P::IDESC);
       tc::tc_commit(&mma_bar);
+      led.issue(0);
     }
-    wait_mma();
+    if (__syncthreads_or(!wait_mma())) break;  // a wait gave up: leave the tile loop
     // }}}
 
     // {{{ 4. level sums -> staging (warp w reads lanes 32 (w % 4)..), epilogue
@@ -677,6 +682,11 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
     // tensor-memory use follows two barriers
     // }}}
   }
+  // after a wait gave up: the issuing thread waits (bounded) for products it
+  // still owes before the tensor memory is released; if they never complete
+  // the status already reads DG_ERR_TIMEOUT and the memory is released with
+  // them outstanding
+  if (t == 0 && led.owes(0)) mbar_wait_bounded(&mma_bar, led.phase[0]);
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0)

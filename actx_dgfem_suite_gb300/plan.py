@@ -233,19 +233,44 @@ class DevicePlan:
     def set_variant(self, variant: int) -> None:
         _lib.check(self._lib.dg_plan_set_variant(self._handle, int(variant)))
 
-    def autotune(self, q: torch.Tensor, reps: int = 3, stream=None) -> dict:
+    def autotune(self, q: torch.Tensor, reps: int = 3, stream=None,
+                 ref: torch.Tensor | None = None,
+                 max_rel_l2: float | None = None) -> dict:
         """Time the supported launch variants on state ``q`` and keep the
-        fastest; returns ``{"chosen": v, "ms": {variant: ms or None}}``."""
+        fastest; returns ``{"chosen": v, "ms": {variant: ms or None}}``.
+
+        With ``ref`` (a trusted RHS of ``q``, e.g. the FP64 plan's) and
+        ``max_rel_l2``, only variants whose result lies within that relative
+        L2 distance of ``ref`` compete (the most accurate one is kept if none
+        does); the result then also carries ``"rel_l2": {variant: err}``."""
         self._check_tensor(q, "state")
         out = torch.empty_like(q)
         chosen = ctypes.c_int32()
         ms = (ctypes.c_float * 5)()
-        _lib.check(self._lib.dg_plan_autotune(
-            self._handle, ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-            int(reps), _stream_handle(stream), ctypes.byref(chosen), ms))
-        return {"chosen": chosen.value,
-                "ms": {self.VARIANTS[v]: (float(ms[v]) if ms[v] >= 0 else None)
-                       for v in range(5)}}
+        if ref is None:
+            _lib.check(self._lib.dg_plan_autotune(
+                self._handle, ctypes.c_void_p(q.data_ptr()),
+                ctypes.c_void_p(out.data_ptr()), int(reps), _stream_handle(stream),
+                ctypes.byref(chosen), ms))
+            errs = None
+        else:
+            self._check_tensor(ref, "ref")
+            if max_rel_l2 is None:
+                raise ValueError("max_rel_l2 is required with ref")
+            errs = (ctypes.c_double * 5)()
+            _lib.check(self._lib.dg_plan_autotune_bounded(
+                self._handle, ctypes.c_void_p(q.data_ptr()),
+                ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ref.data_ptr()),
+                float(max_rel_l2), int(reps), _stream_handle(stream),
+                ctypes.byref(chosen), ms, errs))
+        res = {"chosen": chosen.value,
+               "ms": {self.VARIANTS[v]: (float(ms[v]) if ms[v] >= 0 else None)
+                      for v in range(5)}}
+        if errs is not None:
+            res["max_rel_l2"] = float(max_rel_l2)
+            res["rel_l2"] = {self.VARIANTS[v]: (float(errs[v]) if errs[v] >= 0 else None)
+                             for v in range(5)}
+        return res
 
     def vjp(self, q: torch.Tensor, x: torch.Tensor, out: torch.Tensor | None = None,
             stream=None) -> torch.Tensor:

@@ -170,6 +170,16 @@ int dg_rhs_vjp(dg_plan* plan, const double* q, const double* x, double* y,
  * rejected with DG_ERR_ARGUMENT.  The plan's device must be current.
  * The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * The address is cached for the CUDA context it was looked up in and looked
+ * up again when the current context changes (a context destroyed by
+ * cudaDeviceReset and created again holds the array elsewhere).
+ * Memory: the 64 MiB are part of the library's device code, so they are
+ * committed on a device when that code is loaded there -- with CUDA's
+ * default lazy module loading at the latest by the first call of this
+ * function (plan creation on a mesh with face_partner loads it too).  A
+ * caller that reserves the rest of the device for its own pool should make
+ * one call (any small wave plan will do) before taking that reservation,
+ * or the first call may fail with DG_ERR_CUDA (out of memory).
  * Nothing in the array needs to start at zero: each call writes every entry
  * it later reads.  All calls share the one array, so calls that overlap on
  * the GPU (concurrent streams) race and must be serialised by the caller. */
@@ -223,12 +233,28 @@ int dg_plan_set_variant(dg_plan* plan, int32_t variant);
  * launches of dg_rhs(q -> rhs) each, CUDA events on `stream`), keep the
  * fastest and report it in *chosen (may be NULL); ms_per_variant (may be
  * NULL) receives 5 floats (variants 0..4), -1 for variants the plan does
- * not support.
+ * not support and for variants whose launches raised a device-side status
+ * (DG_ERR_TIMEOUT, DG_ERR_INDEX; read and cleared after each variant, and
+ * such a variant is never chosen).
  * Writes rhs.  The autotuner of the batched (ensemble) path: the reference
  * fixes its loop-nest tiling in its loopy transforms instead
  * (actx_dgfem_suite/arraycontext/batched_einsum_loop_transforms.py:142). */
 int dg_plan_autotune(dg_plan* plan, const double* q, double* rhs, int32_t reps,
                      void* stream, int32_t* chosen, float* ms_per_variant);
+
+/* dg_plan_autotune under an accuracy bound: `ref` (device, the plan's state
+ * shape) holds a trusted RHS of q, typically the DG_FP64 plan's; after its
+ * timed launches each variant's result is compared with ref, and only
+ * variants with ||rhs - ref|| / ||ref|| <= max_rel_l2 compete on time.  If
+ * none meets the bound, the most accurate variant is kept.  err_per_variant
+ * (may be NULL) receives 5 doubles, -1 where ms_per_variant is -1.  The
+ * reference checks every array context against its numpy context after the
+ * first call (actx_dgfem_suite/run/__main__.py:87-96); this applies such a
+ * tolerance to the choice of kernel. */
+int dg_plan_autotune_bounded(dg_plan* plan, const double* q, double* rhs,
+                             const double* ref, double max_rel_l2, int32_t reps,
+                             void* stream, int32_t* chosen, float* ms_per_variant,
+                             double* err_per_variant);
 
 /* Release the plan's device buffers.  Replaces dropping the compiled program
  * and freeing the memory pool (actx_dgfem_suite/tools/wave_dof_scaling.py:108-126). */
@@ -269,7 +295,8 @@ int dg_wait_probe(int32_t* status, void* stream);
 const char* dg_last_error(void);
 
 /* ABI version, bumped on any incompatible change (3: dg_plan_autotune
- * writes 5 floats to ms_per_variant, variant 4 added). */
+ * writes 5 floats to ms_per_variant, variant 4 added; 4: variants that
+ * raise a device-side status report -1, dg_plan_autotune_bounded added). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus

@@ -74,6 +74,34 @@ def test_autotune_picks_a_supported_variant():
         ref.set_variant(1)
 
 
+def test_bounded_autotune_respects_the_error_budget():
+    """dg_plan_autotune_bounded: every reported error is the variant's true
+    relative L2 distance from the FP64 result, and the chosen variant lies
+    within the budget (or is the most accurate when none does)."""
+    prob, ref, mixed = _plans("wave", 3, seed=2)
+    q = torch.from_numpy(prob.fields).cuda()
+    r64 = ref.rhs(q)
+    ref.finish()
+    names = {v: k for k, v in mixed.VARIANTS.items()}
+    for budget in (1e-3, 0.0):
+        res = mixed.autotune(q, reps=1, ref=r64, max_rel_l2=budget)
+        errs = {names[k]: v for k, v in res["rel_l2"].items() if v is not None}
+        assert set(errs) == {0, 1, 2, 3, 4}
+        for v, e in errs.items():  # the reported errors are the real ones
+            mixed.set_variant(v)
+            got = mixed.rhs(q)
+            true = float(torch.linalg.norm(got - r64) / torch.linalg.norm(r64))
+            assert abs(true - e) <= 1e-3 * true + 1e-15, (v, e, true)
+        inside = [v for v, e in errs.items() if e <= budget]
+        if inside:
+            ms = {names[k]: v for k, v in res["ms"].items() if v is not None}
+            assert res["chosen"] in inside
+            assert ms[res["chosen"]] == min(ms[v] for v in inside)
+        else:  # nothing meets a zero budget: the most accurate is kept
+            assert res["chosen"] == min(errs, key=errs.get)
+    mixed.finish()
+
+
 @pytest.mark.parametrize("equation", ["wave", "euler", "maxwell"])
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
 def test_tcgen05_mixed_matches_fp64(equation, order):
