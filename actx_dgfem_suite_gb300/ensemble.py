@@ -42,11 +42,21 @@ class Ensemble:
     def shape(self):
         return self.plan.shape
 
-    def autotune(self, q: torch.Tensor, reps: int = 3) -> dict:
+    def autotune(self, q: torch.Tensor, reps: int = 3,
+                 max_rel_l2: float | None = None) -> dict:
         """Pick the launch variant of the batched kernel (tensor-core or
-        CUDA-core products, persistent or one-CTA-per-tile grid) by timing
-        it on the ensemble state ``q``; call before :meth:`capture`."""
-        self.tuning = self.plan.autotune(q, reps)
+        CUDA-core products, persistent or one-CTA-per-tile grid, tcgen05) by
+        timing it on the ensemble state ``q``; call before :meth:`capture`.
+        With ``max_rel_l2``, only variants whose result lies within that
+        relative L2 distance of the FP64 RHS of ``q`` (evaluated here by an
+        FP64 plan on the same union mesh) compete."""
+        ref = None
+        if max_rel_l2 is not None:
+            p64 = DevicePlan(self.mesh, self.plan.equation, self.plan.params, "fp64")
+            ref = p64.rhs(q)
+            p64.finish()
+            p64.close()
+        self.tuning = self.plan.autotune(q, reps, ref=ref, max_rel_l2=max_rel_l2)
         return self.tuning
 
     def member(self, x: torch.Tensor, k: int) -> torch.Tensor:

@@ -20,7 +20,7 @@ import json
 
 def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
         reps: int = 10, seed: int = 0, precision: str = "fp32-mixed",
-        device_setup: bool = True) -> dict:
+        device_setup: bool = True, max_rel_l2: float | None = 1e-5) -> dict:
     import time
 
     import numpy as np
@@ -61,7 +61,7 @@ def run(members: int = 64, lo: int = 12, hi: int = 40, order: int = 3,
             p.disc._cache.clear()
     setup_s = time.perf_counter() - t0
 
-    tuning = ens.autotune(q, reps=3)
+    tuning = ens.autotune(q, reps=3, max_rel_l2=max_rel_l2)
     ens.capture(q, out)
     stream = torch.cuda.current_stream()
     for _ in range(3):

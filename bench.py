@@ -45,6 +45,8 @@ CASES = [(eq, p, n) for eq in ("wave", "euler", "maxwell")
          for p, n in ((1, 95), (2, 70), (3, 56), (4, 46))]
 METRIC = "RHS DOF-updates/s (plain FP64, wave+Euler+Maxwell P1-P4 sweep)"
 UNIT = "DOF-updates/s"
+#: relative L2 bound of the mixed-precision results against FP64
+MIXED_RTOL = 1e-5
 WORKLOAD = ("plain FP64 RHS sweep: {wave, euler, maxwell} x P1-P4 on box meshes "
             "of 6 n^3 tets, n = 95/70/56/46; one RHS per case per step")
 
@@ -183,12 +185,24 @@ def fp64_peak_tflops(torch) -> float:
     return best / 1e12
 
 
+def bench_config(args, world: int) -> dict:
+    """The workload description both arms print (the reference arm times a
+    bounded sample of it, described in its ``cpu_baseline.sample``)."""
+    return {"workload": WORKLOAD, "problem": "baseline definitions",
+            "precision": args.precision,
+            "l2": "inputs larger than L2 (every case's state > 129 MB)",
+            "parallelism": f"replicas x{world}",
+            "scale_divisor": args.scale}
+
+
 # {{{ reference arm (CPU oracle)
 
 
 def _oracle_case(args):
-    eq, order, n_sample, reps = args
-    import numpy as np  # noqa: F401
+    """One case of the CPU oracle sweep: (DOF updates, seconds per RHS, and
+    with ``keep`` the oracle's RHS for the parity check)."""
+    eq, order, n_sample, reps, keep = args
+    import numpy as np
 
     from actx_dgfem_suite_gb300.rhs_builder import get_problem
     from oracle.geometry import build_oracle_disc
@@ -200,27 +214,35 @@ def _oracle_case(args):
     t0 = time.perf_counter()
     for _ in range(reps):
         if eq == "wave":
-            wave_rhs(od, q[0], q[1:4], *prob.params)
+            rhs = wave_rhs(od, q[0], q[1:4], *prob.params)
         elif eq == "euler":
-            euler_rhs(od, q, *prob.params)
+            rhs = euler_rhs(od, q, *prob.params)
         else:
-            maxwell_rhs(od, q, *prob.params)
+            rhs = maxwell_rhs(od, q, *prob.params)
     dt = (time.perf_counter() - t0) / reps
-    return prob.nfields * d.nelements * d.np_, dt
+    dofs = prob.nfields * d.nelements * d.np_
+    if not keep:
+        return dofs, dt, None
+    if eq == "wave":
+        rhs = np.concatenate([rhs[0][None], rhs[1]])
+    # the product's nodes must sit at the oracle's (independently built) ones
+    node_err = float(np.max(np.abs(d.nodes() - od.nodes)))
+    return dofs, dt, {"rhs": np.asarray(rhs), "node_err": node_err}
 
 
 def cpu_sample_sizes(scale: int) -> list[int]:
     return [max(2, n // scale) for (_, _, n) in CASES]
 
 
-def run_oracle_sweep(scale: int, reps: int = 1, procs: int | None = None):
-    """Times the oracle on every case at n // scale; returns (dofs, seconds,
-    cores) where seconds is the wall time of the sweep with one process per
-    case."""
+def run_oracle_sweep(scale: int, reps: int = 1, procs: int | None = None,
+                     keep: bool = False):
+    """Times the oracle on every case at n // scale; returns (dofs, wall
+    seconds, busy seconds, cores[, per-case outputs with ``keep``]), one
+    process per case."""
     import multiprocessing as mp
     from concurrent.futures import ProcessPoolExecutor
     sizes = cpu_sample_sizes(scale)
-    jobs = [(eq, p, ns, reps) for (eq, p, _), ns in zip(CASES, sizes)]
+    jobs = [(eq, p, ns, reps, keep) for (eq, p, _), ns in zip(CASES, sizes)]
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
         os.environ[var] = "1"   # one core per worker process
     cores = procs or min(len(jobs), os.cpu_count() or 1)
@@ -231,6 +253,8 @@ def run_oracle_sweep(scale: int, reps: int = 1, procs: int | None = None):
     wall = time.perf_counter() - t0
     dofs = sum(r[0] for r in res)
     busy = sum(r[1] for r in res)
+    if keep:
+        return dofs, wall, busy, cores, [r[2] for r in res]
     return dofs, wall, busy, cores
 
 
@@ -257,8 +281,7 @@ def reference_arm(args) -> None:
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD + " (bounded CPU sample)",
-                   "problem": "baseline definitions"},
+        "config": bench_config(args, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -268,6 +291,34 @@ def reference_arm(args) -> None:
 
 
 # }}}
+
+
+def parity_vs_oracle(actx, scale: int, outs: list) -> dict:
+    """Every benchmark case at the CPU sample's size (n // scale), evaluated
+    through the public API on the GPU (the default FP64 path, and fp64-tc
+    at orders 3-4) and compared with the oracle's RHS from the CPU sweep:
+    relative L2 error per case (bound 1e-12)."""
+    import numpy as np
+
+    from actx_dgfem_suite_gb300.containers import leaves
+    from actx_dgfem_suite_gb300.rhs_builder import get_rhs
+    cases, worst = {}, 0.0
+    for (eq, order, _), ns, o in zip(CASES, cpu_sample_sizes(scale), outs):
+        ref = o["rhs"]
+        rhs, call_args = get_rhs(eq, actx, 3, order, definition="baseline", nel_1d=ns)
+        row = {"n": ns, "node_err": o["node_err"]}
+        for prec in (("fp64", "fp64-tc") if order >= 3 else ("fp64",)):
+            rhs.dg_operator.precision = prec
+            got = np.stack([d[0] for d in leaves(actx.to_numpy(
+                actx.compile(rhs)(*call_args)))])
+            err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+            row["rel_l2" if prec == "fp64" else "rel_l2_fp64_tc"] = err
+            worst = max(worst, err)
+        cases[f"{eq}{order}"] = row
+        del rhs, call_args
+    return {"bound": 1e-12, "max_rel_l2": worst, "ok": bool(worst <= 1e-12),
+            "against": "CPU FP64 oracle (independent reference element), same meshes",
+            "cases": cases}
 
 
 def run_extras(args, runs, actx, K, fp64_ms_per_step, fp64_case_ms) -> dict:
@@ -293,8 +344,10 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step, fp64_case_ms) -> dict:
             op.precision = "fp64"
         outs = [torch.empty_like(r["q"]) for r in runs]
         # the autotuner picks each plan's launch variant (tensor-core or CUDA-core
-        # products, persistent or one-CTA-per-tile grid) on the case's own state
-        tuned = [p.autotune(r["q"], reps=2) for p, r in zip(plans, runs)]
+        # products, persistent or one-CTA-per-tile grid, tcgen05) on the case's
+        # own state, among the variants within MIXED_RTOL of the FP64 result
+        tuned = [p.autotune(r["q"], reps=2, ref=r["out"], max_rel_l2=MIXED_RTOL)
+                 for p, r in zip(plans, runs)]
         for _ in range(2):
             for p, r, o in zip(plans, runs, outs):
                 p.rhs(r["q"], o)
@@ -321,6 +374,9 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step, fp64_case_ms) -> dict:
             "autotuned_variant": {f"{r['eq']}{r['order']}": p.VARIANTS[tu["chosen"]]
                                   for r, p, tu in zip(runs, plans, tuned)},
             "variant_ms": {f"{r['eq']}{r['order']}": tu["ms"] for r, tu in zip(runs, tuned)},
+            "variant_rel_l2": {f"{r['eq']}{r['order']}": tu["rel_l2"]
+                               for r, tu in zip(runs, tuned)},
+            "error_budget": MIXED_RTOL,
             "cases_rel_l2_err_vs_fp64": {f"{r['eq']}{r['order']}": e
                                          for r, e in zip(runs, errs)},
         }
@@ -569,12 +625,15 @@ def our_arm(args) -> None:
     # }}}
 
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        dofs_c, wall, busy, cores = run_oracle_sweep(args.cpu_scale, reps=1)
+        dofs_c, wall, busy, cores, outs = run_oracle_sweep(args.cpu_scale, reps=1,
+                                                           keep=True)
         cpu = {"value": dofs_c / (busy / cores), "unit": UNIT, "cores": cores,
                "kind": "port",
                "sample": (f"CPU FP64 oracle, every case at n // {args.cpu_scale}, "
                           f"one process per case")}
+        parity = parity_vs_oracle(actx, args.cpu_scale, outs)
 
     extras = None
     if rank == 0 and world == 1 and not args.no_extras:
@@ -594,17 +653,14 @@ def our_arm(args) -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (f64 state)" if args.precision == "fp32-mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "problem": "baseline definitions",
-                       "precision": args.precision,
-                       "l2": "inputs larger than L2 (every case's state > 129 MB)",
-                       "parallelism": f"replicas x{world}",
-                       "scale_divisor": args.scale},
+            "config": bench_config(args, world),
             "gflops_suite": world * flops_step / (ms_step * 1e-3) / 1e9,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "host_matches_device": bool(ok),
                     "step_ms": [round(x, 1) for x in e2e_step_ms]},
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clock_info,
             "gpu_launches": K * sum(r["compiled"].plan.launches_per_rhs for r in runs),
             "autotuned_variant": {k: v["chosen"] for k, v in tuned.items()},

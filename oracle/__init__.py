@@ -22,12 +22,17 @@ reference (``.test-conda-env.yml:17-25``) and are absent here; their
 algorithms are restated from their published definitions (nodal DG on
 simplices, Hesthaven & Warburton 2008).
 
-Independence from the product: the reference-element matrices here are
-assembled by quadrature (``oracle.refops``), not by the nodal shortcuts of
-``actx_dgfem_suite_gb300.refelem``; exterior face values are found by matching
-physical node coordinates (``oracle.connectivity``), not through the product's
-gather index.  Only the node set, the PKDO basis evaluation and the mesh are
-shared.
+Independence from the product: no module here imports the product package.
+The reference element is the oracle's own (``oracle.refelem``): GLL points
+from NumPy's Legendre roots, the recursive node family placed from its
+definition (vertices, GLL edge points, centroids, and the order-4
+face-interior nodes in closed form), a monomial basis and collapsed
+Gauss-Legendre quadrature; the matrices are assembled by quadrature
+(``oracle.refops``); exterior face values are found by matching physical node
+coordinates (``oracle.geometry``), not through the product's gather index.
+Only the mesh (vertex coordinates and element vertex lists) and the state
+arrays are inputs shared with the product; the tests check that the product's
+nodes sit at the oracle's node coordinates, in the same order.
 
 Parity status: the reference ships no golden vectors, known-answer tests or
 fixtures for this path (``test/test_dgfem_opt_freeze.py:1-4`` is a

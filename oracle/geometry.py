@@ -19,7 +19,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from actx_dgfem_suite_gb300.refelem import FACE_VERTICES
+from oracle.refelem import FACES as FACE_VERTICES
 from oracle.refops import OracleRefOps, oracle_ref_ops
 
 

@@ -12,8 +12,10 @@ the volume node set, the matrices grudge builds through modepy:
   biunit-triangle parametrisation, ``l_j`` the Lagrange basis on the face
   nodes (``reference_face_mass_matrix``).
 
-Every integral uses a Gauss-Jacobi conical-product rule exact for the
+Every integral uses a collapsed Gauss-Legendre rule exact for the
 integrand's degree, so none relies on the face nodes being volume nodes.
+Nodes, basis and quadrature come from :mod:`oracle.refelem`, which shares no
+code with the product.
 """
 
 from __future__ import annotations
@@ -23,16 +25,15 @@ from functools import lru_cache
 
 import numpy as np
 
-from actx_dgfem_suite_gb300.refelem import (
-    BIUNIT_TET_VERTICES,
-    FACE_VERTICES,
-    face_reference_nodes,
-    pkdo_tet,
-    pkdo_tet_grad_interior,
-    pkdo_tri,
-    tet_quadrature,
-    tri_quadrature,
-    volume_nodes,
+from oracle.refelem import (
+    FACES,
+    TET_VERTICES,
+    modal_basis_grads,
+    modal_basis,
+    tet_nodes,
+    tet_rule,
+    tri_nodes,
+    tri_rule,
 )
 
 
@@ -49,21 +50,26 @@ class OracleRefOps:
 
 @lru_cache(maxsize=None)
 def oracle_ref_ops(order: int) -> OracleRefOps:
-    nodes = volume_nodes(order)
-    vinv = np.linalg.inv(pkdo_tet(order, nodes))
-    q, w = tet_quadrature(order + 2)
-    lag = pkdo_tet(order, q) @ vinv                        # (nq, Np)
-    dlag = np.einsum("rqm,mj->rqj", pkdo_tet_grad_interior(order, q), vinv)
+    nodes = tet_nodes(order)
+    q, w = tet_rule(order + 3)
+    # orthonormalise the modal basis on the tetrahedron (Cholesky factor of
+    # its Gram matrix under the quadrature), which keeps the Vandermonde
+    # matrix well conditioned at order 4
+    bq = modal_basis(order, q)
+    tr = np.linalg.inv(np.linalg.cholesky(np.einsum("q,qm,qn->mn", w, bq, bq))).T
+    vinv = np.linalg.inv(modal_basis(order, nodes) @ tr)
+    lag = bq @ tr @ vinv                                    # (nq, Np)
+    dlag = np.einsum("rqm,mn,nj->rqj", modal_basis_grads(order, q), tr, vinv)
     mass = np.einsum("q,qi,qj->ij", w, lag, lag)
     stiff_t = np.einsum("q,rqi,qj->rij", w, dlag, lag)
     diff = np.einsum("ik,rjk->rij", np.linalg.inv(mass), stiff_t)
 
-    fref = face_reference_nodes(order)                     # (Nfp, 2)
-    v2inv = np.linalg.inv(pkdo_tri(order, fref))
-    q2, w2 = tri_quadrature(order + 2)
-    lag2 = pkdo_tri(order, q2) @ v2inv                      # (nq2, Nfp)
-    # barycentric coordinates of the 2D quadrature points / face nodes
-    def bary2(x2):
+    fref = tri_nodes(order)                                 # (Nfp, 2)
+    v2inv = np.linalg.inv(modal_basis(order, fref))
+    q2, w2 = tri_rule(order + 2)
+    lag2 = modal_basis(order, q2) @ v2inv                     # (nq2, Nfp)
+
+    def bary2(x2):  # biunit-triangle coordinates -> barycentric
         l1 = (x2[:, 0] + 1) / 2
         l2 = (x2[:, 1] + 1) / 2
         return np.stack([1 - l1 - l2, l1, l2], axis=1)
@@ -71,10 +77,10 @@ def oracle_ref_ops(order: int) -> OracleRefOps:
     npn, nfp = nodes.shape[0], fref.shape[0]
     emat = np.zeros((npn, 4, nfp))
     fcoords = np.zeros((4, nfp, 3))
-    for f, fv in enumerate(FACE_VERTICES):
-        fverts = BIUNIT_TET_VERTICES[list(fv)]              # (3, 3)
+    for f, fv in enumerate(FACES):
+        fverts = TET_VERTICES[list(fv)]                     # (3, 3)
         xq = bary2(q2) @ fverts
-        vol_lag = pkdo_tet(order, xq) @ vinv                # (nq2, Np)
+        vol_lag = modal_basis(order, xq) @ tr @ vinv          # (nq2, Np)
         emat[:, f, :] = np.einsum("q,qk,qj->kj", w2, vol_lag, lag2)
         fcoords[f] = bary2(fref) @ fverts
     return OracleRefOps(order=order, nodes=nodes, mass=mass, stiff_t=stiff_t,

@@ -21,6 +21,7 @@ def oracle_rhs(problem: Problem, od=None, parts: bool = False):
     d = problem.disc
     if od is None:
         od = build_oracle_disc(d.mesh.vertices, d.mesh.elements, d.order)
+    check_node_layout(d, od)
     q = problem.fields
     if problem.equation == "wave":
         rhs, vol, surf = wave_rhs(od, q[0], q[1:4], *problem.params, parts=True)
@@ -31,6 +32,18 @@ def oracle_rhs(problem: Problem, od=None, parts: bool = False):
     if parts:
         return rhs, float(np.sqrt(np.linalg.norm(vol) ** 2 + np.linalg.norm(surf) ** 2))
     return rhs
+
+
+def check_node_layout(disc, od) -> None:
+    """The product's volume nodes must sit at the oracle's node coordinates,
+    in the same order: the oracle builds its node set independently, so this
+    pins the product's node family, node order and element geometry before
+    any state in the product's layout is handed to the oracle."""
+    x = disc.nodes()
+    if not isinstance(x, np.ndarray):      # a mesh built on the device
+        x = x.detach().cpu().numpy()
+    err = float(np.max(np.abs(np.asarray(x) - od.nodes)))
+    assert err <= 1e-12, f"product nodes differ from the oracle's by {err:.3e}"
 
 
 def rel_l2(a, b) -> float:

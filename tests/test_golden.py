@@ -13,7 +13,10 @@ def test_oracle_reproduces_fixture(eq, order, n):
     fx = np.load(fixture_path(eq, order, n))
     prob, rhs, scale = compute(eq, order, n)
     assert np.isclose(np.linalg.norm(prob.fields), float(fx["input_l2"]), rtol=1e-14)
-    assert parity_error(rhs, fx["rhs"], float(fx["scale"])) < 1e-14
+    # the fixtures were written by an earlier construction of the oracle's
+    # matrices (orthonormal simplex basis, another quadrature); the current
+    # one agrees with it to round-off (<= 4e-14 at order 4)
+    assert parity_error(rhs, fx["rhs"], float(fx["scale"])) < 1e-13
 
 
 @pytest.mark.gpu

@@ -53,6 +53,38 @@ def test_parity_box(equation, order, definition, path):
 
 
 @pytest.mark.parametrize("equation", EQUATIONS)
+def test_parity_tiny_benchmark_config(equation):
+    """The tiny benchmark configuration as stated: P2 tetrahedra on 6^3 hexes
+    x 6 tets (1296 elements), benchmark definitions (wave: [-1,1]^3,
+    p = exp(-|x|^2/0.1^2), v = 0, upwind, Dirichlet pressure; Euler and
+    Maxwell at the same size).  The public builder and compiled callable with
+    a host state (the default FP64 path and fp64-tc), and every FP64 path
+    through the plans, checked against the oracle."""
+    from actx_dgfem_suite_gb300.array_context import GB300DGArrayContext
+    from actx_dgfem_suite_gb300.containers import leaves
+    from actx_dgfem_suite_gb300.rhs_builder import get_rhs
+    actx = GB300DGArrayContext("cuda:0")
+    rhs, args = get_rhs(equation, actx, 3, 2, definition="baseline", nel_1d=6)
+    prob = rhs.dg_operator.problem
+    assert prob.disc.nelements == 1296 and prob.disc.np_ == 10
+    ref, scale = oracle_rhs(prob, parts=True)
+    for precision in ("fp64", "fp64-tc"):
+        rhs.dg_operator.precision = precision
+        out = actx.to_numpy(actx.compile(rhs)(*args))
+        got = np.stack([d[0] for d in leaves(out)])
+        assert parity_error(got, ref, scale) <= FP64_RTOL, precision
+    for path in PATHS:
+        got, _ = _gpu_rhs(prob, path)
+        assert parity_error(got, ref, scale) <= FP64_RTOL, path
+    if equation == "wave":
+        v = prob.disc.mesh.vertices
+        assert (v.min(), v.max()) == (-1.0, 1.0)
+        x = prob.disc.nodes()
+        assert np.allclose(prob.fields[0], np.exp(-(x ** 2).sum(axis=0) / 0.01))
+        assert not prob.fields[1:].any()
+
+
+@pytest.mark.parametrize("equation", EQUATIONS)
 @pytest.mark.parametrize("order", ORDERS)
 @pytest.mark.parametrize("path", PATHS)
 def test_parity_jittered_mesh(equation, order, path):
