@@ -33,7 +33,8 @@ DG_FP64_TC = 2
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
-                    "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc", "dg_rhs_vjp",
+                    "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
+                    "dg_rhs_adjoint_stage", "dg_rhs_vjp",
                     "dg_box_mesh_build",
                     "dg_plan_path", "dg_plan_info", "dg_plan_set_variant",
                     "dg_plan_autotune", "dg_plan_autotune_bounded",
@@ -129,6 +130,9 @@ def lib() -> ctypes.CDLL:
     L.dg_plan_set_element_scale.restype = ctypes.c_int
     L.dg_rhs_adjoint.argtypes = [vp, vp, vp, vp, vp]
     L.dg_rhs_adjoint.restype = ctypes.c_int
+    L.dg_rhs_adjoint_stage.argtypes = [vp, vp, dbl, vp, vp, vp, vp, dbl, dbl, dbl,
+                                       vp, vp]
+    L.dg_rhs_adjoint_stage.restype = ctypes.c_int
     L.dg_rhs_vjp.argtypes = [vp, vp, vp, vp, vp]
     L.dg_rhs_vjp.restype = ctypes.c_int
     L.dg_rhs_adjoint_noalloc.argtypes = [vp, vp, vp, vp]

@@ -10,10 +10,13 @@ initial state and to ``c_e`` is the discrete adjoint of those steps:
 * the operator transpose ``L^T`` is the hand-written adjoint kernel
   (``dg_rhs_adjoint``: transposed D and LIFT, face-gather transpose as a
   deterministic gather over glued face points);
-* the reverse of one LSRK step needs only the stage residuals of the forward
-  step (the c-gradient term ``<rbar, L q>`` uses ``L q^{s-1} =
-  (r^s - a_s r^{s-1}) / (dt c_e)``), so the reverse sweep recomputes them
-  segment by segment from checkpoints.
+* the reverse of one LSRK step needs only the stage RHS of the forward step
+  before the element scale (``L_1 q^(s)``, for the c-gradient term
+  ``<rbar, L_1 q>``), which the forward stages write as they recompute the
+  step (``rhs_unscaled`` of ``dg_rk_stage``) into buffers allocated once;
+  each reverse stage is one fused pair of launches
+  (``dg_rhs_adjoint_stage``: the transpose, the state-adjoint update, the
+  next residual adjoint and the per-element c-gradient inner products).
 
 Checkpointing (``checkpointing=``):
 
@@ -21,10 +24,10 @@ Checkpointing (``checkpointing=``):
   ``ceil(sqrt(N))`` state slots (:mod:`actx_dgfem_suite_gb300.checkpointing`);
   the forward sweep keeps the states the schedule stores first, the reverse
   sweep recomputes the rest, and each reversed step records its 5 stage
-  residuals only while it is being reversed.  Memory: sqrt(N) + 5 states;
+  RHS only while it is being reversed.  Memory: sqrt(N) + 5 states;
   about three forward steps per reversed step at N = 300.
 * ``"segments"`` (default): states every ``k`` steps, segments replayed once
-  with all their 5 k residuals kept; memory ``N/k + 5k`` states, minimal at
+  with all their 5 k stage RHS kept; memory ``N/k + 5k`` states, minimal at
   ``k = sqrt(N / 5)``; each forward step recomputed exactly once, so the
   reverse sweep costs one forward sweep plus the adjoint operators.  The
   binomial schedule trades about two more forward steps per step for a
@@ -132,16 +135,25 @@ class WaveAdjointSolver:
         shape = self.plan.shape
         self._buf = torch.empty(shape, dtype=torch.float64, device=self.device)
         self._res = torch.zeros(shape, dtype=torch.float64, device=self.device)
+        # the reverse sweep's buffers, allocated once: the stage RHS of the
+        # steps being reversed (a segment, or one step under the binomial
+        # schedule), the residual adjoint and the transpose's scratch
+        nrec = 1 if self.schedule is not None else self.segment
+        self._lq = torch.empty((nrec, 5) + shape, dtype=torch.float64,
+                               device=self.device)
+        self._rbar = torch.empty(shape, dtype=torch.float64, device=self.device)
+        self._yscr = torch.empty(shape, dtype=torch.float64, device=self.device)
         self.stats = {}
 
     # {{{ forward
 
-    def _step(self, q: torch.Tensor, record: list | None = None) -> None:
+    def _step(self, q: torch.Tensor, record: torch.Tensor | None = None) -> None:
+        """One LSRK step of q in place; with ``record`` ((5,) + state shape)
+        each stage also writes its RHS before the element scale there."""
         src, dst = q, self._buf
         for s in range(5):
-            self.plan.rk_stage(src, dst, self._res, RK4A[s], RK4B[s], self.dt)
-            if record is not None:
-                record.append(self._res.clone())
+            self.plan.rk_stage(src, dst, self._res, RK4A[s], RK4B[s], self.dt,
+                               rhs_unscaled=None if record is None else record[s])
             src, dst = dst, src
         q.copy_(src)
 
@@ -165,25 +177,19 @@ class WaveAdjointSolver:
 
     # {{{ reverse
 
-    def _adjoint_step(self, lam: torch.Tensor, residuals: list, c: torch.Tensor,
+    def _adjoint_step(self, lam: torch.Tensor, lq: torch.Tensor,
                       cbar: torch.Tensor) -> None:
         """lam <- Phi_q^T lam; cbar += Phi_c^T lam for one forward step whose
-        stage residuals r^1..r^5 are ``residuals``."""
-        dt = self.dt
-        rbar = torch.zeros_like(lam)
-        y = torch.empty_like(lam)
-        inv_c = 1.0 / c
+        stages had the RHS ``lq[s]`` (before the element scale).  Each stage is
+        one fused pair of launches (``dg_rhs_adjoint_stage``): with rbar_4 =
+        b_4 lam and rbar_{s-1} = a_s rbar_s + b_{s-1} lam, lam += dt L^T
+        rbar_s and cbar_e += dt <rbar_s, lq[s]>_e."""
+        rbar = self._rbar
         for s in range(4, -1, -1):
-            rbar.add_(lam, alpha=RK4B[s])
-            self.plan.adjoint(rbar, y)
-            # dt <rbar, L q^{s-1}>_e with L q^{s-1} = (r^s - a_s r^{s-1}) / (dt c_e)
-            g = torch.einsum("fen,fen->e", rbar, residuals[s])
-            if s > 0:
-                g.sub_(torch.einsum("fen,fen->e", rbar, residuals[s - 1]),
-                       alpha=RK4A[s])
-            cbar.addcmul_(g, inv_c)
-            lam.add_(y, alpha=dt)
-            rbar.mul_(RK4A[s])
+            x, xscale = (lam, RK4B[4]) if s == 4 else (rbar, 1.0)
+            self.plan.adjoint_stage(x, xscale, lam, rbar if s > 0 else None, lq[s], cbar,
+                                    RK4A[s], RK4B[s - 1] if s > 0 else 0.0, self.dt,
+                                    self._yscr)
 
     def backward(self, grad_traces: torch.Tensor, ckpts: dict, c: torch.Tensor):
         """(dJ/dq0, dJ/dc) for dJ/dtraces = ``grad_traces``."""
@@ -199,11 +205,10 @@ class WaveAdjointSolver:
 
             def reverse_step(q_n, n):
                 q = q_n.clone()
-                rec: list = []
-                self._step(q, rec)
+                self._step(q, self._lq[0])
                 # trace n was sampled after step n, i.e. from q_{n+1}
                 self.rec.inject(lam, grad_traces[n])
-                self._adjoint_step(lam, rec, c, cbar)
+                self._adjoint_step(lam, self._lq[0], cbar)
 
             stored = {k: v for k, v in ckpts.items() if k != 0}
             st: dict = {}
@@ -216,15 +221,12 @@ class WaveAdjointSolver:
         for seg_start in reversed(starts):
             seg_end = min(self.nsteps, seg_start + self.segment)
             q = ckpts[seg_start].clone()
-            records = []
-            for _ in range(seg_start, seg_end):
-                rec: list = []
-                self._step(q, rec)
-                records.append(rec)
+            for n in range(seg_start, seg_end):
+                self._step(q, self._lq[n - seg_start])
             for n in range(seg_end - 1, seg_start - 1, -1):
                 # trace n was sampled after step n, i.e. from q_{n+1}
                 self.rec.inject(lam, grad_traces[n])
-                self._adjoint_step(lam, records[n - seg_start], c, cbar)
+                self._adjoint_step(lam, self._lq[n - seg_start], cbar)
         return lam, cbar
 
     # }}}

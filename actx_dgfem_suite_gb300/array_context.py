@@ -72,16 +72,46 @@ class _ActxNumpy:
 
 
 class CompiledRHS:
-    """``actx.compile(rhs)``: evaluates the RHS through one DevicePlan."""
+    """``actx.compile(rhs)``: evaluates the RHS through one DevicePlan.
+
+    A state held on the host is copied on the context's host-to-device
+    stream into a device buffer owned by this callable (reused by every call
+    whose state is on the host; the copy of call n+1 waits only for the
+    kernel of call n that read the buffer), and the RHS kernel on the current
+    stream waits for that copy alone.  So a caller that issues several calls
+    before reading results back (``to_numpy``) overlaps the copies of one
+    call with the kernels of another.  As with any asynchronous array
+    context, the host state must not change until the call's result has been
+    read or the stream synchronised."""
 
     def __init__(self, actx: GB300DGArrayContext, op):
         self.actx = actx
         self.op = op
         self.plan: DevicePlan = op.plan_for(actx)
+        self._in_buf: torch.Tensor | None = None
+        self._in_free: torch.cuda.Event | None = None  # last read of _in_buf
+
+    def _upload(self, host: torch.Tensor) -> torch.Tensor:
+        dev = self.actx.device
+        cur = torch.cuda.current_stream(dev)
+        if (self._in_buf is None or self._in_buf.shape != host.shape):
+            self._in_buf = torch.empty(host.shape, dtype=torch.float64, device=dev)
+            self._in_free = None
+        h2d = self.actx.h2d_stream
+        if self._in_free is not None:
+            h2d.wait_event(self._in_free)
+        else:
+            h2d.wait_stream(cur)          # the buffer's allocation
+        with torch.cuda.stream(h2d):
+            self._in_buf.copy_(host, non_blocking=True)
+        ready = torch.cuda.Event()
+        ready.record(h2d)
+        cur.wait_event(ready)
+        return self._in_buf
 
     def stage(self, state) -> torch.Tensor:
         """The (nfields, Nel, Np) device tensor holding ``state``; no copy
-        when the state is already a view of such a tensor."""
+        when the state is already a view of such a tensor on the device."""
         lv = leaves(state)
         st = lv[0]._stack
         if (st is not None and st[0].shape[0] == len(lv)
@@ -90,17 +120,24 @@ class CompiledRHS:
             base = st[0]
             if base.device == self.actx.device and base.is_contiguous():
                 return base
-            return base.to(self.actx.device, non_blocking=True)
+            if base.device.type == "cpu":
+                return self._upload(base)
+            return base.to(self.actx.device)
         arrs = [torch.as_tensor(d[0]) for d in lv]
         if all(a.device == self.actx.device for a in arrs):
             return torch.stack(arrs)
-        host = torch.stack([a.cpu() for a in arrs])
-        return host.to(self.actx.device, non_blocking=True)
+        return self._upload(torch.stack([a.cpu() for a in arrs]))
 
     def __call__(self, *args, out: torch.Tensor | None = None):
         state = args[self.op.state_argnum]
         q = self.stage(state)
         res = self.plan.rhs(q, out)
+        cur = torch.cuda.current_stream(self.actx.device)
+        done = torch.cuda.Event()
+        done.record(cur)
+        if q is self._in_buf:
+            self._in_free = done
+        res._dg_ready = done              # what to_numpy waits for
         return from_stacked(self.actx, state, res)
 
 
@@ -163,6 +200,9 @@ class GB300DGArrayContext:
         self.host_pool = PinnedResultPool()
         self.np = _ActxNumpy(self)
         self._meshes: dict[int, DeviceMesh] = {}
+        # copy streams: host states in, results out, beside the compute stream
+        self.h2d_stream = torch.cuda.Stream(self.device)
+        self.d2h_stream = torch.cuda.Stream(self.device)
 
     # {{{ device data
 
@@ -193,7 +233,21 @@ class GB300DGArrayContext:
         if not self.pinned_results:
             return t.cpu().numpy()
         arr, h = self.host_pool.take(tuple(t.shape), t.dtype)
-        h.copy_(t)
+        # the copy runs on the device-to-host stream and waits only for the
+        # kernel that produced t (a compiled call's result), so kernels the
+        # caller issued after it keep running meanwhile
+        d2h = self.d2h_stream
+        ready = getattr(t, "_dg_ready", None)
+        if ready is None and t._base is not None:
+            ready = getattr(t._base, "_dg_ready", None)
+        if ready is not None:
+            d2h.wait_event(ready)
+        else:
+            d2h.wait_stream(torch.cuda.current_stream(t.device))
+        with torch.cuda.stream(d2h):
+            h.copy_(t, non_blocking=True)
+        t.record_stream(d2h)
+        d2h.synchronize()
         return arr
 
     def release_host_buffers(self) -> None:

@@ -1047,6 +1047,59 @@ int dg_rhs_adjoint(dg_plan* p, const double* x, double* y, double* face_scratch,
   return DG_OK;
 }
 
+int dg_rhs_adjoint_stage(dg_plan* p, const double* x, double xscale, double* lam,
+                         double* rbar_out, const double* lq, double* cbar, double a_coef,
+                         double b_coef, double dt, double* y_scratch, void* stream) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!p->d_adj_ops || p->equation != DG_WAVE || !p->split)
+    return fail(DG_ERR_UNSUPPORTED,
+                "the adjoint stage needs an FP64 wave plan on the face-shared path "
+                "(mesh with face_partner)");
+  if (!x || !lam || !y_scratch)
+    return fail(DG_ERR_ARGUMENT, "x, lam or y_scratch is NULL");
+  if ((cbar != nullptr) != (lq != nullptr))
+    return fail(DG_ERR_ARGUMENT, "lq and cbar go together");
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  // x may be lam or rbar_out itself (each node reads before it writes), but no
+  // other overlap is allowed
+  auto bad = [&](const void* u, const void* v) { return u != v && overlap(u, v, bytes); };
+  if (bad(x, lam) || (rbar_out && (bad(x, rbar_out) || overlap(lam, rbar_out, bytes))) ||
+      overlap(y_scratch, x, bytes) || overlap(y_scratch, lam, bytes) ||
+      (rbar_out && overlap(y_scratch, rbar_out, bytes)) ||
+      (lq && (overlap(lq, lam, bytes) || overlap(lq, y_scratch, bytes) ||
+              (rbar_out && overlap(lq, rbar_out, bytes)))) ||
+      (cbar && (overlap2(cbar, p->nel * 8, lam, bytes) ||
+                overlap2(cbar, p->nel * 8, y_scratch, bytes) ||
+                (rbar_out && overlap2(cbar, p->nel * 8, rbar_out, bytes)))))
+    return fail(DG_ERR_ARGUMENT, "adjoint stage arrays overlap");
+  dg::AdjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.x = x;
+  a.y = y_scratch;
+  a.face_scratch = p->d_flux;
+  a.elem_scale = p->elem_scale;
+  a.c = p->params[0];
+  a.metric = p->metric;
+  a.face_geom = p->face_geom;
+  a.face_partner = p->face_partner;
+  a.ops = p->d_adj_ops;
+  a.ops_bytes = p->adj_ops_bytes;
+  a.nel = p->nel;
+  a.status = p->d_status;
+  a.xscale = xscale;
+  a.lam = lam;
+  a.rbar_out = rbar_out;
+  a.lq = lq;
+  a.cbar = cbar;
+  a.rk_a = a_coef;
+  a.rk_b = b_coef;
+  a.dt = dt;
+  cudaError_t err = dg::adjoint_stage_launch_wave(p->order, a, p->adj_grid, p->nsm,
+                                                  reinterpret_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return cuda_fail(err, "adjoint stage launch");
+  return DG_OK;
+}
+
 int dg_rhs_vjp(dg_plan* p, const double* q, const double* x, double* y,
                void* stream) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");

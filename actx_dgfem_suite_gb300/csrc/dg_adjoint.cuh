@@ -22,6 +22,18 @@
 // The plan's scalar wave speed c and an optional per-element scale c_e
 // (variable wave speed, L = c diag(c_e) L_1) are applied to x on load:
 // L^T x = L_1^T (c c_e x).
+//
+// STAGE = true is one stage s of the reverse sweep of a low-storage
+// Runge-Kutta step, fused around the transpose (the forward stage is
+// r^s = a_s r^{s-1} + dt L(q^(s)), q^(s+1) = q^(s) + b_s r^s):
+//   rbar_s   = xscale x                      (the stage's residual adjoint)
+//   lam     += dt L^T rbar_s                 (state adjoint, in place)
+//   rbar_out = a_s rbar_s + b_{s-1} lam      (the next stage's rbar; may alias x)
+//   cbar_e  += dt <rbar_s, lq>_e             (gradient wrt c_e; lq = c L_1 q^(s),
+//                                             the forward stage's RHS before c_e)
+// The volume kernel reduces each element's inner product in a fixed order
+// and the surface kernel applies the epilogue at every node, so the stage is
+// deterministic and needs no atomics.
 #pragma once
 
 #include "dg_rhs.cuh"
@@ -41,6 +53,13 @@ struct AdjArgs {
   uint32_t ops_bytes;
   int64_t nel;
   int* status;
+  // STAGE (fused reverse RK stage) only
+  double xscale;            // rbar_s = xscale x
+  double* lam;              // (4, Nel, Np), updated in place
+  double* rbar_out;         // (4, Nel, Np) or NULL; may be x itself
+  const double* lq;         // (4, Nel, Np) or NULL
+  double* cbar;             // (Nel) or NULL
+  double rk_a, rk_b, dt;
 };
 
 // [W (3 Np Np, [r][i][j]: the forward layout of W^T) | LIFT ([i][fj]) | face_nodes]
@@ -62,10 +81,11 @@ struct AdjTile {
   static constexpr int GEO = AUX + pad16(3 * E * NP * 8);
   static constexpr int FGEO = GEO + pad16(9 * E * 8);
   static constexpr int VN = FGEO + pad16(16 * E * 8);  // n_f . x_v per face, node
-  static constexpr int SMEM_BYTES = VN + pad16(4 * E * NP * 8);
+  static constexpr int PART = VN + pad16(4 * E * NP * 8);  // STAGE: <rbar, lq> per node
+  static constexpr int SMEM_BYTES = PART + pad16(E * NP * 8);
 };
 
-template <int N>
+template <int N, bool STAGE>
 __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a) {
   using T = AdjTile<N>;
   using Ops = AdjOpsLayout<N>;
@@ -80,6 +100,7 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
   double* sG = reinterpret_cast<double*>(smem + T::GEO);
   double* sFG = reinterpret_cast<double*>(smem + T::FGEO);
   double* sVN = reinterpret_cast<double*>(smem + T::VN);
+  double* sPart = reinterpret_cast<double*>(smem + T::PART);
 
   const int t = threadIdx.x;
   if (t == 0) {
@@ -108,16 +129,33 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
     const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
     {
       const double* xk = a.x + e0 * NP;
+      const double* lk = STAGE && a.lq ? a.lq + e0 * NP : nullptr;
       const double* sc_t = a.elem_scale ? a.elem_scale + e0 : nullptr;
+      const double xs = STAGE ? a.xscale : 1.0;
+      double part[(E * NP + kBlock - 1) / kBlock];  // this thread's <rbar, lq> terms
+#pragma unroll
+      for (int r = 0; r < (E * NP + kBlock - 1) / kBlock; ++r) part[r] = 0.0;
 #pragma unroll
       for (int k = 0; k < 4; ++k, xk += nelnp) {
-        for (int rem = t; rem < E * NP; rem += kBlock) {
+#pragma unroll
+        for (int r = 0; r < (E * NP + kBlock - 1) / kBlock; ++r) {
+          const int rem = t + r * kBlock;
+          if (rem >= E * NP) break;
           double v = 0.0;
           if (rem < ecount * NP) {
-            v = a.c * __ldg(xk + rem);
+            const double rb = xs * __ldg(xk + rem);
+            if (lk) part[r] = fma(rb, __ldg(lk + k * nelnp + rem), part[r]);
+            v = a.c * rb;
             if (sc_t) v *= __ldg(sc_t + rem / NP);
           }
           sX[k * (E * NP) + rem] = v;
+        }
+      }
+      if (STAGE && lk) {
+#pragma unroll
+        for (int r = 0; r < (E * NP + kBlock - 1) / kBlock; ++r) {
+          const int rem = t + r * kBlock;
+          if (rem < E * NP) sPart[rem] = part[r];
         }
       }
       const double* mt = a.metric + e0 * 9;
@@ -128,6 +166,12 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
         sFG[idx] = idx < 16 * ecount ? __ldg(ft + idx) : 0.0;
     }
     __syncthreads();
+
+    if (STAGE && a.lq && a.cbar && active && el < ecount && i == 0) {
+      double g = 0.0;  // the element's <rbar_s, lq>, fixed order
+      for (int j = 0; j < NP; ++j) g += sPart[el * NP + j];
+      a.cbar[e0 + el] += a.dt * g;
+    }
 
     if (active && el < ecount) {
       const double* G = sG + el * 9;
@@ -196,10 +240,11 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_volume(const AdjArgs a
   }
 }
 
-// One thread per node: add the transposed flux and face-gather contributions.
+// One thread per node: add the transposed flux and face-gather contributions
+// (STAGE: then the reverse-stage epilogue at every node).
 // Index arithmetic stays in 32 bits (Nel * 4 Nfp < 2^31 is checked on the
 // host): on GB300 wide integer multiplies compete with FP64 for a narrow pipe.
-template <int N>
+template <int N, bool STAGE>
 __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_surface(const AdjArgs a) {
   using Ops = AdjOpsLayout<N>;
   constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
@@ -224,7 +269,7 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_surface(const AdjArgs 
        g += gridDim.x * blockDim.x) {
     const uint32_t e = g / NP;
     const int i = (int)(g - e * NP);
-    if (sNodeFP[i][0] < 0) continue;  // interior node: volume part only
+    if (!STAGE && sNodeFP[i][0] < 0) continue;  // interior node: volume part only
     double yu = yu_p[g], y0 = y0_p[g], y1 = y1_p[g], y2 = y2_p[g];
     const double* sc = a.face_scratch + e * (2 * NFPT);
     const double* fge = a.face_geom + e * 16;
@@ -263,10 +308,29 @@ __global__ void __launch_bounds__(kBlock) dg_wave_adjoint_surface(const AdjArgs 
         raise_status(a.status, DG_ERR_INDEX);
       }
     }
-    yu_p[g] = yu;
-    y0_p[g] = y0;
-    y1_p[g] = y1;
-    y2_p[g] = y2;
+    if constexpr (STAGE) {
+      // read x and lam of this node before writing: rbar_out may be x and x
+      // may be lam (the first reverse stage reads rbar from lam)
+      const double y[4] = {yu, y0, y1, y2};
+      double rb[4], ln[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        rb[k] = a.xscale * a.x[k * nelnp + g];
+        ln[k] = fma(a.dt, y[k], a.lam[k * nelnp + g]);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) a.lam[k * nelnp + g] = ln[k];
+      if (a.rbar_out) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          a.rbar_out[k * nelnp + g] = fma(a.rk_a, rb[k], a.rk_b * ln[k]);
+      }
+    } else {
+      yu_p[g] = yu;
+      y0_p[g] = y0;
+      y1_p[g] = y1;
+      y2_p[g] = y2;
+    }
   }
 }
 

@@ -102,6 +102,10 @@ int set_error(int code, const char* msg);
 cudaError_t adjoint_shape_wave(int order, LaunchShape* out);
 cudaError_t adjoint_launch_wave(int order, const AdjArgs& a, int grid, int nsm,
                                 cudaStream_t s);
+// The same two launches as one fused reverse LSRK stage (AdjArgs' stage
+// fields: lam += dt L^T rbar, next rbar, c-gradient inner products).
+cudaError_t adjoint_stage_launch_wave(int order, const AdjArgs& a, int grid, int nsm,
+                                      cudaStream_t s);
 
 // Mixed-precision Euler: the per-node pressure table (FP64 recovery from
 // total energy, stored as FP32) that the mixed kernels read; one launch

@@ -226,6 +226,30 @@ class DevicePlan:
             ctypes.c_void_p(scratch.data_ptr()), _stream_handle(stream)))
         return out
 
+    def adjoint_stage(self, x: torch.Tensor, xscale: float, lam: torch.Tensor,
+                      rbar_out: torch.Tensor | None, lq: torch.Tensor | None,
+                      cbar: torch.Tensor | None, a: float, b: float, dt: float,
+                      y_scratch: torch.Tensor, stream=None) -> None:
+        """One fused reverse LSRK stage (``dg_rhs_adjoint_stage``):
+        ``lam += dt L^T (xscale x)``; ``rbar_out = a xscale x + b lam``;
+        ``cbar[e] += dt <xscale x, lq>_e``.  ``x`` may be ``lam`` or
+        ``rbar_out`` itself."""
+        for t, name in ((x, "x"), (lam, "lam"), (y_scratch, "y_scratch")):
+            self._check_tensor(t, name)
+        for t, name in ((rbar_out, "rbar_out"), (lq, "lq")):
+            if t is not None:
+                self._check_tensor(t, name)
+        if cbar is not None and (cbar.dtype != torch.float64 or cbar.device != self.mesh.device
+                                 or tuple(cbar.shape) != (self.mesh.nelements,)
+                                 or not cbar.is_contiguous()):
+            raise ValueError("cbar must be a contiguous float64 (Nel,) tensor on the "
+                             "plan's device")
+        ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        _lib.check(self._lib.dg_rhs_adjoint_stage(
+            self._handle, ptr(x), float(xscale), ptr(lam), ptr(rbar_out), ptr(lq),
+            ptr(cbar), float(a), float(b), float(dt), ptr(y_scratch),
+            _stream_handle(stream)))
+
     #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per tile
     VARIANTS = {0: "persistent", 1: "tensor-core, persistent", 2: "one CTA per tile",
                 3: "tensor-core, one CTA per tile", 4: "tcgen05, persistent"}

@@ -135,6 +135,29 @@ int dg_plan_set_element_scale(dg_plan* plan, const double* scale);
 int dg_rhs_adjoint(dg_plan* plan, const double* x, double* y,
                    double* face_scratch, void* stream);
 
+/* One stage of the reverse sweep of a low-storage Runge-Kutta step, fused
+ * around the transpose (FP64 wave plans on the face-shared path).  For the
+ * forward stage r^s = a_s r^{s-1} + dt L(q^(s)), q^(s+1) = q^(s) + b_s r^s
+ * with L = c diag(c_e) L_1 (c_e from dg_plan_set_element_scale), and the
+ * stage's residual adjoint rbar_s = xscale * x:
+ *   lam      += dt L^T rbar_s                        (in place)
+ *   rbar_out  = a * rbar_s + b * lam                 (skipped if NULL)
+ *   cbar[e]  += dt <rbar_s, lq>_e   for every element (skipped if NULL)
+ * where a = a_s, b = b_{s-1} (the next stage's b) and lq = c L_1 q^(s), the
+ * forward stage's RHS before the element scale as dg_rk_stage wrote it to
+ * rhs_unscaled, so that cbar accumulates the gradient with respect to c_e.  x may be lam itself (the
+ * first reverse stage of a step, rbar = b_4 lam: xscale = b_4) and rbar_out
+ * may be x itself; no other arrays may overlap.  y_scratch: device buffer of
+ * nfields * Nel * Np doubles; the plan's face buffers are used too, so do
+ * not run this concurrently with other calls on the plan.  Every sum has a
+ * fixed order: the result is deterministic.  No counterpart in the
+ * reference (which has no adjoint): it is the reverse step of the gradient
+ * of a misfit with respect to the initial state and wave speed. */
+int dg_rhs_adjoint_stage(dg_plan* plan, const double* x, double xscale, double* lam,
+                         double* rbar_out, const double* lq, double* cbar,
+                         double a, double b, double dt, double* y_scratch,
+                         void* stream);
+
 /* Transposed Jacobian of the plan's operator at state q: y = (dL/dq (q))^T x
  * (the vector-Jacobian product; for the linear wave operator, L^T x).
  * FP64 wave and Euler plans on the face-shared path (mesh with
@@ -296,7 +319,8 @@ const char* dg_last_error(void);
 
 /* ABI version, bumped on any incompatible change (3: dg_plan_autotune
  * writes 5 floats to ms_per_variant, variant 4 added; 4: variants that
- * raise a device-side status report -1, dg_plan_autotune_bounded added). */
+ * raise a device-side status report -1, dg_plan_autotune_bounded and
+ * dg_rhs_adjoint_stage added). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus

@@ -2,10 +2,11 @@
 
 Built without any code of the product, so that a wrong node family, node
 order, basis or quadrature in the product cannot hide behind a shared
-implementation:
+implementation, and evaluated in 32-digit arithmetic (mpmath) so that the
+oracle's matrices are exact to FP64 rounding:
 
-* Gauss-Lobatto-Legendre points from NumPy's Legendre module (the roots of
-  P_n'), not from a Newton iteration;
+* Gauss-Lobatto-Legendre points: the roots of P_n' by Newton's method (from
+  NumPy's double-precision roots), in extended precision;
 * volume and face nodes of the recursive family (Isaac, "Recursive,
   parameter-free, explicitly defined interpolation nodes for simplices",
   SIAM J. Sci. Comput. 42(6), 2020), which meshmode's
@@ -35,8 +36,14 @@ from __future__ import annotations
 from functools import lru_cache
 from math import comb
 
+import mpmath
 import numpy as np
 from numpy.polynomial import legendre as npleg
+
+#: working precision of the reference-element construction (decimal digits)
+DPS = 32
+MP = mpmath.MPContext()
+MP.dps = DPS
 
 TET_VERTICES = np.array([[-1.0, -1.0, -1.0], [1.0, -1.0, -1.0],
                          [-1.0, 1.0, -1.0], [-1.0, -1.0, 1.0]])
@@ -44,14 +51,67 @@ TRI_VERTICES = np.array([[-1.0, -1.0], [1.0, -1.0], [-1.0, 1.0]])
 FACES = ((0, 2, 1), (0, 1, 3), (0, 3, 2), (1, 2, 3))
 
 
-def gll_01(n: int) -> np.ndarray:
+# {{{ Legendre polynomials, Gauss and Gauss-Lobatto points (extended precision)
+
+
+def legendre(n: int, x):
+    """(P_n(x), P_n'(x)) by the three-term recurrence (and P_k' = P_{k-2}' +
+    (2k - 1) P_{k-1})."""
+    x = MP.mpf(x)
+    p0, p1 = MP.mpf(1), x
+    d0, d1 = MP.mpf(0), MP.mpf(1)
+    if n == 0:
+        return p0, d0
+    for k in range(2, n + 1):
+        p0, p1 = p1, ((2 * k - 1) * x * p1 - (k - 1) * p0) / k
+        d0, d1 = d1, d0 + (2 * k - 1) * p0
+    return p1, d1
+
+
+def _dlegendre(n: int, x):
+    """(P_n'(x), P_n''(x)) for |x| < 1, from the Legendre equation
+    (1 - x^2) P'' = 2 x P' - n (n + 1) P."""
+    p, d = legendre(n, x)
+    return d, (2 * x * d - n * (n + 1) * p) / (1 - x * x)
+
+
+def _newton(f, x0, iters: int = 60):
+    x = MP.mpf(x0)
+    for _ in range(iters):
+        fx, dfx = f(x)
+        step = fx / dfx
+        x -= step
+        if abs(step) < MP.mpf(10) ** (-DPS + 2):
+            break
+    return x
+
+
+@lru_cache(maxsize=None)
+def gll_01_mp(n: int) -> tuple:
     """The n + 1 Gauss-Lobatto-Legendre points on [0, 1], ascending."""
     if n == 1:
-        return np.array([0.0, 1.0])
-    inner = np.sort(npleg.Legendre.basis(n).deriv().roots().real)
-    x = np.concatenate([[-1.0], inner, [1.0]])
-    x = 0.5 * (x - x[::-1])          # symmetric to round-off
-    return 0.5 * (x + 1.0)
+        return (MP.mpf(0), MP.mpf(1))
+    guess = np.sort(npleg.Legendre.basis(n).deriv().roots().real)
+    inner = [_newton(lambda x: _dlegendre(n, x), g) for g in guess]
+    pts = [MP.mpf(-1)] + inner + [MP.mpf(1)]
+    pts = [(p - q) / 2 for p, q in zip(pts, pts[::-1])]   # exactly symmetric
+    return tuple((p + 1) / 2 for p in pts)
+
+
+def gll_01(n: int) -> np.ndarray:
+    return np.array([float(x) for x in gll_01_mp(n)])
+
+
+@lru_cache(maxsize=None)
+def gauss_01_mp(m: int) -> tuple:
+    """m-point Gauss-Legendre points and weights on [0, 1]."""
+    guess, _ = npleg.leggauss(m)
+    xs = [_newton(lambda x: legendre(m, x), g) for g in guess]
+    ws = [2 / ((1 - x * x) * legendre(m, x)[1] ** 2) for x in xs]
+    return tuple((x + 1) / 2 for x in xs), tuple(w / 2 for w in ws)
+
+
+# }}}
 
 
 def enumerate_nodes(dim: int, order: int) -> list[tuple[int, ...]]:
@@ -69,37 +129,39 @@ def enumerate_nodes(dim: int, order: int) -> list[tuple[int, ...]]:
     return out
 
 
-def _face_interior_211(order: int) -> np.ndarray:
+def _face_interior_211(order: int) -> list:
     """Barycentric coordinates of the recursive node with multi-index
     (2, 1, 1) on a triangle (order 4): the facet projections weighted by
     x_4[n - alpha_i], i.e. (0, 1/2, 1/2) with weight x_4[2] and the two
     order-3 edge nodes ((1 + 5^-1/2)/2 on the vertex with the 2) with weight
     x_4[3] each."""
     assert order == 4
-    x4, x3 = gll_01(4), gll_01(3)
+    x4, x3 = gll_01_mp(4), gll_01_mp(3)
     w0, w1 = x4[2], x4[3]
     a, c = x3[2], x3[1]
-    b = (w0 * np.array([0.0, 0.5, 0.5]) + w1 * np.array([a, 0.0, c])
-         + w1 * np.array([a, c, 0.0]))
-    return b / (w0 + 2 * w1)
+    half = MP.mpf(1) / 2
+    b = [2 * w1 * a, w0 * half + w1 * c, w0 * half + w1 * c]
+    tot = w0 + 2 * w1
+    return [v / tot for v in b]
 
 
-def barycentric_node(alpha: tuple[int, ...]) -> np.ndarray:
-    """Barycentric coordinates of the node with barycentric multi-index
-    ``alpha`` (length 3 or 4, sum N <= 4)."""
+def barycentric_node_mp(alpha: tuple[int, ...]) -> list:
+    """Barycentric coordinates (extended precision) of the node with
+    barycentric multi-index ``alpha`` (length 3 or 4, sum N <= 4)."""
     alpha = tuple(int(a) for a in alpha)
     n = sum(alpha)
     d = len(alpha)
     nz = [k for k in range(d) if alpha[k] > 0]
-    b = np.zeros(d)
+    b = [MP.mpf(0)] * d
     if len(nz) == 1:                       # vertex
-        b[nz[0]] = 1.0
+        b[nz[0]] = MP.mpf(1)
     elif len(nz) == 2:                     # edge: the GLL point
-        g = gll_01(n)
+        g = gll_01_mp(n)
         b[nz[0]] = g[alpha[nz[0]]]
         b[nz[1]] = g[alpha[nz[1]]]
     elif all(alpha[k] == alpha[nz[0]] for k in nz):   # centroid of a face or the volume
-        b[nz] = 1.0 / len(nz)
+        for k in nz:
+            b[k] = MP.mpf(1) / len(nz)
     elif len(nz) == 3 and n == 4:          # order-4 face interior, (2,1,1) up to order
         big = [k for k in nz if alpha[k] == 2][0]
         rest = [k for k in nz if k != big]
@@ -110,60 +172,77 @@ def barycentric_node(alpha: tuple[int, ...]) -> np.ndarray:
     return b
 
 
+def barycentric_node(alpha: tuple[int, ...]) -> np.ndarray:
+    return np.array([float(v) for v in barycentric_node_mp(alpha)])
+
+
+def _to_ref(bary: list, verts: np.ndarray) -> list:
+    dim = verts.shape[1]
+    return [sum(bary[v] * int(verts[v, x]) for v in range(len(bary))) for x in range(dim)]
+
+
+@lru_cache(maxsize=None)
+def tet_nodes_mp(order: int) -> tuple:
+    """Biunit-tetrahedron coordinates of the volume nodes (extended precision)."""
+    return tuple(tuple(_to_ref(barycentric_node_mp((order - sum(m),) + m), TET_VERTICES))
+                 for m in enumerate_nodes(3, order))
+
+
+@lru_cache(maxsize=None)
+def tri_nodes_mp(order: int) -> tuple:
+    """Biunit-triangle coordinates of the face nodes (extended precision)."""
+    return tuple(tuple(_to_ref(barycentric_node_mp((order - sum(m),) + m), TRI_VERTICES))
+                 for m in enumerate_nodes(2, order))
+
+
+def _as_float(pts) -> np.ndarray:
+    out = np.array([[float(v) for v in p] for p in pts])
+    out.setflags(write=False)
+    return out
+
+
 @lru_cache(maxsize=None)
 def tet_nodes(order: int) -> np.ndarray:
     """(Np, 3) biunit-tetrahedron coordinates of the volume nodes."""
-    pts = [barycentric_node((order - sum(m),) + m) for m in enumerate_nodes(3, order)]
-    out = np.array(pts) @ TET_VERTICES
-    out.setflags(write=False)
-    return out
+    return _as_float(tet_nodes_mp(order))
 
 
 @lru_cache(maxsize=None)
 def tri_nodes(order: int) -> np.ndarray:
     """(Nfp, 2) biunit-triangle coordinates of the face nodes."""
-    pts = [barycentric_node((order - sum(m),) + m) for m in enumerate_nodes(2, order)]
-    out = np.array(pts) @ TRI_VERTICES
-    out.setflags(write=False)
-    return out
+    return _as_float(tri_nodes_mp(order))
 
 
 # {{{ a modal basis of P_N: products of Legendre polynomials
 
 
 def _exponents(dim: int, order: int) -> list[tuple[int, ...]]:
-    return enumerate_nodes(dim, order)
-
-
-def _leg(k: int, x: np.ndarray, deriv: int = 0) -> np.ndarray:
-    c = np.zeros(k + 1)
-    c[k] = 1.0
-    if deriv:
-        c = npleg.legder(c, deriv)
-    return npleg.legval(x, c)
-
-
-def modal_basis(order: int, x: np.ndarray) -> np.ndarray:
-    """(npts, nbasis) values of L_a(r) L_b(s) (L_c(t)), a + b (+ c) <= N:
-    the products of Legendre polynomials of total degree <= N span P_N
-    (better conditioned on the biunit simplex than plain modal_basis)."""
-    dim = x.shape[1]
-    ex = _exponents(dim, order)
+    ex = enumerate_nodes(dim, order)
     assert len(ex) == comb(order + dim, dim)
-    return np.stack([np.prod([_leg(e[k], x[:, k]) for k in range(dim)], axis=0)
-                     for e in ex], axis=1)
+    return ex
 
 
-def modal_basis_grads(order: int, x: np.ndarray) -> np.ndarray:
-    """(3, npts, nbasis) derivatives of the tetrahedron basis functions."""
-    ex = _exponents(3, order)
-    out = np.zeros((3, x.shape[0], len(ex)))
-    for m, e in enumerate(ex):
+def modal_basis(order: int, x) -> list:
+    """Rows (one per point) of L_a(r) L_b(s) (L_c(t)), a + b (+ c) <= N, in
+    extended precision: the products of Legendre polynomials of total degree
+    <= N span P_N."""
+    rows = []
+    for p in x:
+        dim = len(p)
+        vals = [[legendre(k, p[d])[0] for k in range(order + 1)] for d in range(dim)]
+        rows.append([MP.fprod(vals[d][e[d]] for d in range(dim))
+                     for e in _exponents(dim, order)])
+    return rows
+
+
+def modal_basis_grads(order: int, x) -> list:
+    """[r][point][basis]: derivatives of the tetrahedron basis functions."""
+    out = [[], [], []]
+    for p in x:
+        v = [[legendre(k, p[d]) for k in range(order + 1)] for d in range(3)]
         for r in range(3):
-            val = np.ones(x.shape[0])
-            for k in range(3):
-                val = val * _leg(e[k], x[:, k], 1 if k == r else 0)
-            out[r, :, m] = val
+            out[r].append([MP.fprod(v[d][e[d]][1 if d == r else 0] for d in range(3))
+                           for e in _exponents(3, order)])
     return out
 
 
@@ -173,38 +252,31 @@ def modal_basis_grads(order: int, x: np.ndarray) -> np.ndarray:
 # {{{ collapsed Gauss-Legendre quadrature
 
 
-def _gl01(m: int):
-    x, w = npleg.leggauss(m)
-    return 0.5 * (x + 1.0), 0.5 * w
-
-
 def tet_rule(m: int):
-    """Points (biunit tetrahedron) and weights; exact for polynomials of
-    degree <= 2 m - 3."""
-    u, wu = _gl01(m)
+    """Points (biunit tetrahedron) and weights, extended precision; exact for
+    polynomials of degree <= 2 m - 3."""
+    u, wu = gauss_01_mp(m)
     pts, wts = [], []
     for a, wa in zip(u, wu):
         for b, wb in zip(u, wu):
             for c, wc in zip(u, wu):
-                x = a
-                y = (1 - a) * b
-                z = (1 - a) * (1 - b) * c
-                pts.append((x, y, z))
-                wts.append(wa * wb * wc * (1 - a) ** 2 * (1 - b))
-    p = np.array(pts)
-    # unit tetrahedron -> biunit: X = -1 + 2 x, Jacobian 8
-    return -1.0 + 2.0 * p, 8.0 * np.array(wts)
+                x, y, z = a, (1 - a) * b, (1 - a) * (1 - b) * c
+                # unit tetrahedron -> biunit: X = -1 + 2 x, Jacobian 8
+                pts.append((2 * x - 1, 2 * y - 1, 2 * z - 1))
+                wts.append(8 * wa * wb * wc * (1 - a) ** 2 * (1 - b))
+    return pts, wts
 
 
 def tri_rule(m: int):
-    """Points (biunit triangle) and weights; exact for degree <= 2 m - 2."""
-    u, wu = _gl01(m)
+    """Points (biunit triangle) and weights, extended precision; exact for
+    degree <= 2 m - 2."""
+    u, wu = gauss_01_mp(m)
     pts, wts = [], []
     for a, wa in zip(u, wu):
         for b, wb in zip(u, wu):
-            pts.append((a, (1 - a) * b))
-            wts.append(wa * wb * (1 - a))
-    return -1.0 + 2.0 * np.array(pts), 4.0 * np.array(wts)
+            pts.append((2 * a - 1, 2 * (1 - a) * b - 1))
+            wts.append(4 * wa * wb * (1 - a))
+    return pts, wts
 
 
 # }}}

@@ -15,7 +15,8 @@ the volume node set, the matrices grudge builds through modepy:
 Every integral uses a collapsed Gauss-Legendre rule exact for the
 integrand's degree, so none relies on the face nodes being volume nodes.
 Nodes, basis and quadrature come from :mod:`oracle.refelem`, which shares no
-code with the product.
+code with the product; the assembly runs in 32-digit arithmetic and rounds
+each matrix to FP64 once.
 """
 
 from __future__ import annotations
@@ -27,12 +28,14 @@ import numpy as np
 
 from oracle.refelem import (
     FACES,
+    MP,
     TET_VERTICES,
-    modal_basis_grads,
     modal_basis,
+    modal_basis_grads,
     tet_nodes,
+    tet_nodes_mp,
     tet_rule,
-    tri_nodes,
+    tri_nodes_mp,
     tri_rule,
 )
 
@@ -48,40 +51,56 @@ class OracleRefOps:
     face_node_coords: np.ndarray  # (4, Nfp, 3) reference coords of face nodes
 
 
+def _mat(rows) -> "MP.matrix":
+    return MP.matrix(rows)
+
+
+def _f64(m) -> np.ndarray:
+    return np.array([[float(m[i, j]) for j in range(m.cols)] for i in range(m.rows)])
+
+
 @lru_cache(maxsize=None)
 def oracle_ref_ops(order: int) -> OracleRefOps:
-    nodes = tet_nodes(order)
-    q, w = tet_rule(order + 3)
-    # orthonormalise the modal basis on the tetrahedron (Cholesky factor of
-    # its Gram matrix under the quadrature), which keeps the Vandermonde
-    # matrix well conditioned at order 4
-    bq = modal_basis(order, q)
-    tr = np.linalg.inv(np.linalg.cholesky(np.einsum("q,qm,qn->mn", w, bq, bq))).T
-    vinv = np.linalg.inv(modal_basis(order, nodes) @ tr)
-    lag = bq @ tr @ vinv                                    # (nq, Np)
-    dlag = np.einsum("rqm,mn,nj->rqj", modal_basis_grads(order, q), tr, vinv)
-    mass = np.einsum("q,qi,qj->ij", w, lag, lag)
-    stiff_t = np.einsum("q,rqi,qj->rij", w, dlag, lag)
-    diff = np.einsum("ik,rjk->rij", np.linalg.inv(mass), stiff_t)
+    """The reference matrices, assembled by quadrature in extended precision
+    (32 digits) and rounded to FP64 once at the end."""
+    nodes_mp = tet_nodes_mp(order)
+    np_ = len(nodes_mp)
+    q, w = tet_rule(order + 2)                               # exact to degree 2N + 1
+    vinv = _mat(modal_basis(order, nodes_mp)) ** -1          # modal -> nodal
+    lag = _mat(modal_basis(order, q)) * vinv                 # (nq, Np)
+    dlag = [_mat(g) * vinv for g in modal_basis_grads(order, q)]
+    nq = len(w)
+    wd = MP.diag(w)
+    mass = lag.T * wd * lag
+    stiff_t = [d.T * wd * lag for d in dlag]                 # ST[r][i][j] = int d_r phi_i phi_j
+    minv = mass ** -1
+    diff = [minv * st.T for st in stiff_t]
 
-    fref = tri_nodes(order)                                 # (Nfp, 2)
-    v2inv = np.linalg.inv(modal_basis(order, fref))
-    q2, w2 = tri_rule(order + 2)
-    lag2 = modal_basis(order, q2) @ v2inv                     # (nq2, Nfp)
+    fref = tri_nodes_mp(order)
+    nfp = len(fref)
+    v2inv = _mat(modal_basis(order, fref)) ** -1
+    q2, w2 = tri_rule(order + 1)                             # exact to degree 2N
+    lag2 = _mat(modal_basis(order, q2)) * v2inv              # (nq2, Nfp)
+    w2d = MP.diag(w2)
 
     def bary2(x2):  # biunit-triangle coordinates -> barycentric
-        l1 = (x2[:, 0] + 1) / 2
-        l2 = (x2[:, 1] + 1) / 2
-        return np.stack([1 - l1 - l2, l1, l2], axis=1)
+        l1, l2 = (x2[0] + 1) / 2, (x2[1] + 1) / 2
+        return (1 - l1 - l2, l1, l2)
 
-    npn, nfp = nodes.shape[0], fref.shape[0]
-    emat = np.zeros((npn, 4, nfp))
+    emat = np.zeros((np_, 4, nfp))
     fcoords = np.zeros((4, nfp, 3))
     for f, fv in enumerate(FACES):
-        fverts = TET_VERTICES[list(fv)]                     # (3, 3)
-        xq = bary2(q2) @ fverts
-        vol_lag = modal_basis(order, xq) @ tr @ vinv          # (nq2, Np)
-        emat[:, f, :] = np.einsum("q,qk,qj->kj", w2, vol_lag, lag2)
-        fcoords[f] = bary2(fref) @ fverts
-    return OracleRefOps(order=order, nodes=nodes, mass=mass, stiff_t=stiff_t,
-                        diff=diff, face_mass=emat, face_node_coords=fcoords)
+        fverts = [[int(v) for v in TET_VERTICES[k]] for k in fv]   # (3, 3)
+
+        def on_face(x2):
+            b = bary2(x2)
+            return tuple(sum(b[k] * fverts[k][x] for k in range(3)) for x in range(3))
+
+        vol_lag = _mat(modal_basis(order, [on_face(x) for x in q2])) * vinv   # (nq2, Np)
+        emat[:, f, :] = _f64(vol_lag.T * w2d * lag2)
+        fcoords[f] = np.array([[float(v) for v in on_face(x)] for x in fref])
+    del nq
+    return OracleRefOps(order=order, nodes=tet_nodes(order), mass=_f64(mass),
+                        stiff_t=np.stack([_f64(st) for st in stiff_t]),
+                        diff=np.stack([_f64(d) for d in diff]), face_mass=emat,
+                        face_node_coords=fcoords)

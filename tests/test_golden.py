@@ -14,8 +14,8 @@ def test_oracle_reproduces_fixture(eq, order, n):
     prob, rhs, scale = compute(eq, order, n)
     assert np.isclose(np.linalg.norm(prob.fields), float(fx["input_l2"]), rtol=1e-14)
     # the fixtures were written by an earlier construction of the oracle's
-    # matrices (orthonormal simplex basis, another quadrature); the current
-    # one agrees with it to round-off (<= 4e-14 at order 4)
+    # matrices (FP64 quadrature over an orthonormal simplex basis); the
+    # current extended-precision one agrees with it to round-off (<= 1.1e-14)
     assert parity_error(rhs, fx["rhs"], float(fx["scale"])) < 1e-13
 
 

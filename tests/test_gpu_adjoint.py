@@ -146,3 +146,39 @@ def test_checkpointing_schemes_agree():
     for gq, gc in grads[1:]:
         assert float(torch.linalg.norm(gq - grads[0][0])) <= 1e-12 * float(torch.linalg.norm(grads[0][0]))
         assert float(torch.linalg.norm(gc - grads[0][1])) <= 1e-12 * float(torch.linalg.norm(grads[0][1]))
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("alias", ["none", "x_is_lam", "rbar_in_place"])
+def test_fused_adjoint_stage_matches_composition(order, alias):
+    """dg_rhs_adjoint_stage == the same stage composed from the plain
+    transpose and elementwise operations: lam += dt L^T rbar, rbar_out =
+    a rbar + b lam, cbar_e += dt <rbar, lq>_e, including the aliasing the
+    reverse sweep uses (x = lam on its first stage, rbar updated in place)."""
+    prob = make_problem("wave", jittered_box_mesh(3), order)
+    plan = _plan(prob.disc, 1.3)
+    g = torch.Generator(device="cuda:0").manual_seed(10 + order)
+    shape, nel = plan.shape, plan.shape[1]
+    rnd = lambda: torch.randn(shape, dtype=torch.float64, device="cuda:0", generator=g)  # noqa: E731
+    c = 0.8 + 0.4 * torch.rand(nel, dtype=torch.float64, device="cuda:0", generator=g)
+    plan.set_element_scale(c)
+    lam, lq = rnd(), rnd()
+    x = lam.clone() if alias == "x_is_lam" else rnd()
+    cbar = torch.rand(nel, dtype=torch.float64, device="cuda:0", generator=g)
+    xscale, a, b, dt = (0.7, -0.4, 0.3, 1e-2)
+    rb = xscale * x
+    lam_ref = lam + dt * plan.adjoint(rb)
+    rbar_ref = a * rb + b * lam_ref
+    cbar_ref = cbar + dt * (rb * lq).sum(dim=(0, 2))
+    ysc = torch.empty_like(x)
+    if alias == "x_is_lam":
+        xin, out = lam, torch.empty_like(x)
+    elif alias == "rbar_in_place":
+        xin = out = x
+    else:
+        xin, out = x, torch.empty_like(x)
+    plan.adjoint_stage(xin, xscale, lam, out, lq, cbar, a, b, dt, ysc)
+    plan.finish()
+    for got, ref in ((lam, lam_ref), (out, rbar_ref), (cbar, cbar_ref)):
+        err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        assert err <= 1e-14, err
