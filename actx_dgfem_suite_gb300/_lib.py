@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_box_mesh_build",
                     "dg_plan_path", "dg_plan_info", "dg_plan_set_variant",
                     "dg_plan_autotune", "dg_plan_autotune_bounded",
-                    "dg_fp64_fma_probe", "dg_wait_probe",
+                    "dg_fp64_fma_probe", "dg_wait_probe", "dg_stream_copy",
                     "dg_last_error",
                     "dg_abi_version")
 
@@ -162,6 +162,8 @@ def lib() -> ctypes.CDLL:
     L.dg_fp64_fma_probe.argtypes = [vp, ctypes.c_int64, ctypes.c_int32,
                                     ctypes.c_int32, vp]
     L.dg_fp64_fma_probe.restype = ctypes.c_int
+    L.dg_stream_copy.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32, vp]
+    L.dg_stream_copy.restype = ctypes.c_int
     L.dg_wait_probe.argtypes = [ctypes.POINTER(ctypes.c_int32), vp]
     L.dg_wait_probe.restype = ctypes.c_int
     L.dg_last_error.argtypes = []

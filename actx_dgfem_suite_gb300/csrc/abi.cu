@@ -140,6 +140,27 @@ __global__ void __launch_bounds__(256) diff_norm_kernel(const double* a, const d
   }
 }
 
+// dst[k] = src[k] for n 16-byte words, grid-stride, one word per thread and
+// step.  Either side may be page-locked host memory: the SMs then load or
+// store it through the unified address space over the CPU-GPU link, without
+// a copy engine.
+__global__ void __launch_bounds__(256) stream_copy_kernel(const uint4* __restrict__ src,
+                                                          uint4* __restrict__ dst,
+                                                          int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // four independent words in flight per thread
+  for (; k + 3 * stride < n; k += 4 * stride) {
+    const uint4 a = src[k], b = src[k + stride], c = src[k + 2 * stride],
+                d = src[k + 3 * stride];
+    dst[k] = a;
+    dst[k + stride] = b;
+    dst[k + 2 * stride] = c;
+    dst[k + 3 * stride] = d;
+  }
+  for (; k < n; k += stride) dst[k] = src[k];
+}
+
 __global__ void fp64_fma_probe_kernel(double* out, int iters) {
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   double v[8];
@@ -1337,6 +1358,43 @@ int dg_plan_destroy(dg_plan* p) {
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
+  return DG_OK;
+}
+
+int dg_stream_copy(void* dst, const void* src, int64_t bytes, int32_t ctas, void* stream) {
+  if (!dst || !src || bytes < 0 || ctas < 1)
+    return fail(DG_ERR_ARGUMENT, "bad stream copy arguments");
+  if ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) |
+       static_cast<uintptr_t>(bytes)) & 15u)
+    return fail(DG_ERR_ARGUMENT, "stream copy needs 16-byte aligned addresses and sizes");
+  if (overlap(dst, src, bytes)) return fail(DG_ERR_ARGUMENT, "source and destination overlap");
+  // both addresses as the device sees them (page-locked host memory must be
+  // mapped into the unified address space)
+  const void* ptrs[2] = {src, dst};
+  void* dev[2] = {nullptr, nullptr};
+  for (int k = 0; k < 2; ++k) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, ptrs[k]) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(DG_ERR_ARGUMENT, "stream copy: unknown pointer");
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+      dev[k] = const_cast<void*>(ptrs[k]);
+    } else if (attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+      dev[k] = attr.devicePointer;
+    } else {
+      return fail(DG_ERR_ARGUMENT,
+                  "stream copy: host memory must be page-locked and mapped");
+    }
+  }
+  if (bytes == 0) return DG_OK;
+  const int64_t n = bytes / 16;
+  const int64_t need = (n + 255) / 256;
+  const int grid = (int)(need < ctas ? (need > 0 ? need : 1) : ctas);
+  stream_copy_kernel<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      static_cast<const uint4*>(dev[0]), static_cast<uint4*>(dev[1]), n);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return cuda_fail(err, "stream copy launch");
   return DG_OK;
 }
 

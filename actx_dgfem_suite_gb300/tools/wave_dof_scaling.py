@@ -20,7 +20,12 @@ GB300_NDOFS = (1_000_000, 5_000_000, 10_000_000, 15_000_000, 20_000_000,
                25_000_000, 27_000_000)
 
 
-def sweep(degrees, ndofs_list, precision: str = "fp64", dim: int = 3):
+def sweep(degrees, ndofs_list, precision: str = "fp64", dim: int = 3,
+          device_setup: bool = False, events: bool = False):
+    """GDOF/s per (degree, DOF budget).  ``device_setup``: build the mesh and
+    initial state on the GPU (``device_problem``) instead of on the host;
+    ``events``: time 3 warm-up and 10 timed RHS with CUDA events instead of
+    the suite's wall-clock protocol (a quick sweep)."""
     import torch
 
     from actx_dgfem_suite_gb300.array_context import GB300DGArrayContext
@@ -33,12 +38,30 @@ def sweep(degrees, ndofs_list, precision: str = "fp64", dim: int = 3):
     for degree in degrees:
         for ndofs in ndofs_list:
             nel_1d = get_nel_1d_for_regular_rect_mesh(dim, degree, int(ndofs))
-            prob = wave_problem(degree, nel_1d, "reference")
+            if device_setup:
+                from actx_dgfem_suite_gb300.device_setup import device_problem
+                prob = device_problem("wave", degree, nel_1d, "reference", actx.device)
+            else:
+                prob = wave_problem(degree, nel_1d, "reference")
             plan = DevicePlan(DeviceMesh(prob.disc, actx.device), "wave",
                               prob.params, precision)
-            q = torch.from_numpy(prob.fields).to(actx.device)
+            q = torch.as_tensor(prob.fields).to(actx.device)
             o = torch.empty_like(q)
             plan.rhs(q, o)
+            actual = get_ndof_for_regular_rect_mesh(dim, degree, nel_1d)
+            if events:
+                for _ in range(3):
+                    plan.rhs(q, o)
+                e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+                e0.record()
+                for _ in range(10):
+                    plan.rhs(q, o)
+                e1.record()
+                plan.finish()
+                out[(degree, ndofs)] = actual * (dim + 1) / (e0.elapsed_time(e1) * 1e-4)
+                del plan, q, o, prob
+                gc.collect()
+                continue
             i_warmup, t_warmup = 0, 0.0
             while i_warmup < 5 and t_warmup < 2:
                 plan.finish()
@@ -56,7 +79,6 @@ def sweep(degrees, ndofs_list, precision: str = "fp64", dim: int = 3):
                 plan.finish()
                 t_rhs += time() - t0
                 i_timing += 3
-            actual = get_ndof_for_regular_rect_mesh(dim, degree, nel_1d)
             out[(degree, ndofs)] = actual * (dim + 1) / (t_rhs / i_timing)
             del plan, q, o, prob
             gc.collect()

@@ -460,6 +460,23 @@ def run_extras(args, runs, actx, K, fp64_ms_per_step, fp64_case_ms) -> dict:
         out["fp64_tcgen05_emulation"] = {"error": repr(exc)}
     torch.cuda.empty_cache()
     # }}}
+    # {{{ DOF-throughput sweep of the wave operator (the reference's
+    # wave_dof_scaling: P1-P4, 1-27 M DOFs per field)
+    try:
+        from actx_dgfem_suite_gb300.tools.wave_dof_scaling import GB300_NDOFS, sweep
+        t0 = time.perf_counter()
+        res = sweep((1, 2, 3, 4), GB300_NDOFS, "fp64", device_setup=True, events=True)
+        out["wave_dof_scaling"] = {
+            "unit": "G DOF-updates/s (4 fields)", "problem": "reference wave definition",
+            "ndofs_per_field": list(GB300_NDOFS),
+            "gdof_s": {f"P{d}": [res[(d, n)] * 1e-9 for n in GB300_NDOFS]
+                       for d in (1, 2, 3, 4)},
+            "timing": "3 warm-up + 10 timed RHS per point, CUDA events",
+            "wall_s": time.perf_counter() - t0}
+    except Exception as exc:
+        out["wave_dof_scaling"] = {"error": repr(exc)}
+    torch.cuda.empty_cache()
+    # }}}
     for name, mod, kw in (
             ("mixed_precision_euler_p3_lsrk45", "bench_mixed", {}),
             ("ensemble_maxwell_p3_64", "bench_ensemble", {"reps": 5}),

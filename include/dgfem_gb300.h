@@ -306,6 +306,15 @@ int dg_plan_info(const dg_plan* plan, int64_t* nelements, int32_t* order,
 int dg_fp64_fma_probe(double* out, int64_t iters, int32_t grid, int32_t block,
                       void* stream);
 
+/* Copy `bytes` from src to dst with the SMs (a streaming kernel of at most
+ * `ctas` CTAs on `stream`) instead of a copy engine.  Either side may be
+ * page-locked, mapped host memory (cudaHostAlloc / pinned tensors), which
+ * the kernel reads or writes over the CPU-GPU link; the array context uses
+ * it to move host states and results.  Addresses and size must be 16-byte
+ * aligned and the ranges must not overlap.  No counterpart in the reference
+ * (its states live in the array context's device memory pool). */
+int dg_stream_copy(void* dst, const void* src, int64_t bytes, int32_t ctas, void* stream);
+
 /* Failure-detection check (no counterpart in the reference): one thread
  * waits on an mbarrier that nothing arrives at, through the same bounded
  * wait the kernels use (1 s), and reports through *status the code that
