@@ -64,10 +64,11 @@ __global__ void __launch_bounds__(kFaceBlock)
     const double m0 = __ldg(qn + 2 * (size_t)nelnp);
     const double m1 = __ldg(qn + 3 * (size_t)nelnp);
     const double m2 = __ldg(qn + 4 * (size_t)nelnp);
-    const double rinv = 1.0 / rho;
-    const double p = (gamma - 1.0) * (en - 0.5 * (m0 * m0 + m1 * m1 + m2 * m2) * rinv);
-    const double ux = m0 * rinv, uy = m1 * rinv, uz = m2 * rinv;
-    const double lam = sqrt(ux * ux + uy * uy + uz * uz) + sqrt(gamma * (p * rinv));
+    const double rinv = rcp64_nr2(rho);
+    const double mm = fma(m0, m0, fma(m1, m1, m2 * m2));
+    const double p = (gamma - 1.0) * fma(-0.5 * mm, rinv, en);
+    // |u| + c = sqrt(|m|^2) / rho + sqrt(gamma p / rho)
+    const double lam = fma(sqrt64_nr(mm), rinv, sqrt64_nr(gamma * (p * rinv)));
     double* an = aux + idx;
     an[0] = p;
     an[nelnp] = rinv;
@@ -128,8 +129,9 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
       }
     }
     // own[k]: value for this face point; part[k]: for the glued face point
-    // (before each side's sJ/J)
+    // (before each side's sJ/J, and with half_scales before a factor 1/2)
     double own[NF], part[NF];
+    bool half_scales = false;
 
     if constexpr (EQ == DG_WAVE) {
       if (bdry) {  // Dirichlet mirror: exterior (-u, v)
@@ -172,26 +174,30 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
         re = __ldg(an + nelnp + gi);
         le = __ldg(an + 2 * (size_t)nelnp + gi);
       }
+      // F(q).n of one side: with m.n first, u.n = (m.n) / rho costs one
+      // product (the velocity itself is not needed here)
       double fn_i[5], fn_e[5];
       auto side = [&](const double* qq, double p, double rinv, double* fn) {
-        const double ux = qq[2] * rinv, uy = qq[3] * rinv, uz = qq[4] * rinv;
-        const double un = ux * nx + uy * ny + uz * nz;
-        fn[0] = qq[2] * nx + qq[3] * ny + qq[4] * nz;
+        const double mn = fma(qq[2], nx, fma(qq[3], ny, qq[4] * nz));
+        const double un = mn * rinv;
+        fn[0] = mn;
         fn[1] = un * (qq[1] + p);
-        fn[2] = qq[2] * un + p * nx;
-        fn[3] = qq[3] * un + p * ny;
-        fn[4] = qq[4] * un + p * nz;
+        fn[2] = fma(qq[2], un, p * nx);
+        fn[3] = fma(qq[3], un, p * ny);
+        fn[4] = fma(qq[4], un, p * nz);
       };
       side(qi, pi, ri, fn_i);
       side(qe, pe, re, fn_e);
-      const double lam = fmax(li, le);
-      const double nn = nx * nx + ny * ny + nz * nz;
+      // f_k = 1/2 (F_i + F_e).n - 1/2 lam (q_e - q_i) n.n = 1/2 t_k; the 1/2
+      // and the sign go into the per-side scale factors below
+      const double lnn = fmax(li, le) * fma(nx, nx, fma(ny, ny, nz * nz));
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        const double fk = 0.5 * (fn_i[k] + fn_e[k]) - 0.5 * lam * (qe[k] - qi[k]) * nn;
-        own[k] = -fk;
-        part[k] = fk;
+        const double tk = fma(-lnn, qe[k] - qi[k], fn_i[k] + fn_e[k]);
+        own[k] = -tk;
+        part[k] = tk;
       }
+      half_scales = true;
     } else {  // DG_MAXWELL
       if (bdry) {  // PEC: exterior (-E, H)
         qe[0] = -qi[0];
@@ -230,13 +236,15 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
       }
     }
 
+    const double so = half_scales ? 0.5 * scale_o : scale_o;
+    const double sp = half_scales ? 0.5 * scale_p : scale_p;
     double* out = a.flux + fp;
 #pragma unroll
-    for (int k = 0; k < NF; ++k, out += nfp_all) out[0] = scale_o * own[k];
+    for (int k = 0; k < NF; ++k, out += nfp_all) out[0] = so * own[k];
     if (pp >= 0) {
       double* outp = a.flux + (uint32_t)pp;
 #pragma unroll
-      for (int k = 0; k < NF; ++k, outp += nfp_all) outp[0] = scale_p * part[k];
+      for (int k = 0; k < NF; ++k, outp += nfp_all) outp[0] = sp * part[k];
     }
   }
 }

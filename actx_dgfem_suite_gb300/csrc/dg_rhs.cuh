@@ -397,22 +397,23 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
           for (int c = 0; c < 3; ++c) m[c] = md[c];
           rinv = rinv_d;
         }
+        // metric-combined fluxes A_k^r = sum_x G[r][x] F_k,x with
+        // F_0 = m, F_1 = u (E + p), F_{2+c} = m_c u + p e_c; through
+        // U_r = (G u)_r: A_0^r = (G m)_r, A_1^r = (E + p) U_r,
+        // A_{2+c}^r = m_c U_r + p G[r][c] (43 operations per node, not 64)
         const Real u[3] = {m[0] * rinv, m[1] * rinv, m[2] * rinv};
-        Real F[5][3];
+        const Real ep = en + p;
 #pragma unroll
-        for (int x = 0; x < 3; ++x) {
-          F[0][x] = m[x];
-          F[1][x] = u[x] * (en + p);
+        for (int r = 0; r < 3; ++r) {
+          const Real* Gr = G + r * 3;
+          const Real ur = fma(Gr[0], u[0], fma(Gr[1], u[1], Gr[2] * u[2]));
+          Real* out = sAux + (r * E + el) * ROW + i;
+          constexpr int KS = 3 * E * ROW;  // stride of k in sAux
+          out[0 * KS] = fma(Gr[0], m[0], fma(Gr[1], m[1], Gr[2] * m[2]));
+          out[1 * KS] = ep * ur;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) F[2 + c][x] = m[c] * u[x] + (c == x ? p : zero);
+          for (int c = 0; c < 3; ++c) out[(2 + c) * KS] = fma(m[c], ur, p * Gr[c]);
         }
-#pragma unroll
-        for (int k = 0; k < 5; ++k)
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-            sAux[((k * 3 + r) * E + el) * ROW + i] =
-                fma(G[r * 3 + 0], F[k][0],
-                    fma(G[r * 3 + 1], F[k][1], G[r * 3 + 2] * F[k][2]));
       }
     }
     if constexpr (T::NAUX > 0) __syncthreads();

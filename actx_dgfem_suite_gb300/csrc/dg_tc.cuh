@@ -658,21 +658,20 @@ __global__ void __launch_bounds__(tc::kTcBlock, 1) dg_rhs_tc_kernel(const RhsArg
         const double en = sQ[(1 * E + el) * NP + i];
         const double m[3] = {sQ[(2 * E + el) * NP + i], sQ[(3 * E + el) * NP + i],
                              sQ[(4 * E + el) * NP + i]};
+        // metric-combined fluxes through U_r = (G u)_r (as in dg_rhs_kernel)
         const double u[3] = {m[0] * rinv, m[1] * rinv, m[2] * rinv};
-        double F[5][3];
+        const double ep = en + p;
 #pragma unroll
-        for (int x = 0; x < 3; ++x) {
-          F[0][x] = m[x];
-          F[1][x] = u[x] * (en + p);
+        for (int r = 0; r < 3; ++r) {
+          const double* Gr = G + r * 3;
+          const double ur = fma(Gr[0], u[0], fma(Gr[1], u[1], Gr[2] * u[2]));
+          double* out = sR2 + (r * E + el) * NP + i;
+          constexpr int KS = 3 * E * NP;  // stride of k in R2
+          out[0 * KS] = fma(Gr[0], m[0], fma(Gr[1], m[1], Gr[2] * m[2]));
+          out[1 * KS] = ep * ur;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) F[2 + c][x] = m[c] * u[x] + (c == x ? p : 0.0);
+          for (int c = 0; c < 3; ++c) out[(2 + c) * KS] = fma(m[c], ur, p * Gr[c]);
         }
-#pragma unroll
-        for (int k = 0; k < 5; ++k)
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-            sR2[((k * 3 + r) * E + el) * NP + i] =
-                fma(G[r * 3 + 0], F[k][0], fma(G[r * 3 + 1], F[k][1], G[r * 3 + 2] * F[k][2]));
       }
     }
     if constexpr (P::NAUX > 0) __syncthreads();
