@@ -451,8 +451,8 @@ uint16_t half_bits(int d) {
   return static_cast<uint16_t>(sign | ((e + 15) << 10) | mant);
 }
 
-// One product's block: A (m x k, element (r, c) = at(r, c)) as 8 FP16 digit
-// slices of its rows' 54-bit fixed-point integers (balanced base-128 digits,
+// One product's block: A (m x k, element (r, c) = at(r, c)) as 7 FP16 digit
+// slices of its rows' 54-bit fixed-point integers (balanced base-256 digits,
 // slice 0 most significant) in the K-major no-swizzle layout of the
 // tensor-core descriptors (element (r, c) at (r/8) SBO + (c/8) 128 + (r%8) 16
 // + (c%8) 2 bytes, SBO = 128 * k-chunks, rows padded to a multiple of 8),
@@ -462,7 +462,7 @@ int pack_gemm(unsigned char* out, int m, int k, At at) {
   const int mr8 = (m + 7) & ~7, kp = r16h(k), kc = kp / 8;
   const int sbo = kc * 128;
   const int slice = (mr8 / 8) * sbo;
-  const int digits = 8 * slice;
+  const int digits = 7 * slice;
   const int bytes = (digits + mr8 * 4 + 15) & ~15;
   if (!out) return bytes;
   std::memset(out, 0, bytes);             // FP16 zero
@@ -476,9 +476,9 @@ int pack_gemm(unsigned char* out, int m, int k, At at) {
     for (int c = 0; c < k; ++c) {
       long long x = std::llrint(std::ldexp(at(r, c), 54 - e));
       const int within = (r / 8) * sbo + (c / 8) * 128 + (r % 8) * 16 + (c % 8) * 2;
-      for (int sl = 7; sl >= 0; --sl) {   // least significant digit first
-        const long long d = ((x + 64) & 127) - 64;
-        x = (x - d) >> 7;
+      for (int sl = 6; sl >= 0; --sl) {   // least significant digit first
+        const long long d = ((x + 128) & 255) - 128;
+        x = (x - d) >> 8;
         const uint16_t h = half_bits(static_cast<int>(d));
         unsigned char* dst = out + sl * slice + within;
         dst[0] = static_cast<unsigned char>(h & 0xff);

@@ -110,41 +110,4 @@ __device__ __forceinline__ double f2d_alu(float f) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
-// FP64 reciprocal of x: the FP32 estimate (converted on
-// the integer ALU) refined by two Newton steps, r <- r + r (1 - x r); each
-// step squares the relative error (2^-23 -> 2^-46 -> below FP64 rounding),
-// so the result is within an ulp or two of 1/x.  Five FP64 instructions
-// instead of the correctly rounded division's longer sequence; callers use it
-// where an ulp does not matter (the Euler node table).  |x| outside
-// [2^-100, 2^100) takes the correctly rounded division.
-// 2^-100 <= |x| < 2^100, tested on the exponent bits (integer ALU)
-__device__ __forceinline__ bool in_f32_range(double x) {
-  const uint32_t e = ((uint32_t)__double2hiint(x) >> 20) & 0x7ffu;
-  return e - 923u < 200u;
-}
-
-__device__ __forceinline__ double rcp64_nr2(double x) {
-  if (!in_f32_range(x)) return 1.0 / x;
-  double r = f2d_alu(__frcp_rn(d2f_alu(x)));
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
-}
-
-// FP64 square root of x >= 0 (0 for x == 0): the FP32 reciprocal square
-// root estimate refined by two Newton steps y <- y (3 - x y^2) / 2, then
-// s = x y corrected once, s <- s + y (x - s^2) / 2; within an ulp or two of
-// sqrt(x).  x outside [2^-100, 2^100) takes the correctly rounded sqrt.
-__device__ __forceinline__ double sqrt64_nr(double x) {
-  if (!(x > 0.0)) return 0.0;
-  if (!in_f32_range(x)) return sqrt(x);
-  double y = f2d_alu(rsqrtf(d2f_alu(x)));
-  const double hx = 0.5 * x;
-  y = y * fma(-hx * y, y, 1.5);
-  y = y * fma(-hx * y, y, 1.5);
-  const double s = x * y;
-  return fma(0.5 * y, fma(-s, s, x), s);
-}
-
 }  // namespace dg

@@ -64,11 +64,11 @@ __global__ void __launch_bounds__(kFaceBlock)
     const double m0 = __ldg(qn + 2 * (size_t)nelnp);
     const double m1 = __ldg(qn + 3 * (size_t)nelnp);
     const double m2 = __ldg(qn + 4 * (size_t)nelnp);
-    const double rinv = rcp64_nr2(rho);
+    const double rinv = 1.0 / rho;
     const double mm = fma(m0, m0, fma(m1, m1, m2 * m2));
     const double p = (gamma - 1.0) * fma(-0.5 * mm, rinv, en);
     // |u| + c = sqrt(|m|^2) / rho + sqrt(gamma p / rho)
-    const double lam = fma(sqrt64_nr(mm), rinv, sqrt64_nr(gamma * (p * rinv)));
+    const double lam = fma(sqrt(mm), rinv, sqrt(gamma * (p * rinv)));
     double* an = aux + idx;
     an[0] = p;
     an[nelnp] = rinv;

@@ -78,7 +78,7 @@ DG_DECLARE_EQ(maxwell)
 // Operator block of the tensor-core kernel (layout of tc::Plan<N, EQ> in
 // dg_tc.cuh): the volume product [A_0; A_1; A_2] (3 Np x Np, wave and
 // maxwell) or [A_0 A_1 A_2] (Np x 3 Np, euler), then LIFT (Np x 4 Nfp).
-// Each: 8 FP16 digit slices in the K-major no-swizzle layout of the tcgen05
+// Each: 7 FP16 digit slices in the K-major no-swizzle layout of the tcgen05
 // descriptors, then one int32 exponent per padded row; blocks padded to 16
 // bytes.  Returns the block size (out == NULL: size only).
 int pack_tc_ops(int eq, int order, const double* diff, const double* lift,

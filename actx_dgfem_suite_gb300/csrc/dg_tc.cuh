@@ -12,19 +12,19 @@
 // per element and field) is evaluated as
 //
 //   A = 2^(e_m - 54) A_int,  X = 2^(e_n - 54) X_int   (per-row / per-column
-//   exponents, 54-bit integers), each integer written as 8 balanced base-128
-//   digits d_1..d_8 in [-64, 64] (exact in FP16);
-//   v_l = sum_{i + j = l} D^A_i D^X_j    for l = 2..9: one tcgen05.mma
+//   exponents, 54-bit integers), each integer written as 7 balanced base-256
+//   digits d_1..d_7 in [-128, 127] (exact in FP16);
+//   v_l = sum_{i + j = l} D^A_i D^X_j    for l = 2..8: one tcgen05.mma
 //   (kind::f16, M = 128, K = 16, FP32 accumulation in tensor memory) per
-//   digit pair and k-step, all pairs of a level accumulating into that
-//   level's tensor-memory columns -- exactly, because |v_l| <= 8 K 64^2 < 2^22
-//   for K <= 112;
-//   C = 2^(e_m + e_n - 31) (G_hi + 2^-28 G_lo),  G_hi = sum_{l<=5} v_l 2^(7(5-l)),
-//   G_lo = sum_{l>=6} v_l 2^(7(9-l)) in 64-bit integers (exact), read out of
+//   digit pair and k-step (28 pairs), all pairs of a level accumulating into
+//   that level's tensor-memory columns -- exactly, because
+//   |v_l| <= 7 K 128^2 < 2^24 for K <= 146;
+//   C = 2^(e_m + e_n - 60) (G_hi 2^32 + G_lo),  G_hi = sum_{l<=4} v_l 2^(8(4-l)),
+//   G_lo = sum_{l>=5} v_l 2^(8(8-l)) in 64-bit integers (exact), read out of
 //   tensor memory with tcgen05.ld.
 //
 // Error: the 54-bit rounding of the inputs (2^-55 of the row or column
-// maximum) and the dropped digit pairs (l > 9, below ~2^-51 K max_k |A_mk|
+// maximum) and the dropped digit pairs (l > 8, below ~2^-51 K max_k |A_mk|
 // max_k |X_kn|) -- the order of FP64's own accumulation error.  Splitting
 // and recombination are integer work (no FP64 pipe): the level sums are
 // folded by 64-bit Horner sums and converted to FP64 with round-to-nearest-
@@ -41,10 +41,11 @@
 // come from dg_face_flux_kernel (and, for Euler, pressure and 1/rho from
 // dg_euler_aux_kernel), pointwise work (Euler fluxes, metric terms, curl,
 // RK epilogue) stays in FP64.  One 512-thread CTA per SM (the order-4
-// operator digits take 126 KB of shared memory); at order 3 the next tile's
-// inputs arrive by 1D TMA bulk copies into a second buffer while the current
-// tile computes.  Orders 3 and 4 (lower orders have too little contraction
-// work for the digit splitting to pay).
+// operator digits take 109 KB of shared memory); where shared memory allows
+// a second input buffer (order 3; wave and Euler at order 4) the next tile's
+// inputs arrive by 1D TMA bulk copies into it while the current tile
+// computes.  Orders 3 and 4 (lower orders have too little contraction work
+// for the digit splitting to pay).
 #pragma once
 
 #include <cuda_fp16.h>
@@ -58,18 +59,18 @@
 namespace dg {
 namespace tc {
 
-constexpr int kS = 8;        // digits per value
-constexpr int kFix = 54;     // fixed-point bits
-constexpr int kLevels = 9;   // digit pairs with i + j <= kLevels are kept
+constexpr int kS = 7;        // digits per value (balanced, base 256)
+constexpr int kFix = 54;     // fixed-point bits (7 balanced base-256 digits hold |x| < 2^54.99)
+constexpr int kLevels = 8;   // digit pairs with i + j <= kLevels are kept
 constexpr int kTcBlock = 512;  // threads per CTA (one CTA per SM)
-static_assert(kLevels == 9, "the recombination folds levels 2..9");
+static_assert(kLevels == 8 && kS == 7, "the split and recombination are base 256, levels 2..8");
 
 constexpr int r16(int x) { return (x + 15) & ~15; }
 constexpr int r8(int x) { return (x + 7) & ~7; }
 constexpr int p16(int bytes) { return (bytes + 15) & ~15; }
 
 // One emulated product: operator A (M x K) times NC data columns of length K.
-//   operator block (global and shared): 8 FP16 digit slices of A in the
+//   operator block (global and shared): 7 FP16 digit slices of A in the
 //   K-major canonical layout (element (m, k) at (m/8) SBO_A + (k/8) 128 +
 //   (m%8) 16 + (k%8) 2 bytes, SBO_A = KP/8 x 128; rows padded to a multiple of
 //   8), then one int32 exponent per padded row;
@@ -93,7 +94,7 @@ struct Gemm {
   // instruction descriptor: D FP32, A and B FP16, both K-major, N, M = 128
   static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(NPAD >> 3) << 17) | (8u << 24);
   static_assert(M <= 128, "one 128-row product per contraction");
-  static_assert(K <= 112, "exact FP32 level sums need K <= 112");
+  static_assert(K <= 146, "exact FP32 level sums need 7 K 128^2 < 2^24");
   static_assert(TMEM_COLS <= 512, "levels x columns must fit in tensor memory");
 };
 
@@ -222,7 +223,7 @@ __device__ __forceinline__ void fence_async_smem() {
 
 // }}}
 
-// two digits in [-64, 64] -> half2: the bit pattern 0x6600 + d is the half
+// two digits in [-128, 128] -> half2: the bit pattern 0x6600 + d is the half
 // 1536 + d, and one HSUB2 removes the 1536 exactly (bits move through the
 // __ushort_as_half / __half_as_ushort intrinsics, not pointer punning)
 __device__ __forceinline__ uint32_t digits_to_half2(int d0, int d1) {
@@ -235,10 +236,6 @@ __device__ __forceinline__ uint32_t digits_to_half2(int d0, int d1) {
          ((uint32_t)__half_as_ushort(__high2half(d)) << 16);
 }
 
-// FP32 holding an exact integer |v| < 2^22 -> int32 (FADD + IADD, no conversion unit)
-__device__ __forceinline__ int32_t f32_exact_int(float v) {
-  return __float_as_int(v + 12582912.0f) - 0x4B400000;
-}
 
 // int64 |g| < 2^51 -> double, exactly (integer add + one DADD)
 __device__ __forceinline__ double i64_exact_double(long long g) {
@@ -298,40 +295,42 @@ __device__ __forceinline__ int dexp(double x) {
 }
 
 // x -> round(x 2^(54 - e_n)) as a 64-bit integer, where e_n = emax - 1022 and
-// emax is the largest exponent field in x's column (so |result| <= 2^54)
+// emax is the largest exponent field in x's column (so |result| <= 2^54):
+// the 53-bit significand m of x = m 2^(ex - 1075) shifted by ex - emax + 1
 __device__ __forceinline__ long long to_fixed(double x, int emax) {
   const long long bits = __double_as_longlong(x);
   int ex = (int)((bits >> 52) & 0x7ff);
   long long m = bits & 0xfffffffffffffLL;
   if (ex != 0) m |= 0x10000000000000LL;
   else ex = 1;
-  const int sh = emax - ex - 1;  // right shift
+  const int sh = emax - ex - (kFix - 53);  // right shift (>= -1)
   long long r;
-  if (sh < 0) r = m << 1;
+  if (sh < 0) r = m << (-sh);
   else if (sh == 0) r = m;
   else if (sh > 60) r = 0;
   else r = (m + (1LL << (sh - 1))) >> sh;
   return bits < 0 ? -r : r;
 }
 
-// 8 balanced base-128 digits of |x| <= 2^54, most significant first, with
-// 32-bit arithmetic: the low 28 bits give digits 4..7 (leaving a carry of
-// 0 or 1), the high part plus the carry gives digits 0..3
-__device__ __forceinline__ void digits8(long long x, int* d) {
-  int hi = (int)(x >> 28);
-  int lo = (int)(x & 0x0fffffffLL);
+// 7 balanced base-256 digits (each in [-128, 127]) of |x| <= 2^54, most
+// significant first, with 32-bit arithmetic: the low 24 bits give digits
+// 4..6 (leaving a carry of 0 or 1), the high part (|x >> 24| <= 2^30) plus
+// the carry gives digits 0..3
+__device__ __forceinline__ void digits7(long long x, int* d) {
+  int hi = (int)(x >> 24);
+  int lo = (int)(x & 0xffffffLL);
 #pragma unroll
-  for (int s = 7; s >= 4; --s) {
-    const int q = ((lo + 64) & 127) - 64;
+  for (int s = 6; s >= 4; --s) {
+    const int q = ((lo + 128) & 255) - 128;
     d[s] = q;
-    lo = (lo - q) >> 7;
+    lo = (lo - q) >> 8;
   }
   hi += lo;
 #pragma unroll
   for (int s = 3; s >= 0; --s) {
-    const int q = ((hi + 64) & 127) - 64;
+    const int q = ((hi + 128) & 255) - 128;
     d[s] = q;
-    hi = (hi - q) >> 7;
+    hi = (hi - q) >> 8;
   }
 }
 
@@ -376,8 +375,8 @@ __device__ __forceinline__ void split_columns(unsigned char* slices, int* col_em
       if (k + 1 < G::K) x1 = to_fixed(src(n, k + 1), em);
     }
     int d0[kS], d1[kS];
-    digits8(x0, d0);
-    digits8(x1, d1);
+    digits7(x0, d0);
+    digits7(x1, d1);
     unsigned char* dst = slices + ng * G::SBO + kc * 128 + nr * 16 + kp4 * 4;
 #pragma unroll
     for (int sl = 0; sl < kS; ++sl)
@@ -416,7 +415,7 @@ __device__ __forceinline__ void issue_products(uint32_t a_s, uint32_t b_s, uint3
 // read tensor-memory lanes 32 (w % 4).. only; lanes (= rows) at or past M and
 // columns at or past NC are skipped (warp-uniformly), and the columns of a
 // lane quadrant are shared by the warps that can read it.  Per 8 columns the
-// 8 level loads are issued before one wait; the recombination is integer
+// 7 level loads are issued before one wait; the recombination is integer
 // work.  Writes C (FP64) into out[row * NC + col].
 template <class G>
 __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
@@ -437,18 +436,19 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
     for (int l = 0; l < kLevels - 1; ++l)
       tc_ld8(tq + (uint32_t)(l * G::NPAD + c0), v[l]);
     tc_wait_ld();
-    // level sums (exact integers |v_l| < 2^22) -> W = G_hi 2^28 + G_lo with
-    // G_hi = ((v2 2^7 + v3) 2^14 + (v4 2^7 + v5)), G_lo likewise from v6..v9
+    // level sums (exact integers |v_l| < 2^24) -> W = G_hi 2^32 + G_lo with
+    // G_hi = v2 2^16 + v3 2^8 + v4, G_lo = v5 2^24 + v6 2^16 + v7 2^8 + v8,
+    // written as W = T 2^28 + f (|T| < 2^45, f in [0, 2^28))
     long long wt[8];
     unsigned wf[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      int x[kLevels - 1];
+      long long x[kLevels - 1];
 #pragma unroll
-      for (int l = 0; l < kLevels - 1; ++l) x[l] = f32_exact_int(__uint_as_float(v[l][j]));
-      const long long hi = (long long)(x[0] * 128 + x[1]) * 16384 + (x[2] * 128 + x[3]);
-      const long long lo = (long long)(x[4] * 128 + x[5]) * 16384 + (x[6] * 128 + x[7]);
-      wt[j] = hi + (lo >> 28);
+      for (int l = 0; l < kLevels - 1; ++l) x[l] = __float2ll_rn(__uint_as_float(v[l][j]));
+      const long long hi = x[0] * 65536 + x[1] * 256 + x[2];
+      const long long lo = x[3] * 16777216 + x[4] * 65536 + x[5] * 256 + x[6];
+      wt[j] = hi * 16 + (lo >> 28);
       wf[j] = (unsigned)(lo & 0x0fffffffLL);
     }
     if (row < G::M) {
@@ -456,7 +456,8 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
       for (int j = 0; j < 8; ++j) {
         const int col = c0 + j;
         if (col < G::NC) {
-          const int sc = e_row + col_emax[col] - 1022 - 31;
+          // C = W 2^(e_m + e_n - 60), e_n = col_emax - 1022; RN(W) 2^(sc - 28)
+          const int sc = e_row + col_emax[col] - 1022 - 32;
           double r;
           if (!fixed_to_double(wt[j], wf[j], sc - 28, &r))  // not a normal double
             r = fma((double)wf[j], 0x1p-28, i64_exact_double(wt[j])) * pow2(sc);

@@ -4,6 +4,9 @@ the GPU parity tests):
 
 * the FP64 emulation's fold turns W = T 2^28 + f into round-to-nearest-even
   FP64 with integer operations only (``fixed_to_double`` in dg_tc.cuh);
+* the FP64 emulation's whole product (54-bit fixed point, seven balanced
+  base-256 digits, level sums i + j <= 8, recombination) is accurate to
+  FP64 rounding;
 * the mixed kernel writes a row value as four balanced base-256 digits with
   FP32 arithmetic only (``digits4`` in dg_tcm.cuh), exactly;
 * the level sums the tensor core accumulates stay exact integers in FP32.
@@ -112,10 +115,97 @@ def test_level_sums_stay_exact_in_fp32():
     # mixed kernel: four digits (|d| <= 128), levels i + j <= 3 hold at most
     # four pairs, K <= 128 per phase: at most 2^23
     assert 4 * 128 * 128 * 128 <= 2 ** 23
-    # FP64 emulation: eight base-128 digits (|d| <= 64), a level holds at
-    # most eight pairs, K <= 112 per product
-    assert 8 * 112 * 64 * 64 < 2 ** 22
+    # FP64 emulation: seven base-256 digits (|d| <= 128), a level holds at
+    # most seven pairs, K <= 146 per product
+    assert 7 * 146 * 128 * 128 < 2 ** 24
     # integers below 2^24 are exact in FP32
     v = np.arange(2 ** 24 - 1000, 2 ** 24, dtype=np.int64)
     assert np.array_equal(v.astype(np.float32).astype(np.int64), v)
     assert math.isclose(float(np.float32(2 ** 24 + 1)), 2 ** 24)        # and no further
+
+
+def _to_fixed(x: float, emax: int) -> int:
+    """Restatement of to_fixed (dg_tc.cuh): round(x 2^(54 - e_n)), e_n = emax - 1022."""
+    bits = struct.unpack("<q", struct.pack("<d", x))[0]
+    ex = (bits >> 52) & 0x7FF
+    m = bits & ((1 << 52) - 1)
+    if ex:
+        m |= 1 << 52
+    else:
+        ex = 1
+    sh = emax - ex - 1
+    if sh < 0:
+        r = m << (-sh)
+    elif sh == 0:
+        r = m
+    elif sh > 60:
+        r = 0
+    else:
+        r = (m + (1 << (sh - 1))) >> sh
+    return -r if bits < 0 else r
+
+
+def _digits7(x: int) -> list:
+    """Seven balanced base-256 digits, most significant first (digits7 and
+    the host packing)."""
+    d = [0] * 7
+    for s in range(6, -1, -1):
+        q = ((x + 128) & 255) - 128
+        d[s] = q
+        x = (x - q) >> 8
+    assert x == 0
+    return d
+
+
+def _dexp(x: float) -> int:
+    return (struct.unpack("<Q", struct.pack("<d", x))[0] >> 52) & 0x7FF
+
+
+def _emulated_dot(a: list, xs: list) -> float:
+    """One output of the FP64 tensor-core emulation: row a (operator) times
+    column xs (data), as the kernel computes it."""
+    amax = max(abs(v) for v in a)
+    e_m = math.frexp(amax)[1] if amax > 0 else 0              # |a| < 2^e_m
+    emax = max(_dexp(v) for v in xs)
+    da = [_digits7(int(round(math.ldexp(v, 54 - e_m)))) for v in a]
+    dx = [_digits7(_to_fixed(v, emax)) for v in xs]
+    lv = []
+    for l in range(2, 9):                                     # levels 2..8
+        tot = 0
+        for i in range(max(1, l - 7), min(l - 1, 7) + 1):
+            j = l - i
+            tot += sum(p[i - 1] * q[j - 1] for p, q in zip(da, dx))
+        assert abs(tot) < 2 ** 24
+        lv.append(tot)
+    hi = lv[0] * 65536 + lv[1] * 256 + lv[2]
+    lo = lv[3] * 16777216 + lv[4] * 65536 + lv[5] * 256 + lv[6]
+    T, f = hi * 16 + (lo >> 28), lo & ((1 << 28) - 1)
+    s = e_m + (emax - 1022) - 60
+    return _fixed_to_double(T, f, s)
+
+
+def test_seven_digit_emulation_is_accurate_to_fp64():
+    rng = random.Random(3)
+    for K in (20, 35, 60, 105, 146):
+        for _ in range(40):
+            a = [rng.uniform(-1, 1) * 2.0 ** rng.randint(-3, 3) for _ in range(K)]
+            xs = [rng.gauss(0, 1) * 2.0 ** rng.randint(-8, 8) for _ in range(K)]
+            if rng.random() < 0.3:           # cancellation
+                xs[-1] = -sum(p * q for p, q in zip(a[:-1], xs[:-1])) / a[-1]
+            got = _emulated_dot(a, xs)
+            exact = sum(Fraction(p) * Fraction(q) for p, q in zip(a, xs))
+            scale = max(abs(v) for v in a) * max(abs(v) for v in xs)
+            # input rounding 2^-55 per operand and the dropped pairs
+            # (< 2^-51 K), on top of the final rounding
+            bound = 2.0 ** -50 * K * scale + abs(float(exact)) * 2.0 ** -52
+            assert abs(Fraction(got) - exact) <= Fraction(bound), (K, got, float(exact))
+
+
+def test_digits_fit_fp16_and_the_fixed_point_range():
+    for x in (2 ** 54, -(2 ** 54), 2 ** 54 - 1, 12345678901234567, -1, 0):
+        d = _digits7(x)
+        assert max(abs(v) for v in d) <= 128
+        assert sum(v * 256 ** (6 - k) for k, v in enumerate(d)) == x
+    # to_fixed never leaves |x| <= 2^54 for the column's largest exponent
+    for v in (1.0, -1.9999999999999998, 0.75, 1e-300, -3.0):
+        assert abs(_to_fixed(v, _dexp(v))) <= 2 ** 54
