@@ -237,6 +237,19 @@ __device__ __forceinline__ uint32_t digits_to_half2(int d0, int d1) {
 }
 
 
+// FP32 holding an exact integer |v| < 2^24 -> int32 without a conversion
+// instruction (GB300's conversion unit issues at a fraction of the FP32
+// rate): the FADD at 1.5 * 2^31, where the float spacing is 256, rounds v to
+// hi = 256 round(v / 256), read off the sum's mantissa bits; lo = v - hi is
+// exact (|lo| <= 128) and read off the bits of lo + 1.5 * 2^23
+__device__ __forceinline__ int32_t f32_exact_int24(float v) {
+  const float kBig = 3221225472.0f;  // 1.5 * 2^31
+  const float big = __fadd_rn(v, kBig);
+  const float lo = __fsub_rn(v, __fsub_rn(big, kBig));
+  return (__float_as_int(big) - __float_as_int(kBig)) * 256 +
+         (__float_as_int(__fadd_rn(lo, 12582912.0f)) - 0x4B400000);
+}
+
 // int64 |g| < 2^51 -> double, exactly (integer add + one DADD)
 __device__ __forceinline__ double i64_exact_double(long long g) {
   return __longlong_as_double(g + 0x4338000000000000LL) - 6755399441055744.0;
@@ -445,7 +458,7 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
     for (int j = 0; j < 8; ++j) {
       long long x[kLevels - 1];
 #pragma unroll
-      for (int l = 0; l < kLevels - 1; ++l) x[l] = __float2ll_rn(__uint_as_float(v[l][j]));
+      for (int l = 0; l < kLevels - 1; ++l) x[l] = f32_exact_int24(__uint_as_float(v[l][j]));
       const long long hi = x[0] * 65536 + x[1] * 256 + x[2];
       const long long lo = x[3] * 16777216 + x[4] * 65536 + x[5] * 256 + x[6];
       wt[j] = hi * 16 + (lo >> 28);

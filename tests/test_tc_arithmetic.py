@@ -209,3 +209,21 @@ def test_digits_fit_fp16_and_the_fixed_point_range():
     # to_fixed never leaves |x| <= 2^54 for the column's largest exponent
     for v in (1.0, -1.9999999999999998, 0.75, 1e-300, -3.0):
         assert abs(_to_fixed(v, _dexp(v))) <= 2 ** 54
+
+
+def _f32_exact_int24(v: np.float32) -> int:
+    """Restatement of f32_exact_int24 (dg_tc.cuh) in FP32 arithmetic."""
+    f32 = np.float32
+    big_c = f32(3221225472.0)
+    big = f32(v + big_c)
+    lo = f32(v - f32(big - big_c))
+    bits = lambda x: int(np.frombuffer(np.float32(x).tobytes(), np.int32)[0])  # noqa: E731
+    return (bits(big) - bits(big_c)) * 256 + (bits(f32(lo + f32(12582912.0))) - 0x4B400000)
+
+
+def test_level_sum_conversion_is_exact():
+    rng = np.random.default_rng(5)
+    vals = list(rng.integers(-(2 ** 24) + 1, 2 ** 24, 20000)) + [0, 1, -1, 127, 128, -128,
+                                                                 129, 2 ** 24 - 1, -(2 ** 24) + 1]
+    for v in vals:
+        assert _f32_exact_int24(np.float32(v)) == int(v)
