@@ -28,6 +28,7 @@ from actx_dgfem_suite_gb300.containers import (
     leaves,
     map_leaves,
 )
+from actx_dgfem_suite_gb300.hostmem import host_empty, host_empty_like
 from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
 
 
@@ -167,7 +168,8 @@ class PinnedResultPool:
         if free:
             buf = free.pop()
         else:
-            buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=self.pin)
+            buf = (host_empty(nbytes) if self.pin
+                   else torch.empty(nbytes, dtype=torch.uint8))
             self.allocated_bytes += nbytes
         t = buf.view(dtype).view(shape)
         arr = t.numpy()
@@ -249,6 +251,12 @@ class GB300DGArrayContext:
         t.record_stream(d2h)
         d2h.synchronize()
         return arr
+
+    def pinned_host_like(self, t: torch.Tensor) -> torch.Tensor:
+        """A page-locked host tensor shaped like ``t`` (on huge pages where
+        the system allows), for states a caller stages on the host: the
+        context's copies to and from such buffers run at the link rate."""
+        return host_empty_like(t)
 
     def release_host_buffers(self) -> None:
         """Return the pool's free page-locked result buffers to the system."""

@@ -237,6 +237,11 @@ __device__ __forceinline__ uint32_t digits_to_half2(int d0, int d1) {
 }
 
 
+// FP32 holding an exact integer |v| < 2^22 -> int32 (FADD + IADD, no conversion unit)
+__device__ __forceinline__ int32_t f32_exact_int(float v) {
+  return __float_as_int(__fadd_rn(v, 12582912.0f)) - 0x4B400000;
+}
+
 // FP32 holding an exact integer |v| < 2^24 -> int32 without a conversion
 // instruction (GB300's conversion unit issues at a fraction of the FP32
 // rate): the FADD at 1.5 * 2^31, where the float spacing is 256, rounds v to
@@ -458,7 +463,12 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
     for (int j = 0; j < 8; ++j) {
       long long x[kLevels - 1];
 #pragma unroll
-      for (int l = 0; l < kLevels - 1; ++l) x[l] = f32_exact_int24(__uint_as_float(v[l][j]));
+      for (int l = 0; l < kLevels - 1; ++l) {
+        // level l + 2 sums l + 1 digit pairs over K: |v| <= (l + 1) K 2^14,
+        // below 2^22 (the two-instruction form) while (l + 1) K < 256
+        const float fv = __uint_as_float(v[l][j]);
+        x[l] = (l + 1) * G::K < 256 ? f32_exact_int(fv) : f32_exact_int24(fv);
+      }
       const long long hi = x[0] * 65536 + x[1] * 256 + x[2];
       const long long lo = x[3] * 16777216 + x[4] * 65536 + x[5] * 256 + x[6];
       wt[j] = hi * 16 + (lo >> 28);

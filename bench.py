@@ -590,7 +590,8 @@ def our_arm(args) -> None:
     # {{{ e2e through the public API with host buffers
     host_states = []
     for r in runs:
-        hq = r["q"].cpu().pin_memory()
+        hq = actx.pinned_host_like(r["q"])
+        hq.copy_(r["q"])
         tmpl = r["call_args"][-1]
         from actx_dgfem_suite_gb300.containers import from_stacked
         hs = from_stacked(actx, tmpl, hq)

@@ -38,3 +38,25 @@ def test_calls_in_flight_with_host_states(actx):
         out = np.stack([d[0] for d in leaves(actx.to_numpy(c(*a)))])
         want = c.plan.rhs(hq.to(actx.device)).cpu().numpy()
         assert np.array_equal(out, want)
+
+
+def test_pinned_host_buffers(actx):
+    """pinned_host_like: page-locked (huge-page backed where available) host
+    tensors that round-trip through asynchronous copies, freed with their
+    last view."""
+    import gc
+    dev = torch.arange(3 * 1000 * 35, dtype=torch.float64, device=actx.device).view(3, 1000, 35)
+    h = actx.pinned_host_like(dev)
+    assert h.is_pinned() and h.shape == dev.shape and h.dtype == dev.dtype
+    h.copy_(dev, non_blocking=True)
+    torch.cuda.synchronize()
+    back = torch.empty_like(dev)
+    back.copy_(h, non_blocking=True)
+    torch.cuda.synchronize()
+    assert torch.equal(back, dev)
+    view = h[1]
+    del h
+    gc.collect()
+    assert float(view[0, 0]) == 35000.0      # a view keeps the memory alive
+    del view
+    gc.collect()
