@@ -673,11 +673,14 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     }
   }
 
+  // the persistent grid fits the modes the plan launches: RHS and RK stage,
+  // in the face-shared form on the split path
   dg::LaunchShape shape;
-  cudaError_t err = shape_of(equation, N, kprec, 0, &shape);
-  for (int mode = 1; mode < (split ? 4 : 2) && err == cudaSuccess; ++mode) {
+  const int base_mode = split ? dg::MODE_SPLIT : dg::MODE_RHS;
+  cudaError_t err = shape_of(equation, N, kprec, base_mode, &shape);
+  if (err == cudaSuccess) {
     dg::LaunchShape other;
-    err = shape_of(equation, N, kprec, mode, &other);
+    err = shape_of(equation, N, kprec, base_mode | dg::MODE_STAGE, &other);
     if (other.blocks_per_sm < shape.blocks_per_sm)
       shape.blocks_per_sm = other.blocks_per_sm;
   }

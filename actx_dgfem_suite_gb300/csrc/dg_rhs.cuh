@@ -131,8 +131,12 @@ struct OpsLayout {
   static constexpr int SIZE = FN + pad16(NFPT * 4);
 };
 
-// Shared-memory layout of one CTA, in bytes.
-template <int N, int EQ, typename Real>
+// Shared-memory layout of one CTA, in bytes.  SPLIT (the face-shared FP64
+// path, face values computed by the face kernel): no face geometry is
+// staged, and for Euler the face values reuse the flux-input buffer of the
+// volume term (they are loaded after the volume contractions), which keeps
+// more CTAs resident at the low orders.
+template <int N, int EQ, typename Real, bool SPLIT = false>
 struct Tile {
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP,
                        NFPT = Shape<N>::NFPT;
@@ -144,11 +148,16 @@ struct Tile {
   static constexpr int Q = OpsLayout<N, Real>::SIZE;              // double
   static constexpr int QR = Q + pad16(NF * E * NP * 8);           // Real copy
   static constexpr int AUX = QR + (MIXED ? pad16(NF * E * ROW * RS) : 0);
-  static constexpr int FLUX = AUX + pad16(NAUX * E * ROW * RS);
-  static constexpr int GEO = FLUX + pad16(NF * E * FROW * RS);
+  static constexpr int AUX_BYTES = pad16(NAUX * E * ROW * RS);
+  static constexpr int FLUX_BYTES = pad16(NF * E * FROW * RS);
+  // face values loaded late over the volume inputs (split Euler only)
+  static constexpr bool LATE_FLUX = SPLIT && EQ == DG_EULER;
+  static constexpr int FLUX = LATE_FLUX ? AUX : AUX + AUX_BYTES;
+  static constexpr int GEO =
+      LATE_FLUX ? AUX + (AUX_BYTES > FLUX_BYTES ? AUX_BYTES : FLUX_BYTES) : FLUX + FLUX_BYTES;
   static constexpr int FGEO = GEO + pad16(9 * E * RS);
   // mixed-precision Euler: FP64 pressure of every node of the tile
-  static constexpr int PRES = FGEO + pad16(16 * E * RS);
+  static constexpr int PRES = FGEO + (SPLIT ? 0 : pad16(16 * E * RS));
   static constexpr int SMEM_BASE =
       PRES + ((MIXED && EQ == DG_EULER) ? pad16(E * NP * 8) : 0);
   // MODE_TC: FP32 outputs of the tensor-core products (volume, then LIFT)
@@ -255,7 +264,7 @@ __device__ __forceinline__ Real to_real(double v) {
 
 template <int N, int EQ, typename Real, int MODE>
 __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
-  using T = Tile<N, EQ, Real>;
+  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0>;
   using Ops = OpsLayout<N, Real>;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
   constexpr bool SPLIT = (MODE & MODE_SPLIT) != 0;
@@ -334,20 +343,25 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     }
     {
       const double* mt = a.metric + e0 * 9;
-      const double* ft = a.face_geom + e0 * 16;
       for (int idx = t; idx < 9 * E; idx += kBlock)
         sG[idx] = idx < 9 * ecount ? to_real<Real>(__ldg(mt + idx)) : zero;
-      for (int idx = t; idx < 16 * E; idx += kBlock)
-        sFG[idx] = idx < 16 * ecount ? to_real<Real>(__ldg(ft + idx)) : zero;
+      if constexpr (!SPLIT) {  // face geometry: the fused path's fluxes only
+        const double* ft = a.face_geom + e0 * 16;
+        for (int idx = t; idx < 16 * E; idx += kBlock)
+          sFG[idx] = idx < 16 * ecount ? to_real<Real>(__ldg(ft + idx)) : zero;
+      }
     }
-    if constexpr (SPLIT) {  // face values of the tile: contiguous per field
+    // face values of the tile, contiguous per field (split Euler: after the
+    // volume term, over its inputs)
+    auto load_face_values = [&]() {
       const int64_t nfpt_all = nel * NFPT;
       const double* fk = a.flux_in + e0 * NFPT;
 #pragma unroll
       for (int k = 0; k < NF; ++k, fk += nfpt_all)
         for (int rem = t; rem < E * NFPT; rem += kBlock)
           sFlux[k * (E * FROW) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : zero;
-    }
+    };
+    if constexpr (SPLIT && !T::LATE_FLUX) load_face_values();
     __syncthreads();
     // }}}
 
@@ -759,6 +773,10 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       }
     }
     __syncthreads();
+    if constexpr (T::LATE_FLUX) {  // the volume term no longer reads its inputs
+      load_face_values();
+      __syncthreads();
+    }
     // }}}
 
     // {{{ 5. LIFT, then store or fold into the RK stage

@@ -18,12 +18,13 @@ namespace {
 
 template <int N, int EQ, typename Real, int MODE>
 constexpr int smem_of() {
-  return (MODE & MODE_TC) ? Tile<N, EQ, Real>::SMEM_BYTES_TC : Tile<N, EQ, Real>::SMEM_BASE;
+  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0>;
+  return (MODE & MODE_TC) ? T::SMEM_BYTES_TC : T::SMEM_BASE;
 }
 
 template <int N, int EQ, typename Real, int MODE>
 cudaError_t shape_impl(LaunchShape* out) {
-  using T = Tile<N, EQ, Real>;
+  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0>;
   constexpr int SMEM = smem_of<N, EQ, Real, MODE>();
   auto kern = dg_rhs_kernel<N, EQ, Real, MODE>;
   cudaError_t err = cudaFuncSetAttribute(
