@@ -28,7 +28,7 @@ from actx_dgfem_suite_gb300.containers import (
     leaves,
     map_leaves,
 )
-from actx_dgfem_suite_gb300.hostmem import host_empty, host_empty_like
+from actx_dgfem_suite_gb300.hostmem import host_empty_like
 from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
 
 
@@ -168,8 +168,10 @@ class PinnedResultPool:
         if free:
             buf = free.pop()
         else:
-            buf = (host_empty(nbytes) if self.pin
-                   else torch.empty(nbytes, dtype=torch.uint8))
+            # cudaHostAlloc'd memory: device->host copies into registered
+            # (huge-page) memory were measured to wait for every kernel in
+            # flight, while copies into this memory overlap them
+            buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=self.pin)
             self.allocated_bytes += nbytes
         t = buf.view(dtype).view(shape)
         arr = t.numpy()

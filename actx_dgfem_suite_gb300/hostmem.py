@@ -11,6 +11,12 @@ pages (``madvise(MADV_HUGEPAGE)``) before it is first touched, and only then
 registered with CUDA (``cudaHostRegister``), ran at 211 GB/s host->device and
 193 GB/s device->host from its first copy.
 
+Used for states that travel host->device.  Results travel the other way in
+``cudaHostAlloc`` memory (the array context's result pool): a device->host
+copy into registered memory was measured to start only after every kernel
+already queued on the device had finished, while a copy into
+``cudaHostAlloc`` memory overlaps them.
+
 :func:`host_empty` returns such a buffer as a CPU tensor (``is_pinned()`` is
 true, so ``copy_(..., non_blocking=True)`` is asynchronous); the memory is
 unregistered and freed when the tensor and every view of it are gone.  Where

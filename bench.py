@@ -11,10 +11,14 @@ RHS), whole job.
   stream; every case's state is larger than L2 (129 MB), so no L2 flush is
   needed between launches.
 * ``e2e``: the same step through the public API with host buffers:
-  ``compiled(t, host_state)`` (host->device copy of the page-locked state)
-  and ``actx.to_numpy(result)`` (device->host copy into a new page-locked
-  array) inside the timed region; 3-4 untimed steps (the first ones pay the
-  host allocations), then min(steps, 5) timed steps.
+  ``compiled(t, host_state)`` for every case (host->device copy of each
+  page-locked state on the context's copy stream, overlapping the kernels of
+  the cases before it), then ``actx.to_numpy(result)`` for every case
+  (device->host copy into a new page-locked array), all inside the timed
+  region; 3-4 untimed steps (the first ones pay the host allocations), then
+  min(steps, 5) timed steps.  ``split_ms`` times the step's parts alone.
+* ``parity``: every case at the CPU sample's size (n // cpu-scale) through
+  the public API against the CPU oracle's RHS of the same run.
 * ``--impl reference``: the CPU FP64 oracle (a restatement of the
   reference's operators; the reference itself cannot run here) on a bounded
   sample of every case, one process per case over the host's cores.
