@@ -168,9 +168,6 @@ class PinnedResultPool:
         if free:
             buf = free.pop()
         else:
-            # cudaHostAlloc'd memory: device->host copies into registered
-            # (huge-page) memory were measured to wait for every kernel in
-            # flight, while copies into this memory overlap them
             buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=self.pin)
             self.allocated_bytes += nbytes
         t = buf.view(dtype).view(shape)
@@ -231,19 +228,21 @@ class GB300DGArrayContext:
         block costs more than the copy, so buffers are reused by size and
         return to the pool when the caller drops the array.
         ``pinned_results=False`` keeps plain pageable arrays."""
+        # the event after the kernel that produced t (a compiled call's
+        # result), read before detach(), whose new tensor object carries no
+        # Python attributes
+        ready = getattr(t, "_dg_ready", None)
+        if ready is None and t._base is not None:
+            ready = getattr(t._base, "_dg_ready", None)
         t = t.detach()
         if not t.is_cuda:
             return t.numpy()
         if not self.pinned_results:
             return t.cpu().numpy()
         arr, h = self.host_pool.take(tuple(t.shape), t.dtype)
-        # the copy runs on the device-to-host stream and waits only for the
-        # kernel that produced t (a compiled call's result), so kernels the
-        # caller issued after it keep running meanwhile
+        # the copy runs on the device-to-host stream and waits only for that
+        # kernel, so kernels the caller issued after it keep running meanwhile
         d2h = self.d2h_stream
-        ready = getattr(t, "_dg_ready", None)
-        if ready is None and t._base is not None:
-            ready = getattr(t._base, "_dg_ready", None)
         if ready is not None:
             d2h.wait_event(ready)
         else:

@@ -11,11 +11,10 @@ pages (``madvise(MADV_HUGEPAGE)``) before it is first touched, and only then
 registered with CUDA (``cudaHostRegister``), ran at 211 GB/s host->device and
 193 GB/s device->host from its first copy.
 
-Used for states that travel host->device.  Results travel the other way in
-``cudaHostAlloc`` memory (the array context's result pool): a device->host
-copy into registered memory was measured to start only after every kernel
-already queued on the device had finished, while a copy into
-``cudaHostAlloc`` memory overlaps them.
+Used for states that travel host->device (the first copy out of a freshly
+page-locked ``cudaHostAlloc`` buffer is the slow one).  Results travel the
+other way in the array context's pool of ``cudaHostAlloc`` buffers, whose
+first device->host copy already ran at the link rate (193 GB/s).
 
 :func:`host_empty` returns such a buffer as a CPU tensor (``is_pinned()`` is
 true, so ``copy_(..., non_blocking=True)`` is asynchronous); the memory is

@@ -60,3 +60,32 @@ def test_pinned_host_buffers(actx):
     assert float(view[0, 0]) == 35000.0      # a view keeps the memory alive
     del view
     gc.collect()
+
+
+def test_result_readback_waits_only_for_its_own_call(actx):
+    """to_numpy of a compiled call's result waits for that call's kernels,
+    not for work queued after them: a long kernel issued after the call is
+    still running when the result is already on the host."""
+    import ctypes
+
+    from actx_dgfem_suite_gb300 import _lib
+    from actx_dgfem_suite_gb300.containers import leaves
+    from actx_dgfem_suite_gb300.rhs_builder import get_rhs
+    rhs, args = get_rhs("wave", actx, 3, 2, definition="baseline", nel_1d=4)
+    compiled = actx.compile(rhs)
+    ref = np.stack([d[0] for d in leaves(actx.to_numpy(compiled(*args)))])
+    out = compiled(*args)
+    # then about half a second of FP64 FMAs on the same stream
+    L = _lib.lib()
+    nsm = torch.cuda.get_device_properties(actx.device).multi_processor_count
+    buf = torch.empty(nsm * 4 * 256, dtype=torch.float64, device=actx.device)
+    stream = torch.cuda.current_stream(actx.device)
+    _lib.check(L.dg_fp64_fma_probe(ctypes.c_void_p(buf.data_ptr()), 200000, nsm * 4, 256,
+                                   ctypes.c_void_p(stream.cuda_stream)))
+    long_done = torch.cuda.Event()
+    long_done.record(stream)
+    got = np.stack([d[0] for d in leaves(actx.to_numpy(out))])
+    still_running = not long_done.query()
+    torch.cuda.synchronize()
+    assert np.array_equal(got, ref)
+    assert still_running
