@@ -112,9 +112,11 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
         pp = -1;
       }
     }
-    const double* fg = a.face_geom + face * 4u;
-    const double nx = __ldg(fg), ny = __ldg(fg + 1), nz = __ldg(fg + 2);
-    const double scale_o = __ldg(fg + 3);
+    // n_x, n_y, n_z, sJ/J of the face: two 16-byte loads (rows of 32 bytes)
+    const double2* fg = reinterpret_cast<const double2*>(a.face_geom) + face * 2u;
+    const double2 g01 = __ldg(fg), g23 = __ldg(fg + 1);
+    const double nx = g01.x, ny = g01.y, nz = g23.x;
+    const double scale_o = g23.y;
     const double scale_p =
         pp >= 0 ? __ldg(a.face_geom + ((uint32_t)pp / NFP) * 4u + 3) : 0.0;
 
@@ -129,9 +131,9 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
       }
     }
     // own[k]: value for this face point; part[k]: for the glued face point
-    // (before each side's sJ/J, and with half_scales before a factor 1/2)
+    // (before each side's sJ/J and a common factor fs)
     double own[NF], part[NF];
-    bool half_scales = false;
+    double fs = 1.0;
 
     if constexpr (EQ == DG_WAVE) {
       if (bdry) {  // Dirichlet mirror: exterior (-u, v)
@@ -140,20 +142,19 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
         qe[2] = qi[2];
         qe[3] = qi[3];
       }
-      const double c = a.p0;
-      const double vavg_n = 0.5 * (qi[1] + qe[1]) * nx + 0.5 * (qi[2] + qe[2]) * ny +
-                            0.5 * (qi[3] + qe[3]) * nz;
-      const double uavg = 0.5 * (qi[0] + qe[0]);
-      const double vjump = (qe[1] - qi[1]) * nx + (qe[2] - qi[2]) * ny +
-                           (qe[3] - qi[3]) * nz;
-      const double fu = c * (vavg_n + 0.5 * (qe[0] - qi[0]));
-      const double fv = c * (uavg + 0.5 * vjump);
-      own[0] = fu;
-      own[1] = fv * nx;
-      own[2] = fv * ny;
-      own[3] = fv * nz;
+      // F_u = c (avg(v).n + (u+ - u-)/2) = c/2 ((v- + v+).n + u+ - u-),
+      // F_v = c (avg(u) + (v+ - v-).n/2) n = c/2 (u- + u+ + (v+ - v-).n) n;
+      // c/2 goes into the side scales
+      const double sv = fma(qi[1] + qe[1], nx, fma(qi[2] + qe[2], ny, (qi[3] + qe[3]) * nz));
+      const double dv = fma(qe[1] - qi[1], nx, fma(qe[2] - qi[2], ny, (qe[3] - qi[3]) * nz));
+      const double gv = (qi[0] + qe[0]) + dv;
+      own[0] = sv + (qe[0] - qi[0]);
+      own[1] = gv * nx;
+      own[2] = gv * ny;
+      own[3] = gv * nz;
 #pragma unroll
       for (int k = 0; k < NF; ++k) part[k] = -own[k];
+      fs = 0.5 * a.p0;
     } else if constexpr (EQ == DG_EULER) {
       const double* an = a.aux;
       const double pi = __ldg(an + ii), ri = __ldg(an + nelnp + ii),
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
         own[k] = -tk;
         part[k] = tk;
       }
-      half_scales = true;
+      fs = 0.5;
     } else {  // DG_MAXWELL
       if (bdry) {  // PEC: exterior (-E, H)
         qe[0] = -qi[0];
@@ -218,26 +219,28 @@ __global__ void __launch_bounds__(kFaceBlock) dg_face_flux_kernel(const FaceArgs
         c_[2] = a_[0] * b_[1] - a_[1] * b_[0];
       };
       // fe = n x (z jh - alpha n x je) = Ae + Be, fh = n x (y je + alpha n x jh)
-      // = Ah + Bh; swapping the sides keeps Ae, Ah and negates Be, Bh
-      double nxe[3], nxh[3], nnxe[3], nnxh[3], ae[3], ah[3];
+      // = Ah + Bh; swapping the sides keeps Ae, Ah and negates Be, Bh.  With
+      // the constants folded: -ce fe = k1 (n x jh) + k2 (n x n x je),
+      // -ch fh = k3 (n x je) + k4 (n x n x jh)
+      double nxe[3], nxh[3], nnxe[3], nnxh[3];
       cross(n, je, nxe);
       cross(n, jh, nxh);
       cross(n, nxe, nnxe);
       cross(n, nxh, nnxh);
+      const double k1 = -ce * z, k2 = ce * alpha, k3 = -ch * y, k4 = -ch * alpha;
 #pragma unroll
       for (int x = 0; x < 3; ++x) {
-        ae[x] = z * nxh[x];
-        ah[x] = y * nxe[x];
-        const double be = -alpha * nnxe[x], bh = alpha * nnxh[x];
-        own[x] = -(ce * (ae[x] + be));
-        own[3 + x] = -(ch * (ah[x] + bh));
-        part[x] = -(ce * (ae[x] - be));
-        part[3 + x] = -(ch * (ah[x] - bh));
+        const double ae = k1 * nxh[x], be = k2 * nnxe[x];
+        const double ah = k3 * nxe[x], bh = k4 * nnxh[x];
+        own[x] = ae + be;
+        own[3 + x] = ah + bh;
+        part[x] = ae - be;
+        part[3 + x] = ah - bh;
       }
     }
 
-    const double so = half_scales ? 0.5 * scale_o : scale_o;
-    const double sp = half_scales ? 0.5 * scale_p : scale_p;
+    const double so = fs * scale_o;
+    const double sp = fs * scale_p;
     double* out = a.flux + fp;
 #pragma unroll
     for (int k = 0; k < NF; ++k, out += nfp_all) out[0] = so * own[k];
