@@ -72,6 +72,12 @@ class _ActxNumpy:
                                                       else torch.as_tensor(v, dtype=u.dtype, device=u.device)))
 
 
+def _timing_event(stream) -> torch.cuda.Event:
+    ev = torch.cuda.Event(enable_timing=True)
+    ev.record(stream)
+    return ev
+
+
 class CompiledRHS:
     """``actx.compile(rhs)``: evaluates the RHS through one DevicePlan.
 
@@ -103,8 +109,12 @@ class CompiledRHS:
             h2d.wait_event(self._in_free)
         else:
             h2d.wait_stream(cur)          # the buffer's allocation
+        log = self.actx.transfer_log
+        t0 = _timing_event(h2d) if log is not None else None
         with torch.cuda.stream(h2d):
             self._in_buf.copy_(host, non_blocking=True)
+        if log is not None:
+            log.append(("h2d", t0, _timing_event(h2d), host.numel() * host.element_size()))
         ready = torch.cuda.Event()
         ready.record(h2d)
         cur.wait_event(ready)
@@ -204,6 +214,10 @@ class GB300DGArrayContext:
         # copy streams: host states in, results out, beside the compute stream
         self.h2d_stream = torch.cuda.Stream(self.device)
         self.d2h_stream = torch.cuda.Stream(self.device)
+        #: a list to record every host<->device copy of compiled calls and
+        #: to_numpy in, as (direction, start event, end event, bytes) with
+        #: timing events on the copy streams; None (default) records nothing
+        self.transfer_log: list | None = None
 
     # {{{ device data
 
@@ -247,8 +261,12 @@ class GB300DGArrayContext:
             d2h.wait_event(ready)
         else:
             d2h.wait_stream(torch.cuda.current_stream(t.device))
+        log = self.transfer_log
+        t0 = _timing_event(d2h) if log is not None else None
         with torch.cuda.stream(d2h):
             h.copy_(t, non_blocking=True)
+        if log is not None:
+            log.append(("d2h", t0, _timing_event(d2h), t.numel() * t.element_size()))
         t.record_stream(d2h)
         d2h.synchronize()
         return arr

@@ -297,33 +297,27 @@ def reference_arm(args) -> None:
 # }}}
 
 
-def transfer_split(actx, runs, host_states) -> dict:
-    """Milliseconds of one step's host->device copies (every case's state
-    from its page-locked host buffer, through the compiled callables' own
-    staging, as the end-to-end step does) and device->host copies (every
-    result into a page-locked host array through ``to_numpy``), each timed
-    alone with events on the context's copy streams."""
+def transfer_split(actx, step_fn) -> dict:
+    """One more end-to-end step with the array context's transfer log on:
+    the busy time of its host->device and device->host copies (sum of the
+    copies' event intervals on the copy streams), the span from the step's
+    first upload to its last result copy, and the copies' effective rates."""
     import torch
-
-    from actx_dgfem_suite_gb300.containers import leaves
+    torch.cuda.synchronize()
+    actx.transfer_log = []
+    t0 = torch.cuda.Event(enable_timing=True)
+    t0.record(actx.h2d_stream)
+    step_fn()
+    torch.cuda.synchronize()
+    log, actx.transfer_log = actx.transfer_log, None
     res = {}
-    torch.cuda.synchronize()
-    h2d = actx.h2d_stream
-    e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
-    e0.record(h2d)
-    for r, a in zip(runs, host_states):
-        r["compiled"]._upload(leaves(a[-1])[0]._stack[0])
-    e1.record(h2d)
-    torch.cuda.synchronize()
-    res["h2d"] = e0.elapsed_time(e1)
-    d2h = actx.d2h_stream
-    e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
-    e0.record(d2h)
-    back = [actx.to_numpy(r["out"]) for r in runs]
-    e1.record(d2h)
-    d2h.synchronize()
-    res["d2h"] = e0.elapsed_time(e1)
-    del back
+    for kind in ("h2d", "d2h"):
+        rows = [(a.elapsed_time(b), n) for k, a, b, n in log if k == kind]
+        busy = sum(ms for ms, _ in rows)
+        res[kind] = busy
+        res[kind + "_gbs"] = sum(n for _, n in rows) / (busy * 1e-3) / 1e9 if busy > 0 else None
+    ends = [t0.elapsed_time(b) for k, a, b, n in log]
+    res["span"] = max(ends) if ends else 0.0
     return res
 
 
@@ -633,9 +627,9 @@ def our_arm(args) -> None:
              for h, r in zip(host_out[:1], runs[:1]))
     e2e_value = replica_rate(dofs_step, e2e_s, world)
     del host_out
-    # the step's parts timed alone: all host->device copies, all kernels (the
-    # device-resident step above), all device->host copies
-    split = transfer_split(actx, runs, host_states)
+    # the copies' busy time within one more step, beside the kernels' time
+    # (the device-resident step above) and the timed steps' median
+    split = transfer_split(actx, e2e_step)
     split["compute"] = ms_step
     split["step"] = statistics.median(e2e_step_ms)
     # }}}
@@ -715,7 +709,8 @@ def our_arm(args) -> None:
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "host_matches_device": bool(ok),
                     "step_ms": [round(x, 1) for x in e2e_step_ms],
-                    "split_ms": {k: round(v, 2) for k, v in split.items()},
+                    "split_ms": {k: (round(v, 2) if v is not None else None)
+                                 for k, v in split.items()},
                     "overlap": ("all cases' calls issued before their results are read: "
                                 "copies run on the context's copy streams beside the "
                                 "kernels")},
