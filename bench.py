@@ -621,17 +621,18 @@ def our_arm(args) -> None:
         e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, dev)
+    # the copies' busy time within one more step taken like the timed ones,
+    # beside the kernels' time (the device-resident step above) and the
+    # timed steps' median
+    split = transfer_split(actx, e2e_step)
+    split["compute"] = ms_step
+    split["step"] = statistics.median(e2e_step_ms)
     # sanity: the host result equals the device-resident result
     ok = all(np.array_equal(np.stack([d[0] for d in leaves(h)]),
                             r["out"].cpu().numpy())
              for h, r in zip(host_out[:1], runs[:1]))
     e2e_value = replica_rate(dofs_step, e2e_s, world)
     del host_out
-    # the copies' busy time within one more step, beside the kernels' time
-    # (the device-resident step above) and the timed steps' median
-    split = transfer_split(actx, e2e_step)
-    split["compute"] = ms_step
-    split["step"] = statistics.median(e2e_step_ms)
     # }}}
 
     # {{{ roofline of the dominant launch
