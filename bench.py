@@ -16,7 +16,8 @@ RHS), whole job.
   the cases before it), then ``actx.to_numpy(result)`` for every case
   (device->host copy into a new page-locked array), all inside the timed
   region; 3-4 untimed steps (the first ones pay the host allocations), then
-  min(steps, 5) timed steps.  ``split_ms`` times the step's parts alone.
+  min(steps, 5) timed steps.  ``split_ms``: the copies' busy time in one
+  more such step (transfer log of the array context), beside the kernels' time.
 * ``parity``: every case at the CPU sample's size (n // cpu-scale) through
   the public API against the CPU oracle's RHS of the same run.
 * ``--impl reference``: the CPU FP64 oracle (a restatement of the
