@@ -143,6 +143,10 @@ class WaveAdjointSolver:
                                device=self.device)
         self._rbar = torch.empty(shape, dtype=torch.float64, device=self.device)
         self._yscr = torch.empty(shape, dtype=torch.float64, device=self.device)
+        # touched once here, so that the first reverse sweep does not pay for
+        # bringing the buffers into use
+        for buf in (self._lq, self._rbar, self._yscr):
+            buf.zero_()
         self.stats = {}
 
     # {{{ forward
