@@ -13,7 +13,7 @@ _LIB_PATH = Path(__file__).resolve().parent / "libdgfem_gb300.so"
 _lib = None
 
 #: ABI version this binding is written for (dg_abi_version() of the library)
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 DG_OK = 0
 DG_ERR_ARGUMENT = 1
@@ -34,7 +34,7 @@ DG_FP64_TC = 2
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
-                    "dg_rhs_adjoint_stage", "dg_rhs_vjp",
+                    "dg_rhs_adjoint_stage", "dg_rhs_vjp", "dg_rhs_vjp_stage",
                     "dg_box_mesh_build",
                     "dg_plan_path", "dg_plan_info", "dg_plan_set_variant",
                     "dg_plan_autotune", "dg_plan_autotune_bounded",
@@ -135,6 +135,8 @@ def lib() -> ctypes.CDLL:
     L.dg_rhs_adjoint_stage.restype = ctypes.c_int
     L.dg_rhs_vjp.argtypes = [vp, vp, vp, vp, vp]
     L.dg_rhs_vjp.restype = ctypes.c_int
+    L.dg_rhs_vjp_stage.argtypes = [vp, vp, vp, dbl, vp, vp, dbl, dbl, dbl, vp, vp]
+    L.dg_rhs_vjp_stage.restype = ctypes.c_int
     L.dg_rhs_adjoint_noalloc.argtypes = [vp, vp, vp, vp]
     L.dg_rhs_adjoint_noalloc.restype = ctypes.c_int
     L.dg_box_mesh_build.argtypes = [ctypes.POINTER(BoxDesc), vp]

@@ -285,9 +285,13 @@ class EulerAdjointSolver:
     Receivers sample the density.  The reverse of one step needs the five
     stage input states ``q^(s)``: stage ``s`` computes ``r^s = a_s r^{s-1} + dt
     L(q^(s))`` and ``q^(s+1) = q^(s) + b_s r^s``, so its adjoint applies the
-    transposed Jacobian ``L'(q^(s))^T`` (``dg_rhs_vjp``) to the residual
-    adjoint.  Checkpoints every ``segment`` steps; a segment is replayed once
-    with its stage states kept (memory ``N/k + 5k`` states)."""
+    transposed Jacobian ``L'(q^(s))^T`` to the residual adjoint.  Checkpoints
+    every ``segment`` steps; a segment is replayed once with its stage states
+    kept (memory ``N/k + 5k`` states): the replayed stages write their output
+    states straight into the record, allocated once, so recording costs no
+    copies.  Each reverse stage is one fused call (``dg_rhs_vjp_stage``: the
+    transposed Jacobian, the state-adjoint update and the next residual
+    adjoint)."""
 
     def __init__(self, disc: DGDiscretization, gamma: float, dt: float, nsteps: int,
                  receivers: Receivers, device=None, segment: int | None = None):
@@ -301,15 +305,36 @@ class EulerAdjointSolver:
         shape = self.plan.shape
         self._buf = torch.empty(shape, dtype=torch.float64, device=self.device)
         self._res = torch.zeros(shape, dtype=torch.float64, device=self.device)
+        # the reverse sweep's buffers, allocated and touched once: the stage
+        # input states of a segment, the residual adjoint and the scratch of
+        # the transposed Jacobian
+        self._qs = torch.zeros((self.segment, 5) + shape, dtype=torch.float64,
+                               device=self.device)
+        self._rbar = torch.zeros(shape, dtype=torch.float64, device=self.device)
+        self._yscr = torch.zeros(shape, dtype=torch.float64, device=self.device)
 
-    def _step(self, q: torch.Tensor, record: list | None = None) -> None:
+    def _step(self, q: torch.Tensor) -> None:
         src, dst = q, self._buf
         for s in range(5):
-            if record is not None:
-                record.append(src.clone())       # stage input state q^(s)
             self.plan.rk_stage(src, dst, self._res, RK4A[s], RK4B[s], self.dt)
             src, dst = dst, src
         q.copy_(src)
+
+    def _replay(self, q0: torch.Tensor, nsteps: int) -> None:
+        """Steps from ``q0`` with every stage input state recorded:
+        ``_qs[k, s]`` = q^(s) of the k-th step (stage s of step k reads
+        ``_qs[k, s]`` and writes the next stage's input in place)."""
+        qs = self._qs
+        qs[0, 0].copy_(q0)
+        for k in range(nsteps):
+            for s in range(5):
+                if s < 4:
+                    dst = qs[k, s + 1]
+                elif k + 1 < nsteps:
+                    dst = qs[k + 1, 0]
+                else:
+                    dst = self._buf         # the next checkpoint: not needed
+                self.plan.rk_stage(qs[k, s], dst, self._res, RK4A[s], RK4B[s], self.dt)
 
     def forward(self, q0: torch.Tensor):
         q = q0.clone()
@@ -323,28 +348,25 @@ class EulerAdjointSolver:
                 ckpts[n + 1] = q.clone()
         return traces, ckpts
 
-    def _adjoint_step(self, lam: torch.Tensor, stages: list) -> None:
-        rbar = torch.zeros_like(lam)
-        y = torch.empty_like(lam)
+    def _adjoint_step(self, lam: torch.Tensor, stages: torch.Tensor) -> None:
+        """lam <- Phi'^T lam for one forward step with stage inputs
+        ``stages[s]``: rbar_4 = b_4 lam, rbar_{s-1} = a_s rbar_s + b_{s-1} lam
+        and lam += dt L'(q^(s))^T rbar_s, one fused call per stage."""
+        rbar = self._rbar
         for s in range(4, -1, -1):
-            rbar.add_(lam, alpha=RK4B[s])
-            self.plan.vjp(stages[s], rbar, y)
-            lam.add_(y, alpha=self.dt)
-            rbar.mul_(RK4A[s])
+            x, xscale = (lam, RK4B[4]) if s == 4 else (rbar, 1.0)
+            self.plan.vjp_stage(stages[s], x, xscale, lam, rbar if s > 0 else None,
+                                RK4A[s], RK4B[s - 1] if s > 0 else 0.0, self.dt,
+                                self._yscr)
 
     def backward(self, grad_traces: torch.Tensor, ckpts: dict) -> torch.Tensor:
         lam = torch.zeros(self.plan.shape, dtype=torch.float64, device=self.device)
         for seg_start in reversed(sorted(ckpts)):
             seg_end = min(self.nsteps, seg_start + self.segment)
-            q = ckpts[seg_start].clone()
-            records = []
-            for _ in range(seg_start, seg_end):
-                rec: list = []
-                self._step(q, rec)
-                records.append(rec)
+            self._replay(ckpts[seg_start], seg_end - seg_start)
             for n in range(seg_end - 1, seg_start - 1, -1):
                 self.rec.inject(lam, grad_traces[n])
-                self._adjoint_step(lam, records[n - seg_start])
+                self._adjoint_step(lam, self._qs[n - seg_start])
         return lam
 
 

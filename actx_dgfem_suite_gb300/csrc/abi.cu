@@ -223,12 +223,13 @@ struct dg_plan {
   // mixed-precision Euler: per-node FP32 pressure table, filled before each RHS
   float* d_pres = nullptr;
   int pres_grid = 0;
-  // mixed precision with tcgen05 contractions (variant 4)
-  bool tcm = false;
-  void* d_tcm_ops = nullptr;
-  uint32_t tcm_ops_bytes = 0;
-  dg::LaunchShape tcm_shape;
-  int tcm_grid = 0;
+  // mixed precision with tcgen05 contractions: [0] exact digit pairs
+  // (variant 4), [1] 3xTF32 products (variant 5)
+  bool tcm[2] = {false, false};
+  void* d_tcm_ops[2] = {nullptr, nullptr};
+  uint32_t tcm_ops_bytes[2] = {0u, 0u};
+  dg::LaunchShape tcm_shape[2];
+  int tcm_grid[2] = {0, 0};
   // face-shared path and adjoint (wave, FP64): the mesh's face_partner
   const int32_t* face_partner = nullptr;
   void* d_adj_ops = nullptr;
@@ -451,6 +452,14 @@ uint16_t half_bits(int d) {
   return static_cast<uint16_t>(sign | ((e + 15) << 10) | mant);
 }
 
+// TF32 bits of a finite float: 10 explicit mantissa bits, rounded to
+// nearest with ties away from zero (the rounding of cvt.rna.tf32.f32)
+uint32_t tf32_rna_bits(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  return (u + 0x1000u) & 0xffffe000u;
+}
+
 // One product's block: A (m x k, element (r, c) = at(r, c)) as 7 FP16 digit
 // slices of its rows' 54-bit fixed-point integers (balanced base-256 digits,
 // slice 0 most significant) in the K-major no-swizzle layout of the
@@ -515,22 +524,29 @@ int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
 }
 
 // Operator block of the mixed tcgen05 kernel: B_V = [A_0 A_1 A_2] and
-// B_L = LIFT as four FP16 digit slices each (layout: tcm::MPlan).
+// B_L = LIFT, as four FP16 digit slices each plus row scales, or (tf32) as
+// TF32 hi / lo slices (layout: tcm::MPlan).
 int pack_tcm_ops(int order, const double* diff, const double* lift,
-                 const int32_t* face_nodes, unsigned char* out, int out_bytes) {
+                 const int32_t* face_nodes, unsigned char* out, int out_bytes, bool tf32) {
   const int np = (order + 1) * (order + 2) * (order + 3) / 6;
   const int nfpt = 2 * (order + 1) * (order + 2);
   const int npp = np + (np & 1);  // node pitch of the volume columns (even)
-  const int nb = (np + 15) & ~15, kv = (3 * npp + 15) & ~15, kl = (nfpt + 15) & ~15;
-  const int sbo_v = (kv / 8) * 128, sbo_l = (kl / 8) * 128;
+  const int kg = tf32 ? 4 : 8, kstep = 2 * kg, esz = 16 / kg, ndig = tf32 ? 2 : 4;
+  auto rup = [](int x, int m) { return (x + m - 1) / m * m; };
+  const int nb = (np + 15) & ~15, kv = rup(3 * npp, kstep), kl = rup(nfpt, kstep);
+  const int sbo_v = (kv / kg) * 128, sbo_l = (kl / kg) * 128;
   const int bs_v = (nb / 8) * sbo_v, bs_l = (nb / 8) * sbo_l;
-  const int ops_l = 4 * bs_v, ops_ev = ops_l + 4 * bs_l, ops_el = ops_ev + nb * 4;
-  const int ops_fn = ops_el + nb * 4;
+  const int ops_l = ndig * bs_v, ops_ev = ops_l + ndig * bs_l;
+  const int ops_el = ops_ev + (tf32 ? 0 : nb * 4);
+  const int ops_fn = ops_el + (tf32 ? 0 : nb * 4);
   const int total = ops_fn + ((nfpt * 4 + 15) & ~15);
   if (!out) return total;
   if (out_bytes != total) return -1;
-  std::memset(out, 0, total);  // FP16 zero digits
-  // one block: rows i < np of at(i, k), k < kk, scaled per row to 31-bit
+  std::memset(out, 0, total);  // FP16 / TF32 zeros
+  auto offset = [&](int i, int k, int sbo) {
+    return (i / 8) * sbo + (k / kg) * 128 + (i % 8) * 16 + (k % kg) * esz;
+  };
+  // digits: rows i < np of at(i, k), k < kk, scaled per row to 31-bit
   // integers (|x| <= 2^31) in four balanced base-256 digits, most significant
   // first; row scales 2^e (FP32) with |at(i, k)| < 2^e
   auto block = [&](int base, int slice, int sbo, int kk, int exp_off, auto at) {
@@ -543,7 +559,7 @@ int pack_tcm_ops(int order, const double* diff, const double* lift,
       rscale[i] = std::ldexp(1.0f, e);
       for (int k = 0; k < kk; ++k) {
         long long x = std::llrint(std::ldexp(at(i, k), 31 - e));
-        const int off = base + (i / 8) * sbo + (k / 8) * 128 + (i % 8) * 16 + (k % 8) * 2;
+        const int off = base + offset(i, k, sbo);
         for (int d = 3; d >= 0; --d) {  // least significant digit first
           const long long dig = d == 0 ? x : ((x + 128) & 255) - 128;
           x = (x - dig) >> 8;
@@ -553,12 +569,32 @@ int pack_tcm_ops(int order, const double* diff, const double* lift,
       }
     }
   };
-  block(0, bs_v, sbo_v, 3 * npp, ops_ev, [&](int i, int k) {
+  // tf32: at(i, k) = hi + lo (+ a remainder below 2^-22 relative), both TF32
+  auto block_tf32 = [&](int base, int slice, int sbo, int kk, auto at) {
+    for (int i = 0; i < np; ++i)
+      for (int k = 0; k < kk; ++k) {
+        const double x = at(i, k);
+        const uint32_t hi = tf32_rna_bits(static_cast<float>(x));
+        float hf;
+        std::memcpy(&hf, &hi, 4);
+        const uint32_t lo = tf32_rna_bits(static_cast<float>(x - static_cast<double>(hf)));
+        const int off = base + offset(i, k, sbo);
+        std::memcpy(out + off, &hi, 4);
+        std::memcpy(out + off + slice, &lo, 4);
+      }
+  };
+  auto vol = [&](int i, int k) {
     const int r = k / npp, j = k - r * npp;  // column r npp + j; j = np is padding
     return j < np ? diff[((size_t)r * np + i) * np + j] : 0.0;
-  });
-  block(ops_l, bs_l, sbo_l, nfpt, ops_el,
-        [&](int i, int k) { return lift[(size_t)i * nfpt + k]; });
+  };
+  auto lft = [&](int i, int k) { return lift[(size_t)i * nfpt + k]; };
+  if (tf32) {
+    block_tf32(0, bs_v, sbo_v, 3 * npp, vol);
+    block_tf32(ops_l, bs_l, sbo_l, nfpt, lft);
+  } else {
+    block(0, bs_v, sbo_v, 3 * npp, ops_ev, vol);
+    block(ops_l, bs_l, sbo_l, nfpt, ops_el, lft);
+  }
   std::memcpy(out + ops_fn, face_nodes, (size_t)nfpt * 4);
   return total;
 }
@@ -612,7 +648,7 @@ extern "C" {
 
 const char* dg_last_error(void) { return g_last_error.c_str(); }
 
-int32_t dg_abi_version(void) { return 4; }
+int32_t dg_abi_version(void) { return 5; }
 
 int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,
@@ -751,33 +787,35 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     const int bps = t1.blocks_per_sm < t0.blocks_per_sm ? t1.blocks_per_sm : t0.blocks_per_sm;
     const int64_t tfull = (int64_t)nsm * (bps > 0 ? bps : 1);
     p->grid_mtc = (int)(ntiles < tfull ? ntiles : tfull);
-    // the tcgen05 form (variant 4)
-    dg::LaunchShape m0, m1;
-    err = tcm_shape_of(equation, N, 0, &m0);
-    if (err == cudaSuccess) err = tcm_shape_of(equation, N, 1, &m1);
-    const int mbytes = dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0);
-    if (err != cudaSuccess || mbytes != m0.ops_bytes) {
-      dg_plan_destroy(p);
-      return err != cudaSuccess ? cuda_fail(err, "tcgen05 mixed kernel configuration")
-                                : fail(DG_ERR_CUDA, "tcgen05 operator layout mismatch");
-    }
-    if (m1.blocks_per_sm < m0.blocks_per_sm) m0.blocks_per_sm = m1.blocks_per_sm;
-    if (m0.blocks_per_sm >= 1) {
+    // the tcgen05 forms (variants 4 and 5)
+    for (int k = 0; k < 2; ++k) {
+      dg::LaunchShape m0, m1;
+      err = tcm_shape_of(equation, N, 2 * k, &m0);
+      if (err == cudaSuccess) err = tcm_shape_of(equation, N, 2 * k + 1, &m1);
+      const int mbytes =
+          dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0, k == 1);
+      if (err != cudaSuccess || mbytes != m0.ops_bytes) {
+        dg_plan_destroy(p);
+        return err != cudaSuccess ? cuda_fail(err, "tcgen05 mixed kernel configuration")
+                                  : fail(DG_ERR_CUDA, "tcgen05 operator layout mismatch");
+      }
+      if (m1.blocks_per_sm < m0.blocks_per_sm) m0.blocks_per_sm = m1.blocks_per_sm;
+      if (m0.blocks_per_sm < 1) continue;
       std::vector<unsigned char> mops(mbytes);
-      dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, mops.data(), mbytes);
-      err = cudaMalloc(&p->d_tcm_ops, mbytes);
+      dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, mops.data(), mbytes, k == 1);
+      err = cudaMalloc(&p->d_tcm_ops[k], mbytes);
       if (err == cudaSuccess)
-        err = cudaMemcpy(p->d_tcm_ops, mops.data(), mbytes, cudaMemcpyHostToDevice);
+        err = cudaMemcpy(p->d_tcm_ops[k], mops.data(), mbytes, cudaMemcpyHostToDevice);
       if (err != cudaSuccess) {
         dg_plan_destroy(p);
         return cuda_fail(err, "tcgen05 operator buffer");
       }
-      p->tcm = true;
-      p->tcm_ops_bytes = static_cast<uint32_t>(mbytes);
-      p->tcm_shape = m0;
+      p->tcm[k] = true;
+      p->tcm_ops_bytes[k] = static_cast<uint32_t>(mbytes);
+      p->tcm_shape[k] = m0;
       const int64_t mtiles = (p->nel + m0.elems_per_tile - 1) / m0.elems_per_tile;
       const int64_t mfull = (int64_t)nsm * m0.blocks_per_sm;
-      p->tcm_grid = (int)(mtiles < mfull ? mtiles : mfull);
+      p->tcm_grid[k] = (int)(mtiles < mfull ? mtiles : mfull);
     }
   }
   p->face_partner = mesh->face_partner;
@@ -881,11 +919,12 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
 
 int dg_plan_set_variant(dg_plan* p, int32_t variant) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
-  if (variant < 0 || variant > 4) return fail(DG_ERR_ARGUMENT, "variant must be 0..4");
+  if (variant < 0 || variant >= DG_NUM_VARIANTS)
+    return fail(DG_ERR_ARGUMENT, "variant must be 0..5");
   if ((variant & 1) && p->precision != DG_FP32_MIXED)
     return fail(DG_ERR_UNSUPPORTED, "tensor-core products are a mixed-precision variant");
-  if (variant == 4 && !p->tcm)
-    return fail(DG_ERR_UNSUPPORTED, "the tcgen05 kernel is a mixed-precision variant");
+  if (variant >= 4 && !p->tcm[variant - 4])
+    return fail(DG_ERR_UNSUPPORTED, "the tcgen05 kernels are mixed-precision variants");
   if (p->tc) return fail(DG_ERR_UNSUPPORTED, "DG_FP64_TC plans have one variant");
   p->variant = variant;
   return DG_OK;
@@ -941,7 +980,7 @@ int autotune_impl(dg_plan* p, const double* q, double* rhs, const double* ref,
                   double max_rel_l2, int32_t reps, void* stream, int32_t* chosen,
                   float* ms_per_variant, double* err_per_variant) {
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const int nvar = p->tc ? 1 : (p->tcm ? 5 : 4);
+  const int nvar = p->tc ? 1 : DG_NUM_VARIANTS;
   const int64_t n = (int64_t)p->nfields * p->nel * p->np;
   cudaEvent_t e0, e1;
   cudaError_t err = cudaEventCreate(&e0);
@@ -952,10 +991,11 @@ int autotune_impl(dg_plan* p, const double* q, double* rhs, const double* ref,
   float best_ms = 0.f;
   double best_err = 0.0;
   int code = DG_OK;
-  for (int v = 0; v < 5 && code == DG_OK; ++v) {
+  for (int v = 0; v < DG_NUM_VARIANTS && code == DG_OK; ++v) {
     float ms = -1.f;
     double rel = -1.0;
-    if (v < nvar && ((v & 1) == 0 || p->precision == DG_FP32_MIXED)) {
+    const bool have = v < 4 || p->tcm[v - 4];
+    if (v < nvar && have && ((v & 1) == 0 || p->precision == DG_FP32_MIXED)) {
       p->variant = v;
       code = dg_rhs(p, q, rhs, stream);  // warm-up
       if (code == DG_OK) err = cudaEventRecord(e0, s);
@@ -997,6 +1037,30 @@ int autotune_impl(dg_plan* p, const double* q, double* rhs, const double* ref,
   if (code == DG_OK && best < 0 && first_status)
     return fail(first_status, "every autotuned variant raised a device-side error");
   return code;
+}
+
+dg::VjpArgs vjp_args(const dg_plan* p, const double* q, const double* x, double* y) {
+  dg::VjpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.q = q;
+  a.x = x;
+  a.y = y;
+  a.aux = p->d_aux;
+  a.scratch = p->d_flux;
+  a.elem_scale = p->elem_scale;
+  a.metric = p->metric;
+  a.face_geom = p->face_geom;
+  a.gather = p->gather;
+  a.partner = p->face_partner;
+  a.owned = p->d_owned;
+  a.nowned = p->nowned;
+  a.ops = p->d_adj_ops;
+  a.ops_bytes = p->adj_ops_bytes;
+  a.nel = p->nel;
+  a.status = p->d_status;
+  a.gamma = p->params[0];
+  a.xscale = 1.0;
+  return a;
 }
 
 }  // namespace
@@ -1137,28 +1201,45 @@ int dg_rhs_vjp(dg_plan* p, const double* q, const double* x, double* y,
     return fail(DG_ERR_ARGUMENT, "y must not overlap q or x");
   if (p->equation == DG_WAVE)  // linear: the transpose, scratch in the face buffer
     return dg_rhs_adjoint(p, x, y, p->d_flux, stream);
-  dg::VjpArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.q = q;
-  a.x = x;
-  a.y = y;
-  a.aux = p->d_aux;
-  a.scratch = p->d_flux;
-  a.elem_scale = p->elem_scale;
-  a.metric = p->metric;
-  a.face_geom = p->face_geom;
-  a.gather = p->gather;
-  a.partner = p->face_partner;
-  a.owned = p->d_owned;
-  a.nowned = p->nowned;
-  a.ops = p->d_adj_ops;
-  a.ops_bytes = p->adj_ops_bytes;
-  a.nel = p->nel;
-  a.status = p->d_status;
-  a.gamma = p->params[0];
-  cudaError_t err = dg::vjp_launch_euler(p->order, a, p->adj_grid, p->nsm,
+  dg::VjpArgs a = vjp_args(p, q, x, y);
+  cudaError_t err = dg::vjp_launch_euler(p->order, a, p->adj_grid, p->nsm, false,
                                          reinterpret_cast<cudaStream_t>(stream));
   if (err != cudaSuccess) return cuda_fail(err, "vjp launch");
+  return DG_OK;
+}
+
+int dg_rhs_vjp_stage(dg_plan* p, const double* q, const double* x, double xscale,
+                     double* lam, double* rbar_out, double a_coef, double b_coef,
+                     double dt, double* y_scratch, void* stream) {
+  if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (!p->d_adj_ops || !p->split)
+    return fail(DG_ERR_UNSUPPORTED,
+                "the reverse stage needs an FP64 wave or Euler plan built with "
+                "face_partner");
+  if (p->equation == DG_WAVE)  // linear: q is not read
+    return dg_rhs_adjoint_stage(p, x, xscale, lam, rbar_out, nullptr, nullptr, a_coef,
+                                b_coef, dt, y_scratch, stream);
+  if (!q || !x || !lam || !y_scratch)
+    return fail(DG_ERR_ARGUMENT, "q, x, lam or y_scratch is NULL");
+  const int64_t bytes = (int64_t)p->nfields * p->nel * p->np * 8;
+  // x may be lam or rbar_out itself (each node reads before it writes); q is
+  // only read, and may not overlap a written array
+  auto bad = [&](const void* u, const void* v) { return u != v && overlap(u, v, bytes); };
+  if (bad(x, lam) || (rbar_out && (bad(x, rbar_out) || overlap(lam, rbar_out, bytes))) ||
+      overlap(y_scratch, x, bytes) || overlap(y_scratch, lam, bytes) ||
+      overlap(y_scratch, q, bytes) || overlap(q, lam, bytes) ||
+      (rbar_out && (overlap(y_scratch, rbar_out, bytes) || overlap(q, rbar_out, bytes))))
+    return fail(DG_ERR_ARGUMENT, "reverse stage arrays overlap");
+  dg::VjpArgs a = vjp_args(p, q, x, y_scratch);
+  a.xscale = xscale;
+  a.lam = lam;
+  a.rbar_out = rbar_out;
+  a.rk_a = a_coef;
+  a.rk_b = b_coef;
+  a.dt = dt;
+  cudaError_t err = dg::vjp_launch_euler(p->order, a, p->adj_grid, p->nsm, true,
+                                         reinterpret_cast<cudaStream_t>(stream));
+  if (err != cudaSuccess) return cuda_fail(err, "reverse stage launch");
   return DG_OK;
 }
 
@@ -1185,10 +1266,11 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     a.ops = p->d_tc_ops;
     a.ops_bytes = p->tc_ops_bytes;
     err = tc_launch_of(p->equation, p->order, 0, a, p->tc_grid, s);
-  } else if (p->variant == 4) {
-    a.ops = p->d_tcm_ops;
-    a.ops_bytes = p->tcm_ops_bytes;
-    err = tcm_launch_of(p->equation, p->order, 0, a, p->tcm_grid, s);
+  } else if (p->variant >= 4) {
+    const int k = p->variant - 4;
+    a.ops = p->d_tcm_ops[k];
+    a.ops_bytes = p->tcm_ops_bytes[k];
+    err = tcm_launch_of(p->equation, p->order, 2 * k, a, p->tcm_grid[k], s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
                     main_mode(p, p->split ? dg::MODE_SPLIT : dg::MODE_RHS), a,
@@ -1236,10 +1318,11 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     a.ops = p->d_tc_ops;
     a.ops_bytes = p->tc_ops_bytes;
     err = tc_launch_of(p->equation, p->order, 1, a, p->tc_grid, s);
-  } else if (p->variant == 4) {
-    a.ops = p->d_tcm_ops;
-    a.ops_bytes = p->tcm_ops_bytes;
-    err = tcm_launch_of(p->equation, p->order, 1, a, p->tcm_grid, s);
+  } else if (p->variant >= 4) {
+    const int k = p->variant - 4;
+    a.ops = p->d_tcm_ops[k];
+    a.ops_bytes = p->tcm_ops_bytes[k];
+    err = tcm_launch_of(p->equation, p->order, 2 * k + 1, a, p->tcm_grid[k], s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
                     main_mode(p, dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0)), a,
@@ -1357,7 +1440,8 @@ int dg_plan_destroy(dg_plan* p) {
   if (p->d_status && cudaFree(p->d_status) != cudaSuccess) code = DG_ERR_CUDA;
   if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
   for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux,
-                  (void*)p->d_tc_ops, (void*)p->d_tcm_ops, (void*)p->d_pres})
+                  (void*)p->d_tc_ops, p->d_tcm_ops[0], p->d_tcm_ops[1],
+                  (void*)p->d_pres})
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;
   if (code != DG_OK) return fail(code, "cudaFree failed");
@@ -1437,7 +1521,7 @@ int dg_plan_path(const dg_plan* p, int32_t* face_shared, int32_t* tensor_cores,
   if (face_shared) *face_shared = p->split ? 1 : 0;
   if (tensor_cores)
     *tensor_cores =
-        (p->tc || p->variant == 4 || ((p->variant & 1) && p->precision == DG_FP32_MIXED)) ? 1 : 0;
+        (p->tc || p->variant >= 4 || ((p->variant & 1) && p->precision == DG_FP32_MIXED)) ? 1 : 0;
   if (launches_per_rhs)
     *launches_per_rhs = p->split ? (p->equation == DG_EULER ? 3 : 2) : (p->d_pres ? 2 : 1);
   if (owned_faces) *owned_faces = p->split ? p->nowned : 0;
@@ -1451,12 +1535,14 @@ int dg_plan_info(const dg_plan* p, int64_t* nelements, int32_t* order,
   if (nelements) *nelements = p->nel;
   if (order) *order = p->order;
   if (nfields) *nfields = p->nfields;
-  const bool m4 = !p->tc && p->variant == 4;
-  if (grid) *grid = p->tc ? p->tc_grid : (m4 ? p->tcm_grid : main_grid(p));
-  if (block) *block = p->tc ? p->tc_shape.threads : (m4 ? p->tcm_shape.threads : dg::kBlock);
+  const bool m4 = !p->tc && p->variant >= 4;
+  const int k = m4 ? p->variant - 4 : 0;
+  if (grid) *grid = p->tc ? p->tc_grid : (m4 ? p->tcm_grid[k] : main_grid(p));
+  if (block)
+    *block = p->tc ? p->tc_shape.threads : (m4 ? p->tcm_shape[k].threads : dg::kBlock);
   if (smem_bytes)
     *smem_bytes = p->tc ? p->tc_shape.smem_bytes
-                        : (m4 ? p->tcm_shape.smem_bytes : p->shape.smem_bytes);
+                        : (m4 ? p->tcm_shape[k].smem_bytes : p->shape.smem_bytes);
   return DG_OK;
 }
 

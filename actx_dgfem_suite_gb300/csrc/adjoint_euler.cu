@@ -23,7 +23,7 @@ cudaError_t vjp_shape_n(LaunchShape* out) {
 }
 
 template <int N>
-cudaError_t vjp_launch_n(const VjpArgs& a, int grid, int nsm, cudaStream_t s) {
+cudaError_t vjp_launch_n(const VjpArgs& a, int grid, int nsm, bool stage, cudaStream_t s) {
   constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP;
   const int64_t nodes = a.nel * NP;
   const int64_t cap = (int64_t)nsm * 16;
@@ -42,7 +42,10 @@ cudaError_t vjp_launch_n(const VjpArgs& a, int grid, int nsm, cudaStream_t s) {
   dg_euler_vjp_face<N><<<(int)fb, kFaceBlock, 0, s>>>(a);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  dg_vjp_node_gather<N, 5><<<(int)nb, kBlock, 0, s>>>(a);
+  if (stage)
+    dg_vjp_node_gather<N, 5, true><<<(int)nb, kBlock, 0, s>>>(a);
+  else
+    dg_vjp_node_gather<N, 5><<<(int)nb, kBlock, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -58,13 +61,13 @@ cudaError_t vjp_shape_euler(int order, LaunchShape* out) {
   }
 }
 
-cudaError_t vjp_launch_euler(int order, const VjpArgs& a, int grid, int nsm,
+cudaError_t vjp_launch_euler(int order, const VjpArgs& a, int grid, int nsm, bool stage,
                              cudaStream_t s) {
   switch (order) {
-    case 1: return vjp_launch_n<1>(a, grid, nsm, s);
-    case 2: return vjp_launch_n<2>(a, grid, nsm, s);
-    case 3: return vjp_launch_n<3>(a, grid, nsm, s);
-    case 4: return vjp_launch_n<4>(a, grid, nsm, s);
+    case 1: return vjp_launch_n<1>(a, grid, nsm, stage, s);
+    case 2: return vjp_launch_n<2>(a, grid, nsm, stage, s);
+    case 3: return vjp_launch_n<3>(a, grid, nsm, stage, s);
+    case 4: return vjp_launch_n<4>(a, grid, nsm, stage, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -47,6 +47,12 @@ struct VjpArgs {
   int64_t nel;
   int* status;
   double gamma;
+  // reverse-stage epilogue of the node gather (dg_rhs_vjp_stage): with
+  // rbar = xscale x, lam += dt J^T rbar and rbar_out = rk_a rbar + rk_b lam
+  double xscale;
+  double* lam;
+  double* rbar_out;         // or NULL
+  double rk_a, rk_b, dt;
 };
 
 // g = J_n(q)^T z for the Euler flux F(q).n: q = (rho, E, m), rinv = 1/rho,
@@ -333,8 +339,10 @@ __global__ void __launch_bounds__(kFaceBlock) dg_euler_vjp_face(const VjpArgs a)
 }
 
 // y_k(e, i) += sum of the face-point slots of node i (a node lies on at most
-// 3 faces); 32-bit indices.
-template <int N, int NF>
+// 3 faces); 32-bit indices.  STAGE: instead of storing y, every node applies
+// the reverse LSRK stage update to lam and rbar_out (x may be lam or
+// rbar_out: each node reads its x and lam before it writes either).
+template <int N, int NF, bool STAGE = false>
 __global__ void __launch_bounds__(kBlock) dg_vjp_node_gather(const VjpArgs a) {
   using Ops = AdjOpsLayout<N>;
   constexpr int NP = Shape<N>::NP, NFPT = Shape<N>::NFPT;
@@ -354,17 +362,25 @@ __global__ void __launch_bounds__(kBlock) dg_vjp_node_gather(const VjpArgs a) {
        gnode += gridDim.x * blockDim.x) {
     const uint32_t e = gnode / NP;
     const int i = (int)(gnode - e * NP);
-    if (sNodeFP[i][0] < 0) continue;
+    if (!STAGE && sNodeFP[i][0] < 0) continue;
 #pragma unroll
     for (int k = 0; k < NF; ++k) {
-      double acc = a.y[k * (size_t)nelnp + gnode];
+      const size_t o = k * (size_t)nelnp + gnode;
+      double acc = a.y[o];
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         const int fj = sNodeFP[i][m];
         if (fj < 0) break;
         acc += a.scratch[k * (size_t)nfp_all + e * NFPT + fj];
       }
-      a.y[k * (size_t)nelnp + gnode] = acc;
+      if constexpr (STAGE) {
+        const double rb = a.xscale * a.x[o];
+        const double ln = fma(a.dt * a.xscale, acc, a.lam[o]);
+        a.lam[o] = ln;
+        if (a.rbar_out) a.rbar_out[o] = fma(a.rk_a, rb, a.rk_b * ln);
+      } else {
+        a.y[o] = acc;
+      }
     }
   }
 }

@@ -55,7 +55,8 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
 // tc_shape_* / tc_launch_*: the face-shared volume/LIFT kernel with the
 // contractions on the tensor cores (mode 0 RHS, 1 RK stage).
 // tcm_shape_* / tcm_launch_*: the mixed-precision kernel with its
-// contractions on tcgen05 (exact digit-pair products; mode 0 RHS, 1 RK stage).
+// contractions on tcgen05 (mode bit 0: RK stage; bit 1: 3xTF32 products,
+// else exact digit-pair products).
 #define DG_DECLARE_EQ(name)                                                   \
   cudaError_t shape_##name(int order, int precision, int mode,               \
                            LaunchShape* out);                                \
@@ -84,13 +85,15 @@ DG_DECLARE_EQ(maxwell)
 int pack_tc_ops(int eq, int order, const double* diff, const double* lift,
                 unsigned char* out, int out_bytes);
 
-// Operator block of the mixed tcgen05 kernel (tcm::MPlan<N, EQ> in
-// dg_tcm.cuh): [A_0 A_1 A_2] (Np x 3 Np) and LIFT (Np x 4 Nfp), each row
-// scaled to 31-bit integers written as four FP16 digit slices in the K-major
-// no-swizzle layout, then the FP32 row scales 2^e of each, then the int32
-// face node table.  Returns the block size (out == NULL: size only).
+// Operator block of the mixed tcgen05 kernel (tcm::MPlan<N, EQ, tf32> in
+// dg_tcm.cuh): [A_0 A_1 A_2] (Np x 3 Np) and LIFT (Np x 4 Nfp) in the K-major
+// no-swizzle layout of the tcgen05 descriptors; digits (tf32 false): each
+// row scaled to 31-bit integers written as four FP16 digit slices, then the
+// FP32 row scales 2^e of each; tf32: two slices, x = hi + lo in TF32.  Then
+// the int32 face node table.  Returns the block size (out == NULL: size only).
 int pack_tcm_ops(int order, const double* diff, const double* lift,
-                 const int32_t* face_nodes, unsigned char* out, int out_bytes);
+                 const int32_t* face_nodes, unsigned char* out, int out_bytes,
+                 bool tf32);
 
 // Record `msg` as the calling thread's last error (dg_last_error) and
 // return `code`; shared by the translation units behind the C ABI.
@@ -114,9 +117,11 @@ cudaError_t pressure_launch_euler(const double* q, float* pres, int64_t nelnp,
                                   double gamma, int grid, cudaStream_t s);
 
 // Transposed Jacobian of the FP64 Euler RHS (dg_adjoint_euler.cuh): shape of
-// the volume kernel, and the launches (node table, volume, face, node gather).
+// the volume kernel, and the launches (node table, volume, face, node gather;
+// with stage, the gather applies the reverse LSRK stage update instead of
+// storing y).
 cudaError_t vjp_shape_euler(int order, LaunchShape* out);
-cudaError_t vjp_launch_euler(int order, const VjpArgs& a, int grid, int nsm,
+cudaError_t vjp_launch_euler(int order, const VjpArgs& a, int grid, int nsm, bool stage,
                              cudaStream_t s);
 
 }  // namespace dg

@@ -34,6 +34,18 @@
 // unbiased, where TF32 products accumulated by the tensor core lose accuracy
 // with every accumulation step.
 //
+// 3xTF32 form (TF = true, variant 5).  Every value of X and B is split into
+// x = hi + lo, both TF32 (cvt.rna; hi carries 11 significant bits, lo the
+// next 11), and tcgen05.mma kind::tf32 (M = 128, N = NB, K = 8) forms
+// hi hi in one accumulator and hi lo + lo hi in a second one (2^-11 smaller,
+// so its own roundings do not matter); the epilogue adds the two.  No row
+// scaling and no digit fold: the split is three instructions per value
+// against ~30 for the four digits, the volume inputs are computed once and
+// written straight into X, and there are 3 products per k-step instead of
+// 10.  Its error is that of FP32 arithmetic with the tensor core's own
+// accumulation order (FP32 partial sums, no exactness argument), so the
+// bounded autotuner decides per plan whether it is admissible.
+//
 // Per tile of E = 128 / NF elements (8 elements x 4 pairs of nodes or face
 // points per warp; a pair's digits are one 4-byte word per digit slice, and
 // the 32 words a warp stores fall in 32 distinct banks):
@@ -71,7 +83,11 @@ constexpr int pow2_cols(int c) {
   return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
 }
 
-template <int N, int EQ>
+constexpr int rup(int x, int m) { return (x + m - 1) / m * m; }
+
+// Tile plan of the kernel.  TF = false: exact FP16 digit pairs (variant 4);
+// TF = true: 3xTF32 products (variant 5; see dg_rhs_tcm_kernel).
+template <int N, int EQ, bool TF = false>
 struct MPlan {
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
   static constexpr int NF = EqInfo<EQ>::NF;
@@ -83,19 +99,24 @@ struct MPlan {
   // X_V column of derivative r and node j: k = r NPP + j, NPP = Np rounded up
   // to even, so the two nodes a lane writes share one 4-byte word
   static constexpr int NPP = NP + (NP & 1);
-  static constexpr int KV = r16(3 * NPP), KL = r16(NFPT);
-  // K-major, no swizzle: element (m, k) of a digit slice at
-  //   (m / 8) SBO + (k / 8) 128 + (m % 8) 16 + (k % 8) 2 bytes
-  static constexpr int SBO_V = (KV / 8) * 128, SBO_L = (KL / 8) * 128;
+  // operand elements: FP16 digits (2 bytes) or TF32 parts (4 bytes); a
+  // core-matrix row holds 16 bytes (KG elements), one MMA consumes two core
+  // matrices along K (KSTEP = 16 FP16 or 8 TF32 values)
+  static constexpr int ESZ = TF ? 4 : 2, KG = 16 / ESZ, KSTEP = 2 * KG;
+  static constexpr int KV = rup(3 * NPP, KSTEP), KL = rup(NFPT, KSTEP);
+  // K-major, no swizzle: element (m, k) of a slice at
+  //   (m / 8) SBO + (k / KG) 128 + (m % 8) 16 + (k % KG) ESZ bytes
+  static constexpr int SBO_V = (KV / KG) * 128, SBO_L = (KL / KG) * 128;
   static constexpr int A_SLICE_V = 16 * SBO_V, A_SLICE_L = 16 * SBO_L;
-  static constexpr int NDIG = 4;  // digits per value
+  static constexpr int NDIG = TF ? 2 : 4;  // slices per value: digits, or TF32 hi / lo
   static constexpr int A_BYTES = NDIG * (A_SLICE_V > A_SLICE_L ? A_SLICE_V : A_SLICE_L);
-  // operator block (global and shared): B_V digits (4 slices) | B_L digits |
-  // FP32 row scales 2^e of B_V | of B_L (|B_ik| < 2^e) | int32 face nodes
+  // operator block (global and shared): B_V slices | B_L slices | (digits
+  // only) FP32 row scales 2^e of B_V | of B_L (|B_ik| < 2^e) | int32 face nodes
   static constexpr int B_SLICE_V = (NB / 8) * SBO_V, B_SLICE_L = (NB / 8) * SBO_L;
   static constexpr int OPS_V = 0, OPS_L = NDIG * B_SLICE_V;
-  static constexpr int OPS_EV = OPS_L + NDIG * B_SLICE_L, OPS_EL = OPS_EV + NB * 4;
-  static constexpr int OPS_FN = OPS_EL + NB * 4;
+  static constexpr int OPS_EV = OPS_L + NDIG * B_SLICE_L;
+  static constexpr int OPS_EL = OPS_EV + (TF ? 0 : NB * 4);
+  static constexpr int OPS_FN = OPS_EL + (TF ? 0 : NB * 4);
   static constexpr int OPS_BYTES = OPS_FN + p16(NFPT * 4);
   static constexpr int QP = pitch_q(NP);  // FP32 state rows
   static constexpr int OP = NP | 1;       // FP32 result rows (odd pitch)
@@ -104,17 +125,23 @@ struct MPlan {
   static constexpr int SM_Q = SM_OPS + OPS_BYTES;
   static constexpr int SM_G = SM_Q + p16(NF * E * QP * 4);
   static constexpr int SM_OUT = SM_G + p16(9 * E * 4);
-  static constexpr int SM_RMAX = SM_OUT + p16(NCOL * OP * 4);  // [2 tiles][2 phases][128]
-  static constexpr int SM_P = SM_RMAX + 4 * 128 * 4;  // euler: node pressures (FP32)
+  // digits only: row maxima [2 tiles][2 phases][128]
+  static constexpr int SM_RMAX = SM_OUT + p16(NCOL * OP * 4);
+  static constexpr int SM_P = SM_RMAX + (TF ? 0 : 4 * 128 * 4);  // euler: node pressures
   static constexpr int SMEM_BYTES = SM_P + (EQ == DG_EULER ? p16(E * NP * 4) : 0);
-  // accumulators: levels 0..3 of the volume phase, then of the LIFT phase
-  static constexpr int ACC_L = 4 * NB;
-  static constexpr int TMEM_COLS = pow2_cols(8 * NB);
-  // instruction descriptor: D FP32, A and B FP16, both K-major, N, M = 128
-  static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(NB >> 3) << 17) | (8u << 24);
+  // accumulators of the volume phase, then of the LIFT phase: levels 0..3
+  // (digits), or hi x hi and the two cross terms (TF32)
+  static constexpr int NACC = TF ? 2 : 4;
+  static constexpr int ACC_L = NACC * NB;
+  static constexpr int TMEM_COLS = pow2_cols(2 * NACC * NB);
+  // instruction descriptor: D FP32, A and B FP16 (0) or TF32 (2), both
+  // K-major, N, M = 128
+  static constexpr uint32_t IDESC = (1u << 4) | (TF ? (2u << 7) | (2u << 10) : 0u) |
+                                    ((uint32_t)(NB >> 3) << 17) | (8u << 24);
   static_assert(NCOL <= 128, "one 128-row product per tile");
   static_assert(NB >= 16 && NB <= 256, "MMA N range");
-  static_assert(KV <= 128 && KL <= 128, "level sums (4 pairs) of at most 2^23 need K <= 128");
+  static_assert(TF || (KV <= 128 && KL <= 128),
+                "level sums (4 pairs) of at most 2^23 need K <= 128");
   static_assert(TMEM_COLS <= 512, "accumulators fit in tensor memory");
   static_assert(SMEM_BYTES <= 227 * 1024, "tile does not fit in shared memory");
 };
@@ -140,8 +167,58 @@ __device__ __forceinline__ FluxConsts flux_consts(const RhsArgs& a) {
   return f;
 }
 
+// byte offset of element (m, k) in a K-major slice of KG elements per
+// 16-byte core-matrix row
+template <int KG = 8>
 __device__ __forceinline__ int kmajor_off(int m, int k, int sbo) {
-  return (m >> 3) * sbo + (k >> 3) * 128 + (m & 7) * 16 + (k & 7) * 2;
+  return (m >> 3) * sbo + (k / KG) * 128 + (m & 7) * 16 + (k % KG) * (16 / KG);
+}
+
+// x -> TF32 (round to nearest, ties away from zero), as a bit pattern
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// two values of one row at columns k, k + 1 (k even: one 8-byte word per
+// slice) -> x = hi + lo, both TF32, hi in the first slice, lo in the second
+__device__ __forceinline__ void put_tf32x2(unsigned char* base, int slice, int off, float x0,
+                                           float x1) {
+  const uint32_t h0 = tf32_bits(x0), h1 = tf32_bits(x1);
+  const uint32_t l0 = tf32_bits(x0 - __uint_as_float(h0));
+  const uint32_t l1 = tf32_bits(x1 - __uint_as_float(h1));
+  *reinterpret_cast<uint2*>(base + off) = make_uint2(h0, h1);
+  *reinterpret_cast<uint2*>(base + slice + off) = make_uint2(l0, l1);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+      ::"r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// One phase of 3xTF32 products: per k-step of 8, hi x hi into acc and
+// hi x lo + lo x hi into acc + NB (the cross terms, 2^-11 smaller, in an
+// accumulator of their own so that they do not lengthen the main sum's
+// chain of roundings).
+template <int K, int SBO, int A_SLICE, int B_SLICE, int NB>
+__device__ __forceinline__ void issue_phase_tf32(uint32_t a_s, uint32_t b_s, uint32_t acc,
+                                                 uint32_t idesc) {
+  tc::tc_fence_after();
+#pragma unroll 1
+  for (int kt = 0; kt < K / 8; ++kt) {
+    const uint32_t ka = a_s + kt * 256, kb = b_s + kt * 256;
+    const uint64_t ah = tc::smem_desc(ka, 128, SBO), al = tc::smem_desc(ka + A_SLICE, 128, SBO);
+    const uint64_t bh = tc::smem_desc(kb, 128, SBO), bl = tc::smem_desc(kb + B_SLICE, 128, SBO);
+    const uint32_t more = kt > 0 ? 1u : 0u;
+    mma_tf32(acc, ah, bh, idesc, more);
+    mma_tf32(acc + (uint32_t)NB, ah, bl, idesc, more);
+    mma_tf32(acc + (uint32_t)NB, al, bh, idesc, 1u);
+  }
 }
 
 // 2^s as a float for s in [-126, 127]
@@ -326,12 +403,13 @@ __device__ __forceinline__ void face_point_flux(const FluxConsts& fc, const floa
 
 }  // namespace tcm
 
-template <int N, int EQ, int MODE>
-__global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>::MIN_BLOCKS)
+template <int N, int EQ, int MODE, bool TF = false>
+__global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
+                                  tcm::MPlan<N, EQ, TF>::MIN_BLOCKS)
     dg_rhs_tcm_kernel(const RhsArgs a) {
-  using P = tcm::MPlan<N, EQ>;
+  using P = tcm::MPlan<N, EQ, TF>;
   constexpr int NP = P::NP, NFP = P::NFP, NFPT = P::NFPT, NF = P::NF, E = P::E;
-  constexpr int QP = P::QP, OP = P::OP, NB = P::NB, THREADS = P::THREADS;
+  constexpr int QP = P::QP, OP = P::OP, NB = P::NB, THREADS = P::THREADS, KG = P::KG;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
   constexpr int NWARP = THREADS / 32;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -367,7 +445,8 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
   // columns or unused rows; it must hold finite values, so clear X once
   for (int idx = t; idx < P::A_BYTES / 16; idx += THREADS)
     reinterpret_cast<uint4*>(sA)[idx] = make_uint4(0u, 0u, 0u, 0u);
-  for (int idx = t; idx < 4 * 128; idx += THREADS) sRmax[idx] = 0u;
+  if constexpr (!TF)
+    for (int idx = t; idx < 4 * 128; idx += THREADS) sRmax[idx] = 0u;
   __syncthreads();
   if (!ops_ok) return;
   if (warp == 0) {
@@ -448,12 +527,13 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
     const int ecount = (nel - e0) < (int64_t)E ? (int)(nel - e0) : E;
     unsigned* rmaxV = sRmax + (it & 1) * 256;  // this tile's row maxima
     unsigned* rmaxL = rmaxV + 128;
-    {  // the other buffer was last read before the previous tile's final barrier
+    if constexpr (!TF) {  // the other buffer was last read before the previous tile's final barrier
       unsigned* other = sRmax + ((it + 1) & 1) * 256;
       for (int idx = t; idx < 256; idx += THREADS) other[idx] = 0u;
     }
 
-    // {{{ 1. state -> FP32 copies, volume inputs -> row maxima
+    // {{{ 1. state -> FP32 copies, volume inputs -> row maxima (digits) or
+    //        straight into X_V as TF32 pairs
     for (int u = warp; u < EG * JG; u += NWARP) {
       const int e = (u % EG) * 8 + (lane & 7);
       const int j0 = 2 * ((u / EG) * 4 + (lane >> 3));
@@ -468,6 +548,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
       float m[NF];
 #pragma unroll
       for (int c = 0; c < NF; ++c) m[c] = 0.f;
+      [[maybe_unused]] float wt[2][NF][3];  // TF32: both nodes' inputs
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int j = j0 + h;
@@ -489,22 +570,40 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
         }
         float w[NF][3];
         vol_inputs(qf, G, p, rinv, w);
-        if (item) {
+        if constexpr (TF) {  // a node past Np is the zero padding column
+#pragma unroll
+          for (int c = 0; c < NF; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) wt[h][c][r] = item ? w[c][r] : 0.f;
+        } else if (item) {
 #pragma unroll
           for (int c = 0; c < NF; ++c)
             m[c] = fmaxf(m[c], fmaxf(fabsf(w[c][0]), fmaxf(fabsf(w[c][1]), fabsf(w[c][2]))));
         }
       }
+      if constexpr (TF) {
+        if (ein && j0 < NP) {
 #pragma unroll
-      for (int c = 0; c < NF; ++c)
-        tcm::row_max(rmaxV, c * E + (ein ? e : 0), m[c], (lane >> 3) == 0 && ein);
+          for (int c = 0; c < NF; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+              tcm::put_tf32x2(sA, P::A_SLICE_V,
+                              tcm::kmajor_off<KG>(c * E + e, r * NPP + j0, P::SBO_V),
+                              wt[0][c][r], wt[1][c][r]);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < NF; ++c)
+          tcm::row_max(rmaxV, c * E + (ein ? e : 0), m[c], (lane >> 3) == 0 && ein);
+      }
     }
+    if constexpr (TF) tc::fence_async_smem();
     __syncthreads();
     // }}}
 
-    // {{{ 2. volume inputs -> digits of X_V (node pairs; a node past Np is the
-    //        zero padding column)
-    for (int u = warp; u < EG * JG; u += NWARP) {
+    // {{{ 2. (digits) volume inputs -> digits of X_V (node pairs; a node past
+    //        Np is the zero padding column)
+    for (int u = warp; u < (TF ? 0 : EG * JG); u += NWARP) {
       const int e = (u % EG) * 8 + (lane & 7);
       const int j0 = 2 * ((u / EG) * 4 + (lane >> 3));
       if (e >= E || j0 >= NP) continue;
@@ -533,15 +632,21 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
                            w0[c][r], two ? w1[c][r] : 0.f, ex);
       }
     }
-    tc::fence_async_smem();
-    __syncthreads();
+    if constexpr (!TF) {
+      tc::fence_async_smem();
+      __syncthreads();
+    }
     // }}}
 
     // {{{ 3. volume products (one thread); face fluxes (registers) and their
     //        row maxima; then X_L and the LIFT products
     if (t == 0) {
-      tcm::issue_phase<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V, NB>(a_s, b_s + P::OPS_V,
-                                                                       tmem, P::IDESC);
+      if constexpr (TF)
+        tcm::issue_phase_tf32<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V, NB>(
+            a_s, b_s + P::OPS_V, tmem, P::IDESC);
+      else
+        tcm::issue_phase<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V, NB>(
+            a_s, b_s + P::OPS_V, tmem, P::IDESC);
       tc::tc_commit(&mma_bar);
       led.issue(0);
     }
@@ -591,7 +696,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
         }
         fm[rd] = e | (fj0 << 8);
       }
-      if (u < EG * FG) {  // warp-uniform: every lane joins the shuffles
+      if (!TF && u < EG * FG) {  // warp-uniform: every lane joins the shuffles
 #pragma unroll
         for (int c = 0; c < NF; ++c)
           tcm::row_max(rmaxL, c * E + (e < E ? e : 0),
@@ -608,15 +713,23 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
         const int m = c * E + e;
-        tcm::put_digits2(sA, P::A_SLICE_L, tcm::kmajor_off(m, fj0, P::SBO_L), fv[rd][0][c],
-                         fv[rd][1][c], tcm::row_exp_bits(rmaxL[m]));
+        if constexpr (TF)
+          tcm::put_tf32x2(sA, P::A_SLICE_L, tcm::kmajor_off<KG>(m, fj0, P::SBO_L),
+                          fv[rd][0][c], fv[rd][1][c]);
+        else
+          tcm::put_digits2(sA, P::A_SLICE_L, tcm::kmajor_off(m, fj0, P::SBO_L), fv[rd][0][c],
+                           fv[rd][1][c], tcm::row_exp_bits(rmaxL[m]));
       }
     }
     tc::fence_async_smem();
     __syncthreads();
     if (t == 0) {
-      tcm::issue_phase<P::KL, P::SBO_L, P::A_SLICE_L, P::B_SLICE_L, NB>(
-          a_s, b_s + P::OPS_L, tmem + P::ACC_L, P::IDESC);
+      if constexpr (TF)
+        tcm::issue_phase_tf32<P::KL, P::SBO_L, P::A_SLICE_L, P::B_SLICE_L, NB>(
+            a_s, b_s + P::OPS_L, tmem + P::ACC_L, P::IDESC);
+      else
+        tcm::issue_phase<P::KL, P::SBO_L, P::A_SLICE_L, P::B_SLICE_L, NB>(
+            a_s, b_s + P::OPS_L, tmem + P::ACC_L, P::IDESC);
       tc::tc_commit(&mma_bar);
       led.issue(0);
     }
@@ -624,7 +737,33 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ>::THREADS, tcm::MPlan<N, EQ>:
     // }}}
 
     // {{{ 4. level sums -> staging (warp w reads lanes 32 (w % 4)..), epilogue
-    {
+    if constexpr (TF) {
+      const int qd = warp & 3;
+      const int row = 32 * qd + lane;
+      const uint32_t tq = tmem + ((uint32_t)(32 * qd) << 16);
+      float sc = 1.f;
+      if constexpr (EQ == DG_MAXWELL) sc = (row / E) < 3 ? fc.ie : fc.im;
+#pragma unroll 1
+      for (int ch = warp >> 2; ch < NB / 8; ch += NWARP / 4) {
+        uint32_t v[16], l[16];  // hi x hi, cross terms x 8 columns
+        tc::tc_ld8(tq + (uint32_t)(ch * 8), v);
+        tc::tc_ld8(tq + (uint32_t)(NB + ch * 8), v + 8);
+        tc::tc_ld8(tq + (uint32_t)(P::ACC_L + ch * 8), l);
+        tc::tc_ld8(tq + (uint32_t)(P::ACC_L + NB + ch * 8), l + 8);
+        tc::tc_wait_ld();
+        if (row < P::NCOL) {
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const int col = ch * 8 + jj;
+            if (col < NP) {
+              const float vol = __uint_as_float(v[jj]) + __uint_as_float(v[8 + jj]);
+              const float lift = __uint_as_float(l[jj]) + __uint_as_float(l[8 + jj]);
+              sOut[row * OP + col] = sc * (vol + lift);
+            }
+          }
+        }
+      }
+    } else {
       const int qd = warp & 3;
       const int row = 32 * qd + lane;
       const uint32_t tq = tmem + ((uint32_t)(32 * qd) << 16);

@@ -237,10 +237,10 @@ cudaError_t tc_launch_any(int order, int mode, const RhsArgs& a, int grid,
 
 // {{{ mixed precision with tcgen05 contractions (fused face fluxes)
 
-template <int N, int EQ, int MODE>
+template <int N, int EQ, int MODE, bool TF>
 cudaError_t tcm_shape_impl(LaunchShape* out) {
-  using P = tcm::MPlan<N, EQ>;
-  auto kern = dg_rhs_tcm_kernel<N, EQ, MODE>;
+  using P = tcm::MPlan<N, EQ, TF>;
+  auto kern = dg_rhs_tcm_kernel<N, EQ, MODE, TF>;
   cudaError_t err = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
   if (err != cudaSuccess) return err;
@@ -271,25 +271,37 @@ cudaError_t tcm_shape_impl(LaunchShape* out) {
   return err;
 }
 
+// mode bit 0: fused RK stage; bit 1: 3xTF32 products instead of exact digits
 template <int N, int EQ>
 cudaError_t tcm_shape_n(int mode, LaunchShape* out) {
-  return mode == 0 ? tcm_shape_impl<N, EQ, MODE_RHS>(out)
-                   : tcm_shape_impl<N, EQ, MODE_STAGE>(out);
+  switch (mode) {
+    case 0: return tcm_shape_impl<N, EQ, MODE_RHS, false>(out);
+    case 1: return tcm_shape_impl<N, EQ, MODE_STAGE, false>(out);
+    case 2: return tcm_shape_impl<N, EQ, MODE_RHS, true>(out);
+    default: return tcm_shape_impl<N, EQ, MODE_STAGE, true>(out);
+  }
+}
+
+template <int N, int EQ, int MODE, bool TF>
+cudaError_t tcm_launch_impl(const RhsArgs& a, int grid, cudaStream_t s) {
+  using P = tcm::MPlan<N, EQ, TF>;
+  dg_rhs_tcm_kernel<N, EQ, MODE, TF><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
+  return cudaGetLastError();
 }
 
 template <int N, int EQ>
 cudaError_t tcm_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
-  using P = tcm::MPlan<N, EQ>;
-  if (mode == 0)
-    dg_rhs_tcm_kernel<N, EQ, MODE_RHS><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
-  else
-    dg_rhs_tcm_kernel<N, EQ, MODE_STAGE><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
-  return cudaGetLastError();
+  switch (mode) {
+    case 0: return tcm_launch_impl<N, EQ, MODE_RHS, false>(a, grid, s);
+    case 1: return tcm_launch_impl<N, EQ, MODE_STAGE, false>(a, grid, s);
+    case 2: return tcm_launch_impl<N, EQ, MODE_RHS, true>(a, grid, s);
+    default: return tcm_launch_impl<N, EQ, MODE_STAGE, true>(a, grid, s);
+  }
 }
 
 template <int EQ>
 cudaError_t tcm_shape_any(int order, int mode, LaunchShape* out) {
-  if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
+  if (mode < 0 || mode > 3) return cudaErrorInvalidValue;
   switch (order) {
     case 1: return tcm_shape_n<1, EQ>(mode, out);
     case 2: return tcm_shape_n<2, EQ>(mode, out);
@@ -302,7 +314,7 @@ cudaError_t tcm_shape_any(int order, int mode, LaunchShape* out) {
 template <int EQ>
 cudaError_t tcm_launch_any(int order, int mode, const RhsArgs& a, int grid,
                            cudaStream_t s) {
-  if (mode != 0 && mode != 1) return cudaErrorInvalidValue;
+  if (mode < 0 || mode > 3) return cudaErrorInvalidValue;
   switch (order) {
     case 1: return tcm_launch_n<1, EQ>(mode, a, grid, s);
     case 2: return tcm_launch_n<2, EQ>(mode, a, grid, s);

@@ -250,9 +250,11 @@ class DevicePlan:
             ptr(cbar), float(a), float(b), float(dt), ptr(y_scratch),
             _stream_handle(stream)))
 
-    #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per tile
+    #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per
+    #: tile; 4 and 5 the tcgen05 kernel (exact digit pairs, 3xTF32)
     VARIANTS = {0: "persistent", 1: "tensor-core, persistent", 2: "one CTA per tile",
-                3: "tensor-core, one CTA per tile", 4: "tcgen05, persistent"}
+                3: "tensor-core, one CTA per tile", 4: "tcgen05, persistent",
+                5: "tcgen05 3xTF32, persistent"}
 
     def set_variant(self, variant: int) -> None:
         _lib.check(self._lib.dg_plan_set_variant(self._handle, int(variant)))
@@ -270,7 +272,8 @@ class DevicePlan:
         self._check_tensor(q, "state")
         out = torch.empty_like(q)
         chosen = ctypes.c_int32()
-        ms = (ctypes.c_float * 5)()
+        nv = len(self.VARIANTS)
+        ms = (ctypes.c_float * nv)()
         if ref is None:
             _lib.check(self._lib.dg_plan_autotune(
                 self._handle, ctypes.c_void_p(q.data_ptr()),
@@ -281,7 +284,7 @@ class DevicePlan:
             self._check_tensor(ref, "ref")
             if max_rel_l2 is None:
                 raise ValueError("max_rel_l2 is required with ref")
-            errs = (ctypes.c_double * 5)()
+            errs = (ctypes.c_double * nv)()
             _lib.check(self._lib.dg_plan_autotune_bounded(
                 self._handle, ctypes.c_void_p(q.data_ptr()),
                 ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ref.data_ptr()),
@@ -289,11 +292,11 @@ class DevicePlan:
                 ctypes.byref(chosen), ms, errs))
         res = {"chosen": chosen.value,
                "ms": {self.VARIANTS[v]: (float(ms[v]) if ms[v] >= 0 else None)
-                      for v in range(5)}}
+                      for v in range(nv)}}
         if errs is not None:
             res["max_rel_l2"] = float(max_rel_l2)
             res["rel_l2"] = {self.VARIANTS[v]: (float(errs[v]) if errs[v] >= 0 else None)
-                             for v in range(5)}
+                             for v in range(nv)}
         return res
 
     def vjp(self, q: torch.Tensor, x: torch.Tensor, out: torch.Tensor | None = None,
@@ -309,6 +312,22 @@ class DevicePlan:
             self._handle, ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(x.data_ptr()),
             ctypes.c_void_p(out.data_ptr()), _stream_handle(stream)))
         return out
+
+    def vjp_stage(self, q: torch.Tensor, x: torch.Tensor, xscale: float,
+                  lam: torch.Tensor, rbar_out: torch.Tensor | None, a: float, b: float,
+                  dt: float, y_scratch: torch.Tensor, stream=None) -> None:
+        """One fused reverse LSRK stage of the operator linearised at the stage
+        input ``q`` (``dg_rhs_vjp_stage``): ``lam += dt (dL/dq)^T (xscale x)``;
+        ``rbar_out = a xscale x + b lam``.  ``x`` may be ``lam`` or
+        ``rbar_out`` itself."""
+        for t, name in ((q, "q"), (x, "x"), (lam, "lam"), (y_scratch, "y_scratch")):
+            self._check_tensor(t, name)
+        if rbar_out is not None:
+            self._check_tensor(rbar_out, "rbar_out")
+        ptr = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        _lib.check(self._lib.dg_rhs_vjp_stage(
+            self._handle, ptr(q), ptr(x), float(xscale), ptr(lam), ptr(rbar_out),
+            float(a), float(b), float(dt), ptr(y_scratch), _stream_handle(stream)))
 
     def finish(self, stream=None) -> None:
         _lib.check(self._lib.dg_finish(self._handle, _stream_handle(stream)))

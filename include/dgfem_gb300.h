@@ -173,6 +173,25 @@ int dg_rhs_adjoint_stage(dg_plan* plan, const double* x, double xscale, double* 
 int dg_rhs_vjp(dg_plan* plan, const double* q, const double* x, double* y,
                void* stream);
 
+/* One reverse LSRK stage of a nonlinear operator, fused: for the forward
+ * stage r^s = a_s r^{s-1} + dt L(q^(s)), q^(s+1) = q^(s) + b_s r^s and the
+ * stage's residual adjoint rbar_s = xscale * x:
+ *   lam      += dt (dL/dq (q^(s)))^T rbar_s          (in place)
+ *   rbar_out  = a * rbar_s + b * lam                 (skipped if NULL)
+ * with q = q^(s), the stage's input state, a = a_s and b = b_{s-1}.  The
+ * launches of dg_rhs_vjp, whose last one (the node gather) applies the two
+ * updates instead of storing the product, so that the stage reads and
+ * writes each state-sized array once.  x may be lam itself (the first
+ * reverse stage of a step: rbar_4 = b_4 lam, xscale = b_4) and rbar_out may
+ * be x itself; q and y_scratch (nfields * Nel * Np doubles) may overlap
+ * nothing that is written.  For a wave plan q is not read and the call is
+ * dg_rhs_adjoint_stage without the element-scale gradient.  Uses the plan's
+ * face buffers: do not run it concurrently with other calls on the plan.
+ * No counterpart in the reference (which has no adjoint). */
+int dg_rhs_vjp_stage(dg_plan* plan, const double* q, const double* x, double xscale,
+                     double* lam, double* rbar_out, double a, double b, double dt,
+                     double* y_scratch, void* stream);
+
 /* Size of the device buffer that dg_rhs_adjoint_noalloc works in. */
 #define DG_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 
@@ -241,21 +260,26 @@ typedef struct dg_box_desc {
 
 int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 
+/* Number of launch variants (0 .. DG_NUM_VARIANTS - 1). */
+#define DG_NUM_VARIANTS 6
+
 /* Launch variant of the plan's main kernel: bit 0 = contractions on the
  * tensor cores (DG_FP32_MIXED plans: 3xTF32 split with FP32 accumulation,
  * i.e. FP32 accuracy, as warp-level mma.sync), bit 1 = one CTA per tile
- * instead of the persistent grid; 4 = the DG_FP32_MIXED kernel with its
- * volume and LIFT contractions as one tcgen05 product per tile (rows scaled
- * to 31-bit integers in four FP16 digits, digit-pair products accumulated
- * exactly in tensor memory: the most accurate mixed variant; persistent
- * grid).
+ * instead of the persistent grid; 4 and 5 = the DG_FP32_MIXED kernel with
+ * its volume and LIFT contractions as one tcgen05 product per 128-row tile
+ * (persistent grid): 4 with rows scaled to 31-bit integers in four FP16
+ * digits and the digit-pair products accumulated exactly in tensor memory
+ * (the most accurate mixed variant), 5 with both operands split into TF32
+ * pairs hi + lo and the products hi hi + hi lo + lo hi accumulated in FP32
+ * (FP32 accuracy, far fewer instructions per tile).
  * Default 0.  No counterpart in the reference. */
 int dg_plan_set_variant(dg_plan* plan, int32_t variant);
 
 /* Time every variant the plan supports (after one warm-up launch, `reps`
  * launches of dg_rhs(q -> rhs) each, CUDA events on `stream`), keep the
  * fastest and report it in *chosen (may be NULL); ms_per_variant (may be
- * NULL) receives 5 floats (variants 0..4), -1 for variants the plan does
+ * NULL) receives DG_NUM_VARIANTS floats, -1 for variants the plan does
  * not support and for variants whose launches raised a device-side status
  * (DG_ERR_TIMEOUT, DG_ERR_INDEX; read and cleared after each variant, and
  * such a variant is never chosen).
@@ -270,7 +294,8 @@ int dg_plan_autotune(dg_plan* plan, const double* q, double* rhs, int32_t reps,
  * timed launches each variant's result is compared with ref, and only
  * variants with ||rhs - ref|| / ||ref|| <= max_rel_l2 compete on time.  If
  * none meets the bound, the most accurate variant is kept.  err_per_variant
- * (may be NULL) receives 5 doubles, -1 where ms_per_variant is -1.  The
+ * (may be NULL) receives DG_NUM_VARIANTS doubles, -1 where ms_per_variant
+ * is -1.  The
  * reference checks every array context against its numpy context after the
  * first call (actx_dgfem_suite/run/__main__.py:87-96); this applies such a
  * tolerance to the choice of kernel. */
@@ -329,7 +354,8 @@ const char* dg_last_error(void);
 /* ABI version, bumped on any incompatible change (3: dg_plan_autotune
  * writes 5 floats to ms_per_variant, variant 4 added; 4: variants that
  * raise a device-side status report -1, dg_plan_autotune_bounded and
- * dg_rhs_adjoint_stage added). */
+ * dg_rhs_adjoint_stage added; 5: dg_rhs_vjp_stage and variant 5 added, the
+ * autotuners write DG_NUM_VARIANTS = 6 entries). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus

@@ -35,7 +35,7 @@ def test_library_exports_all_declared_symbols():
 
 def test_version_and_error_strings():
     L = _lib.lib()
-    assert L.dg_abi_version() == 4
+    assert L.dg_abi_version() == 5
     assert isinstance(L.dg_last_error(), bytes)
 
 

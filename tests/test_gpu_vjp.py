@@ -127,3 +127,62 @@ def test_euler_misfit_gradient_matches_finite_differences():
         fd = (float(loss(q0 + eps * dq)) - float(loss(q0 - eps * dq))) / (2 * eps)
     an = float(torch.sum(qv.grad * dq))
     assert abs(an - fd) <= 1e-5 * abs(fd), (an, fd)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("alias", ["none", "x_is_lam", "rbar_in_place"])
+def test_fused_vjp_stage_matches_composition(order, alias):
+    """dg_rhs_vjp_stage == the same reverse stage composed from dg_rhs_vjp and
+    elementwise operations: lam += dt L'(q)^T rbar, rbar_out = a rbar + b lam,
+    with a per-element scale and the aliasing the reverse sweep uses (x = lam
+    on its first stage, rbar updated in place)."""
+    prob, plan = _plan("euler", order, seed=20 + order)
+    rng = np.random.default_rng(40 + order)
+    shape = prob.fields.shape
+    q = torch.from_numpy(_euler_state(shape, rng)).cuda()
+    plan.set_element_scale(torch.from_numpy(rng.uniform(0.5, 1.5, shape[1])).cuda())
+    lam = torch.from_numpy(rng.standard_normal(shape)).cuda()
+    x = lam.clone() if alias == "x_is_lam" else torch.from_numpy(
+        rng.standard_normal(shape)).cuda()
+    xscale, a, b, dt = (0.7, -0.4, 0.3, 1e-2)
+    rb = xscale * x
+    lam_ref = lam + dt * plan.vjp(q, rb)
+    rbar_ref = a * rb + b * lam_ref
+    ysc = torch.empty_like(x)
+    if alias == "x_is_lam":
+        xin, out = lam, torch.empty_like(x)
+    elif alias == "rbar_in_place":
+        xin = out = x
+    else:
+        xin, out = x, torch.empty_like(x)
+    plan.vjp_stage(q, xin, xscale, lam, out, a, b, dt, ysc)
+    plan.finish()
+    for got, ref in ((lam, lam_ref), (out, rbar_ref)):
+        err = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+        assert err <= 1e-14, err
+
+
+def test_vjp_stage_wave_plan_and_overlap_errors():
+    """On a wave plan dg_rhs_vjp_stage is dg_rhs_adjoint_stage without the
+    element-scale gradient; overlapping q or scratch arrays are refused."""
+    from actx_dgfem_suite_gb300._lib import DGError
+    prob, plan = _plan("wave", 2)
+    rng = np.random.default_rng(1)
+    shape = prob.fields.shape
+    lam = torch.from_numpy(rng.standard_normal(shape)).cuda()
+    x = torch.from_numpy(rng.standard_normal(shape)).cuda()
+    lam2 = lam.clone()
+    out1, out2, ysc = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    plan.vjp_stage(x, x, 0.5, lam, out1, 0.2, 0.3, 1e-2, ysc)
+    plan.adjoint_stage(x, 0.5, lam2, out2, None, None, 0.2, 0.3, 1e-2, ysc)
+    plan.finish()
+    assert torch.equal(lam, lam2) and torch.equal(out1, out2)
+    eprob, eplan = _plan("euler", 2)
+    eshape = eprob.fields.shape
+    q = torch.from_numpy(_euler_state(eshape, rng)).cuda()
+    ex = torch.from_numpy(rng.standard_normal(eshape)).cuda()
+    elam, eysc = torch.zeros_like(ex), torch.empty_like(ex)
+    with pytest.raises(DGError):
+        eplan.vjp_stage(q, ex, 1.0, q, None, 0.2, 0.3, 1e-2, eysc)      # lam is q
+    with pytest.raises(DGError):
+        eplan.vjp_stage(q, ex, 1.0, elam, None, 0.2, 0.3, 1e-2, elam)   # scratch is lam
