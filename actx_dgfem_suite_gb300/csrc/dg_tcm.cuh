@@ -123,10 +123,17 @@ struct MPlan {
   static constexpr int SM_A = 0;
   static constexpr int SM_OPS = SM_A + A_BYTES;
   static constexpr int SM_Q = SM_OPS + OPS_BYTES;
+  // FP32 metric (9 values at a pitch of 12 per element) and face geometry
+  // (n_x, n_y, n_z, sJ/J per face), converted once per tile
   static constexpr int SM_G = SM_Q + p16(NF * E * QP * 4);
-  static constexpr int SM_OUT = SM_G + p16(9 * E * 4);
+  static constexpr int SM_FG = SM_G + p16(12 * E * 4);
+  // FP32 results.  TF32: staged over X once the LIFT products have read it
+  // (X's padding then holds finite FP32 values, harmless against the zero
+  // operator columns); digits: a region of their own, since FP32 bit
+  // patterns read as FP16 digits may be infinite or NaN in X's padding
+  static constexpr int SM_OUT = TF ? SM_A : SM_FG + p16(16 * E * 4);
   // digits only: row maxima [2 tiles][2 phases][128]
-  static constexpr int SM_RMAX = SM_OUT + p16(NCOL * OP * 4);
+  static constexpr int SM_RMAX = TF ? SM_FG + p16(16 * E * 4) : SM_OUT + p16(NCOL * OP * 4);
   static constexpr int SM_P = SM_RMAX + (TF ? 0 : 4 * 128 * 4);  // euler: node pressures
   static constexpr int SMEM_BYTES = SM_P + (EQ == DG_EULER ? p16(E * NP * 4) : 0);
   // accumulators of the volume phase, then of the LIFT phase: levels 0..3
@@ -143,6 +150,7 @@ struct MPlan {
   static_assert(TF || (KV <= 128 && KL <= 128),
                 "level sums (4 pairs) of at most 2^23 need K <= 128");
   static_assert(TMEM_COLS <= 512, "accumulators fit in tensor memory");
+  static_assert(NCOL * OP * 4 <= A_BYTES, "result staging fits over X");
   static_assert(SMEM_BYTES <= 227 * 1024, "tile does not fit in shared memory");
 };
 
@@ -425,6 +433,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
   const float* sEL = reinterpret_cast<const float*>(smem + P::SM_OPS + P::OPS_EL);
   float* sq = reinterpret_cast<float*>(smem + P::SM_Q);
   float* sG = reinterpret_cast<float*>(smem + P::SM_G);
+  float* sFG = reinterpret_cast<float*>(smem + P::SM_FG);
   float* sOut = reinterpret_cast<float*>(smem + P::SM_OUT);
   unsigned* sRmax = reinterpret_cast<unsigned*>(smem + P::SM_RMAX);
   float* sP = reinterpret_cast<float*>(smem + P::SM_P);  // euler: node pressures
@@ -521,6 +530,22 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
     }
   };
 
+  // a tile's metric and face geometry in FP32 (coalesced loads); the first
+  // tile's here, every further tile's while the previous tile's LIFT
+  // products run
+  auto stage_geometry = [&](int64_t tile) {
+    const int64_t g0 = tile * E;
+    const int cnt = (nel - g0) < (int64_t)E ? (int)(nel - g0) : E;
+    for (int idx = t; idx < 9 * E; idx += THREADS) {
+      const int e = idx / 9;
+      sG[e * 12 + (idx - e * 9)] = e < cnt ? d2f_alu(__ldg(a.metric + g0 * 9 + idx)) : 0.f;
+    }
+    for (int idx = t; idx < 16 * E; idx += THREADS)
+      sFG[idx] = idx < 16 * cnt ? d2f_alu(__ldg(a.face_geom + g0 * 16 + idx)) : 0.f;
+  };
+  if (blockIdx.x < ntiles) stage_geometry(blockIdx.x);
+  __syncthreads();
+
   int it = 0;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
     const int64_t e0 = tile * E;
@@ -531,6 +556,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
       unsigned* other = sRmax + ((it + 1) & 1) * 256;
       for (int idx = t; idx < 256; idx += THREADS) other[idx] = 0u;
     }
+    const bool pair_loads = (NP % 2 == 0) && ((reinterpret_cast<uintptr_t>(a.q) & 15u) == 0u);
 
     // {{{ 1. state -> FP32 copies, volume inputs -> row maxima (digits) or
     //        straight into X_V as TF32 pairs
@@ -538,12 +564,30 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
       const int e = (u % EG) * 8 + (lane & 7);
       const int j0 = 2 * ((u / EG) * 4 + (lane >> 3));
       const bool ein = e < E;
-      const bool valid_e = ein && e < ecount;
-      float G[9];
+      float G[12];
+      {
+        const float4* g4 = reinterpret_cast<const float4*>(sG + (ein ? e : 0) * 12);
 #pragma unroll
-      for (int x = 0; x < 9; ++x) {
-        G[x] = valid_e ? d2f_alu(__ldg(a.metric + (e0 + e) * 9 + x)) : 0.f;
-        if (ein && j0 == 0) sG[e * 9 + x] = G[x];
+        for (int x = 0; x < 3; ++x) {
+          const float4 v = g4[x];
+          G[4 * x] = v.x;
+          G[4 * x + 1] = v.y;
+          G[4 * x + 2] = v.z;
+          G[4 * x + 3] = v.w;
+        }
+      }
+      // both nodes' FP64 state as 16-byte loads (a node past Np or an element
+      // past the mesh reads the neutral state rho = 1, else 0)
+      [[maybe_unused]] double2 qpair[NF];
+      if constexpr (NP % 2 == 0) {
+        if (pair_loads) {
+          const bool vp = ein && j0 < NP && e < ecount;
+          const int64_t g0 = (e0 + e) * NP + j0;
+#pragma unroll
+          for (int k = 0; k < NF; ++k)
+            qpair[k] = vp ? __ldg(reinterpret_cast<const double2*>(a.q + k * nelnp + g0))
+                          : make_double2(k == 0 ? 1.0 : 0.0, k == 0 ? 1.0 : 0.0);
+        }
       }
       float m[NF];
 #pragma unroll
@@ -559,7 +603,12 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
         float p = 0.f, rinv = 1.f;
 #pragma unroll
         for (int k = 0; k < NF; ++k) {
-          const double qd = valid ? __ldg(a.q + k * nelnp + gnode) : (k == 0 ? 1.0 : 0.0);
+          double qd;
+          if constexpr (NP % 2 == 0)
+            qd = pair_loads ? (h == 0 ? qpair[k].x : qpair[k].y)
+                            : (valid ? __ldg(a.q + k * nelnp + gnode) : (k == 0 ? 1.0 : 0.0));
+          else
+            qd = valid ? __ldg(a.q + k * nelnp + gnode) : (k == 0 ? 1.0 : 0.0);
           qf[k] = d2f_alu(qd);
           if (item) sq[(k * E + e) * QP + j] = qf[k];
         }
@@ -597,7 +646,18 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
           tcm::row_max(rmaxV, c * E + (ein ? e : 0), m[c], (lane >> 3) == 0 && ein);
       }
     }
-    if constexpr (TF) tc::fence_async_smem();
+    if constexpr (TF) {
+      // X_V's padding columns meet zero operator columns; they are rewritten
+      // with zeros every tile because the results of the previous tile were
+      // staged over X (a NaN left there would spread into this tile)
+      constexpr int PADV = (P::KV - 3 * NPP) / 2;
+      for (int idx = t; idx < 128 * PADV; idx += THREADS) {
+        const int m = idx / PADV, c = idx - m * PADV;
+        tcm::put_tf32x2(sA, P::A_SLICE_V, tcm::kmajor_off<KG>(m, 3 * NPP + 2 * c, P::SBO_V),
+                        0.f, 0.f);
+      }
+      tc::fence_async_smem();
+    }
     __syncthreads();
     // }}}
 
@@ -620,7 +680,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
           p = sP[e * NP + j];
           rinv = __frcp_rn(qf[0]);
         }
-        vol_inputs(qf, sG + e * 9, p, rinv, h == 0 ? w0 : w1);
+        vol_inputs(qf, sG + e * 12, p, rinv, h == 0 ? w0 : w1);
       }
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
@@ -676,9 +736,8 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
             raise_status(a.status, DG_ERR_INDEX);
             gi = (uint32_t)((e0 + e) * NP + node);
           }
-          const double* fg = a.face_geom + (e0 + e) * 16 + f * 4;
-          const float nx = d2f_alu(__ldg(fg + 0)), ny = d2f_alu(__ldg(fg + 1)),
-                      nz = d2f_alu(__ldg(fg + 2)), scale = d2f_alu(__ldg(fg + 3));
+          const float4 fg = *reinterpret_cast<const float4*>(sFG + (e * 4 + f) * 4);
+          const float nx = fg.x, ny = fg.y, nz = fg.z, scale = fg.w;
           float qi[NF];
           double qed[NF];
 #pragma unroll
@@ -721,6 +780,14 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
                            fv[rd][1][c], tcm::row_exp_bits(rmaxL[m]));
       }
     }
+    if constexpr (TF) {  // X_L's padding columns, as X_V's above
+      constexpr int PADL = (P::KL - NFPT) / 2;
+      for (int idx = t; idx < 128 * PADL; idx += THREADS) {
+        const int m = idx / PADL, c = idx - m * PADL;
+        tcm::put_tf32x2(sA, P::A_SLICE_L, tcm::kmajor_off<KG>(m, NFPT + 2 * c, P::SBO_L),
+                        0.f, 0.f);
+      }
+    }
     tc::fence_async_smem();
     __syncthreads();
     if (t == 0) {
@@ -733,6 +800,9 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
       tc::tc_commit(&mma_bar);
       led.issue(0);
     }
+    // the face phase and the volume inputs of this tile are complete (they
+    // read the geometry before the barrier above): stage the next tile's
+    if (tile + gridDim.x < ntiles) stage_geometry(tile + gridDim.x);
     if (__syncthreads_or(!wait_mma())) break;  // a wait gave up: leave the tile loop
     // }}}
 
@@ -816,9 +886,11 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
         }
       }
     }
-    // no barrier: the next tile writes the state copies, X and the other
-    // row-maxima buffer, none of which a thread still reads; its first
-    // tensor-memory use follows two barriers
+    // digits: no barrier, the next tile's phase 1 writes the state copies and
+    // the other row-maxima buffer, which no thread still reads.  TF32: its
+    // phase 1 writes X, where the results above were staged.  The first
+    // tensor-memory use follows two barriers.
+    if constexpr (TF) __syncthreads();
     // }}}
   }
   // after a wait gave up: the issuing thread waits (bounded) for products it
