@@ -224,12 +224,13 @@ struct dg_plan {
   float* d_pres = nullptr;
   int pres_grid = 0;
   // mixed precision with tcgen05 contractions: [0] exact digit pairs
-  // (variant 4), [1] 3xTF32 products (variant 5)
-  bool tcm[2] = {false, false};
-  void* d_tcm_ops[2] = {nullptr, nullptr};
-  uint32_t tcm_ops_bytes[2] = {0u, 0u};
-  dg::LaunchShape tcm_shape[2];
-  int tcm_grid[2] = {0, 0};
+  // (variant 4), [1] 3xTF32 products (variant 5), [2] the same with the
+  // other CTA size (variant 6); [2] shares [1]'s operator block
+  bool tcm[3] = {false, false, false};
+  void* d_tcm_ops[3] = {nullptr, nullptr, nullptr};
+  uint32_t tcm_ops_bytes[3] = {0u, 0u, 0u};
+  dg::LaunchShape tcm_shape[3];
+  int tcm_grid[3] = {0, 0, 0};
   // face-shared path and adjoint (wave, FP64): the mesh's face_partner
   const int32_t* face_partner = nullptr;
   void* d_adj_ops = nullptr;
@@ -621,6 +622,10 @@ cudaError_t tc_launch_of(int eq, int order, int mode, const dg::RhsArgs& a, int 
   }
 }
 
+// launch mode of tcgen05 form k (0 digits, 1 3xTF32, 2 3xTF32 at the other
+// CTA size), RHS; | 1 for the RK stage
+int tcm_mode(int k) { return k == 0 ? 0 : (k == 1 ? 2 : 6); }
+
 cudaError_t tcm_shape_of(int eq, int order, int mode, dg::LaunchShape* out) {
   switch (eq) {
     case DG_WAVE: return dg::tcm_shape_wave(order, mode, out);
@@ -787,13 +792,13 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     const int bps = t1.blocks_per_sm < t0.blocks_per_sm ? t1.blocks_per_sm : t0.blocks_per_sm;
     const int64_t tfull = (int64_t)nsm * (bps > 0 ? bps : 1);
     p->grid_mtc = (int)(ntiles < tfull ? ntiles : tfull);
-    // the tcgen05 forms (variants 4 and 5)
-    for (int k = 0; k < 2; ++k) {
+    // the tcgen05 forms (variants 4, 5 and 6)
+    for (int k = 0; k < 3; ++k) {
       dg::LaunchShape m0, m1;
-      err = tcm_shape_of(equation, N, 2 * k, &m0);
-      if (err == cudaSuccess) err = tcm_shape_of(equation, N, 2 * k + 1, &m1);
+      err = tcm_shape_of(equation, N, tcm_mode(k), &m0);
+      if (err == cudaSuccess) err = tcm_shape_of(equation, N, tcm_mode(k) | 1, &m1);
       const int mbytes =
-          dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0, k == 1);
+          dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0, k >= 1);
       if (err != cudaSuccess || mbytes != m0.ops_bytes) {
         dg_plan_destroy(p);
         return err != cudaSuccess ? cuda_fail(err, "tcgen05 mixed kernel configuration")
@@ -801,14 +806,18 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
       }
       if (m1.blocks_per_sm < m0.blocks_per_sm) m0.blocks_per_sm = m1.blocks_per_sm;
       if (m0.blocks_per_sm < 1) continue;
-      std::vector<unsigned char> mops(mbytes);
-      dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, mops.data(), mbytes, k == 1);
-      err = cudaMalloc(&p->d_tcm_ops[k], mbytes);
-      if (err == cudaSuccess)
-        err = cudaMemcpy(p->d_tcm_ops[k], mops.data(), mbytes, cudaMemcpyHostToDevice);
-      if (err != cudaSuccess) {
-        dg_plan_destroy(p);
-        return cuda_fail(err, "tcgen05 operator buffer");
+      if (k == 2 && p->tcm[1]) {  // same operator block as variant 5
+        p->d_tcm_ops[2] = p->d_tcm_ops[1];
+      } else {
+        std::vector<unsigned char> mops(mbytes);
+        dg::pack_tcm_ops(N, diff, mesh->lift, mesh->face_nodes, mops.data(), mbytes, k >= 1);
+        err = cudaMalloc(&p->d_tcm_ops[k], mbytes);
+        if (err == cudaSuccess)
+          err = cudaMemcpy(p->d_tcm_ops[k], mops.data(), mbytes, cudaMemcpyHostToDevice);
+        if (err != cudaSuccess) {
+          dg_plan_destroy(p);
+          return cuda_fail(err, "tcgen05 operator buffer");
+        }
       }
       p->tcm[k] = true;
       p->tcm_ops_bytes[k] = static_cast<uint32_t>(mbytes);
@@ -920,7 +929,7 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
 int dg_plan_set_variant(dg_plan* p, int32_t variant) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (variant < 0 || variant >= DG_NUM_VARIANTS)
-    return fail(DG_ERR_ARGUMENT, "variant must be 0..5");
+    return fail(DG_ERR_ARGUMENT, "variant must be 0..6");
   if ((variant & 1) && p->precision != DG_FP32_MIXED)
     return fail(DG_ERR_UNSUPPORTED, "tensor-core products are a mixed-precision variant");
   if (variant >= 4 && !p->tcm[variant - 4])
@@ -1270,7 +1279,7 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     const int k = p->variant - 4;
     a.ops = p->d_tcm_ops[k];
     a.ops_bytes = p->tcm_ops_bytes[k];
-    err = tcm_launch_of(p->equation, p->order, 2 * k, a, p->tcm_grid[k], s);
+    err = tcm_launch_of(p->equation, p->order, tcm_mode(k), a, p->tcm_grid[k], s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
                     main_mode(p, p->split ? dg::MODE_SPLIT : dg::MODE_RHS), a,
@@ -1322,7 +1331,7 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     const int k = p->variant - 4;
     a.ops = p->d_tcm_ops[k];
     a.ops_bytes = p->tcm_ops_bytes[k];
-    err = tcm_launch_of(p->equation, p->order, 2 * k + 1, a, p->tcm_grid[k], s);
+    err = tcm_launch_of(p->equation, p->order, tcm_mode(k) | 1, a, p->tcm_grid[k], s);
   } else {
     err = launch_of(p->equation, p->order, p->precision == DG_FP32_MIXED ? 1 : 0,
                     main_mode(p, dg::MODE_STAGE | (p->split ? dg::MODE_SPLIT : 0)), a,
@@ -1441,6 +1450,7 @@ int dg_plan_destroy(dg_plan* p) {
   if (p->d_adj_ops && cudaFree(p->d_adj_ops) != cudaSuccess) code = DG_ERR_CUDA;
   for (void* b : {(void*)p->d_owned, (void*)p->d_flux, (void*)p->d_aux,
                   (void*)p->d_tc_ops, p->d_tcm_ops[0], p->d_tcm_ops[1],
+                  p->d_tcm_ops[2] != p->d_tcm_ops[1] ? p->d_tcm_ops[2] : nullptr,
                   (void*)p->d_pres})
     if (b && cudaFree(b) != cudaSuccess) code = DG_ERR_CUDA;
   delete p;

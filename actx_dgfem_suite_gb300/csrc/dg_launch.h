@@ -56,7 +56,7 @@ inline OpsOffsets ops_offsets(int np, int nfp, int rs) {
 // contractions on the tensor cores (mode 0 RHS, 1 RK stage).
 // tcm_shape_* / tcm_launch_*: the mixed-precision kernel with its
 // contractions on tcgen05 (mode bit 0: RK stage; bit 1: 3xTF32 products,
-// else exact digit-pair products).
+// else exact digit-pair products; bit 2, with bit 1: the other CTA size).
 #define DG_DECLARE_EQ(name)                                                   \
   cudaError_t shape_##name(int order, int precision, int mode,               \
                            LaunchShape* out);                                \

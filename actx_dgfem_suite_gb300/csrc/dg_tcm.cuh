@@ -86,13 +86,18 @@ constexpr int pow2_cols(int c) {
 constexpr int rup(int x, int m) { return (x + m - 1) / m * m; }
 
 // Tile plan of the kernel.  TF = false: exact FP16 digit pairs (variant 4);
-// TF = true: 3xTF32 products (variant 5; see dg_rhs_tcm_kernel).
-template <int N, int EQ, bool TF = false>
+// TF = true: 3xTF32 products (variant 5; see dg_rhs_tcm_kernel).  ALT: the
+// other CTA size for the same 128-row tile (variant 6), a tile shape the
+// autotuner chooses: 128 threads where the default is 256 (orders 2-3: the
+// same warps per SM spread over twice the tiles in flight, where shared
+// memory allows), 256 where it is 128 or 512 (orders 1 and 4).
+template <int N, int EQ, bool TF = false, bool ALT = false>
 struct MPlan {
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP, NFPT = Shape<N>::NFPT;
   static constexpr int NF = EqInfo<EQ>::NF;
-  static constexpr int THREADS = N == 1 ? 128 : (N == 4 ? 512 : 256);
-  static constexpr int MIN_BLOCKS = N == 4 ? 1 : 2;
+  static constexpr int BASE_THREADS = N == 1 ? 128 : (N == 4 ? 512 : 256);
+  static constexpr int THREADS = !ALT ? BASE_THREADS : (BASE_THREADS == 256 ? 128 : 256);
+  static constexpr int MIN_BLOCKS = N == 4 ? 1 : (THREADS == 128 ? 4 : 2);
   static constexpr int E = 128 / NF;      // elements per tile
   static constexpr int NCOL = NF * E;     // rows of X in use (m = c E + e)
   static constexpr int NB = r16(NP);      // operator rows (MMA N)
@@ -411,11 +416,11 @@ __device__ __forceinline__ void face_point_flux(const FluxConsts& fc, const floa
 
 }  // namespace tcm
 
-template <int N, int EQ, int MODE, bool TF = false>
-__global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF>::THREADS,
-                                  tcm::MPlan<N, EQ, TF>::MIN_BLOCKS)
+template <int N, int EQ, int MODE, bool TF = false, bool ALT = false>
+__global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
+                                  tcm::MPlan<N, EQ, TF, ALT>::MIN_BLOCKS)
     dg_rhs_tcm_kernel(const RhsArgs a) {
-  using P = tcm::MPlan<N, EQ, TF>;
+  using P = tcm::MPlan<N, EQ, TF, ALT>;
   constexpr int NP = P::NP, NFP = P::NFP, NFPT = P::NFPT, NF = P::NF, E = P::E;
   constexpr int QP = P::QP, OP = P::OP, NB = P::NB, THREADS = P::THREADS, KG = P::KG;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;

@@ -237,10 +237,10 @@ cudaError_t tc_launch_any(int order, int mode, const RhsArgs& a, int grid,
 
 // {{{ mixed precision with tcgen05 contractions (fused face fluxes)
 
-template <int N, int EQ, int MODE, bool TF>
+template <int N, int EQ, int MODE, bool TF, bool ALT = false>
 cudaError_t tcm_shape_impl(LaunchShape* out) {
-  using P = tcm::MPlan<N, EQ, TF>;
-  auto kern = dg_rhs_tcm_kernel<N, EQ, MODE, TF>;
+  using P = tcm::MPlan<N, EQ, TF, ALT>;
+  auto kern = dg_rhs_tcm_kernel<N, EQ, MODE, TF, ALT>;
   cudaError_t err = cudaFuncSetAttribute(
       kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM_BYTES);
   if (err != cudaSuccess) return err;
@@ -271,21 +271,26 @@ cudaError_t tcm_shape_impl(LaunchShape* out) {
   return err;
 }
 
-// mode bit 0: fused RK stage; bit 1: 3xTF32 products instead of exact digits
+// mode bit 0: fused RK stage; bit 1: 3xTF32 products instead of exact
+// digits; bit 2 (3xTF32 only): the other CTA size (MPlan::ALT)
+constexpr bool tcm_mode_ok(int mode) { return mode >= 0 && mode <= 7 && (mode < 4 || (mode & 2)); }
+
 template <int N, int EQ>
 cudaError_t tcm_shape_n(int mode, LaunchShape* out) {
   switch (mode) {
     case 0: return tcm_shape_impl<N, EQ, MODE_RHS, false>(out);
     case 1: return tcm_shape_impl<N, EQ, MODE_STAGE, false>(out);
     case 2: return tcm_shape_impl<N, EQ, MODE_RHS, true>(out);
-    default: return tcm_shape_impl<N, EQ, MODE_STAGE, true>(out);
+    case 3: return tcm_shape_impl<N, EQ, MODE_STAGE, true>(out);
+    case 6: return tcm_shape_impl<N, EQ, MODE_RHS, true, true>(out);
+    default: return tcm_shape_impl<N, EQ, MODE_STAGE, true, true>(out);
   }
 }
 
-template <int N, int EQ, int MODE, bool TF>
+template <int N, int EQ, int MODE, bool TF, bool ALT = false>
 cudaError_t tcm_launch_impl(const RhsArgs& a, int grid, cudaStream_t s) {
-  using P = tcm::MPlan<N, EQ, TF>;
-  dg_rhs_tcm_kernel<N, EQ, MODE, TF><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
+  using P = tcm::MPlan<N, EQ, TF, ALT>;
+  dg_rhs_tcm_kernel<N, EQ, MODE, TF, ALT><<<grid, P::THREADS, P::SMEM_BYTES, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -295,13 +300,15 @@ cudaError_t tcm_launch_n(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
     case 0: return tcm_launch_impl<N, EQ, MODE_RHS, false>(a, grid, s);
     case 1: return tcm_launch_impl<N, EQ, MODE_STAGE, false>(a, grid, s);
     case 2: return tcm_launch_impl<N, EQ, MODE_RHS, true>(a, grid, s);
-    default: return tcm_launch_impl<N, EQ, MODE_STAGE, true>(a, grid, s);
+    case 3: return tcm_launch_impl<N, EQ, MODE_STAGE, true>(a, grid, s);
+    case 6: return tcm_launch_impl<N, EQ, MODE_RHS, true, true>(a, grid, s);
+    default: return tcm_launch_impl<N, EQ, MODE_STAGE, true, true>(a, grid, s);
   }
 }
 
 template <int EQ>
 cudaError_t tcm_shape_any(int order, int mode, LaunchShape* out) {
-  if (mode < 0 || mode > 3) return cudaErrorInvalidValue;
+  if (!tcm_mode_ok(mode)) return cudaErrorInvalidValue;
   switch (order) {
     case 1: return tcm_shape_n<1, EQ>(mode, out);
     case 2: return tcm_shape_n<2, EQ>(mode, out);
@@ -314,7 +321,7 @@ cudaError_t tcm_shape_any(int order, int mode, LaunchShape* out) {
 template <int EQ>
 cudaError_t tcm_launch_any(int order, int mode, const RhsArgs& a, int grid,
                            cudaStream_t s) {
-  if (mode < 0 || mode > 3) return cudaErrorInvalidValue;
+  if (!tcm_mode_ok(mode)) return cudaErrorInvalidValue;
   switch (order) {
     case 1: return tcm_launch_n<1, EQ>(mode, a, grid, s);
     case 2: return tcm_launch_n<2, EQ>(mode, a, grid, s);

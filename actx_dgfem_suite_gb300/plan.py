@@ -251,10 +251,11 @@ class DevicePlan:
             _stream_handle(stream)))
 
     #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per
-    #: tile; 4 and 5 the tcgen05 kernel (exact digit pairs, 3xTF32)
+    #: tile; 4 and 5 the tcgen05 kernel (exact digit pairs, 3xTF32), 6 the
+    #: 3xTF32 kernel at its other CTA size
     VARIANTS = {0: "persistent", 1: "tensor-core, persistent", 2: "one CTA per tile",
                 3: "tensor-core, one CTA per tile", 4: "tcgen05, persistent",
-                5: "tcgen05 3xTF32, persistent"}
+                5: "tcgen05 3xTF32, persistent", 6: "tcgen05 3xTF32, other CTA size"}
 
     def set_variant(self, variant: int) -> None:
         _lib.check(self._lib.dg_plan_set_variant(self._handle, int(variant)))

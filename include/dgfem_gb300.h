@@ -261,7 +261,7 @@ typedef struct dg_box_desc {
 int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 
 /* Number of launch variants (0 .. DG_NUM_VARIANTS - 1). */
-#define DG_NUM_VARIANTS 6
+#define DG_NUM_VARIANTS 7
 
 /* Launch variant of the plan's main kernel: bit 0 = contractions on the
  * tensor cores (DG_FP32_MIXED plans: 3xTF32 split with FP32 accumulation,
@@ -272,7 +272,10 @@ int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
  * digits and the digit-pair products accumulated exactly in tensor memory
  * (the most accurate mixed variant), 5 with both operands split into TF32
  * pairs hi + lo and the products hi hi + hi lo + lo hi accumulated in FP32
- * (FP32 accuracy, far fewer instructions per tile).
+ * (FP32 accuracy, far fewer instructions per tile); 6 = variant 5 with the
+ * other CTA size for the same 128-row tile (128 threads at orders 2-3, so
+ * that more tiles are in flight per SM, 256 at orders 1 and 4): the tile
+ * shape the autotuner chooses along with the variant.
  * Default 0.  No counterpart in the reference. */
 int dg_plan_set_variant(dg_plan* plan, int32_t variant);
 
@@ -354,8 +357,8 @@ const char* dg_last_error(void);
 /* ABI version, bumped on any incompatible change (3: dg_plan_autotune
  * writes 5 floats to ms_per_variant, variant 4 added; 4: variants that
  * raise a device-side status report -1, dg_plan_autotune_bounded and
- * dg_rhs_adjoint_stage added; 5: dg_rhs_vjp_stage and variant 5 added, the
- * autotuners write DG_NUM_VARIANTS = 6 entries). */
+ * dg_rhs_adjoint_stage added; 5: dg_rhs_vjp_stage and variants 5 and 6
+ * added, the autotuners write DG_NUM_VARIANTS = 7 entries). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus
