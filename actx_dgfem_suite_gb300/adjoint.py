@@ -323,7 +323,9 @@ class EulerAdjointSolver:
     def _replay(self, q0: torch.Tensor, nsteps: int) -> None:
         """Steps from ``q0`` with every stage input state recorded:
         ``_qs[k, s]`` = q^(s) of the k-th step (stage s of step k reads
-        ``_qs[k, s]`` and writes the next stage's input in place)."""
+        ``_qs[k, s]`` and writes the next stage's input in place).  The last
+        step's final stage is not run: the reverse sweep needs stage inputs
+        only."""
         qs = self._qs
         qs[0, 0].copy_(q0)
         for k in range(nsteps):
@@ -333,7 +335,7 @@ class EulerAdjointSolver:
                 elif k + 1 < nsteps:
                     dst = qs[k + 1, 0]
                 else:
-                    dst = self._buf         # the next checkpoint: not needed
+                    break       # its output, the next checkpoint, is not needed
                 self.plan.rk_stage(qs[k, s], dst, self._res, RK4A[s], RK4B[s], self.dt)
 
     def forward(self, q0: torch.Tensor):
