@@ -242,6 +242,15 @@ class GB300DGArrayContext:
         block costs more than the copy, so buffers are reused by size and
         return to the pool when the caller drops the array.
         ``pinned_results=False`` keeps plain pageable arrays."""
+        arr, pending = self._host_issue(t)
+        if pending:
+            self.d2h_stream.synchronize()
+        return arr
+
+    def _host_issue(self, t: torch.Tensor) -> tuple[np.ndarray, bool]:
+        """Start the copy of ``t`` into a new host array; the array is valid
+        once the device-to-host stream has drained (the flag says whether a
+        copy is pending)."""
         # the event after the kernel that produced t (a compiled call's
         # result), read before detach(), whose new tensor object carries no
         # Python attributes
@@ -250,9 +259,9 @@ class GB300DGArrayContext:
             ready = getattr(t._base, "_dg_ready", None)
         t = t.detach()
         if not t.is_cuda:
-            return t.numpy()
+            return t.numpy(), False
         if not self.pinned_results:
-            return t.cpu().numpy()
+            return t.cpu().numpy(), False
         arr, h = self.host_pool.take(tuple(t.shape), t.dtype)
         # the copy runs on the device-to-host stream and waits only for that
         # kernel, so kernels the caller issued after it keep running meanwhile
@@ -268,8 +277,7 @@ class GB300DGArrayContext:
         if log is not None:
             log.append(("d2h", t0, _timing_event(d2h), t.numel() * t.element_size()))
         t.record_stream(d2h)
-        d2h.synchronize()
-        return arr
+        return arr, True
 
     def pinned_host_like(self, t: torch.Tensor) -> torch.Tensor:
         """A page-locked host tensor shaped like ``t`` (on huge pages where
@@ -282,20 +290,41 @@ class GB300DGArrayContext:
         self.host_pool.release()
 
     def to_numpy(self, x):
+        return self._to_numpy(x, self._host)
+
+    def to_numpy_batch(self, xs) -> list:
+        """``[to_numpy(x) for x in xs]`` with one wait: every copy is issued
+        on the device-to-host stream behind its own kernel, then the stream is
+        drained once, so the host neither waits between copies nor holds the
+        copies back while it runs (a stall of the calling thread after the
+        copies are issued does not delay them)."""
+        pending = [False]
+
+        def issue(t):
+            arr, p = self._host_issue(t)
+            pending[0] |= p
+            return arr
+
+        out = [self._to_numpy(x, issue) for x in xs]
+        if pending[0]:
+            self.d2h_stream.synchronize()
+        return out
+
+    def _to_numpy(self, x, host):
         if isinstance(x, torch.Tensor):
-            return self._host(x)
+            return host(x)
         if isinstance(x, DOFArray):
             if x._stack is not None:
-                host = self._host(x._stack[0])
-                return DOFArray(None, [host[x._stack[1]]])
-            return DOFArray(None, [self.to_numpy(a) for a in x])
+                h = host(x._stack[0])
+                return DOFArray(None, [h[x._stack[1]]])
+            return DOFArray(None, [self._to_numpy(a, host) for a in x])
         lv = leaves(x)
         st = lv[0]._stack
         if st is not None and all(d._stack is not None and d._stack[0] is st[0]
                                   for d in lv):
-            host = self._host(st[0])   # one device->host copy
-            return map_leaves(x, lambda d: DOFArray(None, [host[d._stack[1]]]))
-        return map_leaves(x, lambda d: self.to_numpy(d))
+            h = host(st[0])   # one device->host copy
+            return map_leaves(x, lambda d: DOFArray(None, [h[d._stack[1]]]))
+        return map_leaves(x, lambda d: self._to_numpy(d, host))
 
     def zeros(self, shape, dtype=torch.float64):
         return torch.zeros(shape, dtype=dtype, device=self.device)

@@ -30,6 +30,14 @@ def test_calls_in_flight_with_host_states(actx):
         got = [np.stack([d[0] for d in leaves(actx.to_numpy(o))]) for o in outs]
         for g, r in zip(got, refs):
             assert np.array_equal(g, r)
+    # batched readback: the same arrays, one wait; containers and bare tensors
+    for _ in range(2):
+        outs = [c(*a) for c, a in zip(calls, host_args)]
+        got = actx.to_numpy_batch(outs + [outs[0]])
+        for g, r in zip(got, refs + refs[:1]):
+            assert np.array_equal(np.stack([d[0] for d in leaves(g)]), r)
+    t = torch.arange(12.0, dtype=torch.float64, device=actx.device).reshape(3, 4)
+    assert np.array_equal(actx.to_numpy_batch([t])[0], t.cpu().numpy())
     # a state that changes between calls reaches the kernel each time
     c, a = calls[0], host_args[0]
     hq = leaves(a[-1])[0]._stack[0]
