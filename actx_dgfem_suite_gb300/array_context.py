@@ -297,7 +297,11 @@ class GB300DGArrayContext:
         on the device-to-host stream behind its own kernel, then the stream is
         drained once, so the host neither waits between copies nor holds the
         copies back while it runs (a stall of the calling thread after the
-        copies are issued does not delay them)."""
+        copies are issued does not delay them).  The copies also wait for the
+        host-to-device copies issued before them, so that the two directions
+        do not compete for the host's memory bandwidth while the uploads the
+        kernels need are still running."""
+        self.d2h_stream.wait_stream(self.h2d_stream)
         pending = [False]
 
         def issue(t):

@@ -19,8 +19,11 @@ RHS), whole job.
   copy of each result into a new page-locked array behind its own kernel,
   one wait at the end), all inside the timed
   region; 3-4 untimed steps (the first ones pay the host allocations), then
-  min(steps, 5) timed steps.  ``split_ms``: the copies' busy time in one
-  more such step (transfer log of the array context), beside the kernels' time.
+  min(steps, 5) timed steps.  ``logged_steps``: as many steps again with
+  the array context's transfer log on (the copies' busy times and rates, the
+  span to the last copy, the end of the last kernel, the wall time);
+  ``split_ms``: the logged step of median wall time, beside the kernels'
+  time of the device-resident step.
 * ``parity``: every case at the CPU sample's size (n // cpu-scale) through
   the public API against the CPU oracle's RHS of the same run.
 * ``--impl reference``: the CPU FP64 oracle (a restatement of the
@@ -301,17 +304,23 @@ def reference_arm(args) -> None:
 # }}}
 
 
-def transfer_split(actx, step_fn) -> dict:
-    """One more end-to-end step with the array context's transfer log on:
-    the busy time of its host->device and device->host copies (sum of the
-    copies' event intervals on the copy streams), the span from the step's
-    first upload to its last result copy, and the copies' effective rates."""
+def transfer_split(actx, step_fn, klog: list | None = None) -> dict:
+    """One end-to-end step with the array context's transfer log on: the busy
+    time of its host->device and device->host copies (sum of the copies'
+    event intervals on the copy streams), the span from the step's first
+    upload to its last result copy, when its last kernel ended (``kernels``,
+    from the timing events ``step_fn`` appends to ``klog``), the copies'
+    effective rates and the step's wall time."""
     import torch
     torch.cuda.synchronize()
     actx.transfer_log = []
+    if klog is not None:
+        klog.clear()
     t0 = torch.cuda.Event(enable_timing=True)
     t0.record(actx.h2d_stream)
+    w = time.perf_counter()
     step_fn()
+    wall = (time.perf_counter() - w) * 1e3
     torch.cuda.synchronize()
     log, actx.transfer_log = actx.transfer_log, None
     res = {}
@@ -322,6 +331,8 @@ def transfer_split(actx, step_fn) -> dict:
         res[kind + "_gbs"] = sum(n for _, n in rows) / (busy * 1e-3) / 1e9 if busy > 0 else None
     ends = [t0.elapsed_time(b) for k, a, b, n in log]
     res["span"] = max(ends) if ends else 0.0
+    res["kernels"] = max(t0.elapsed_time(e) for e in klog) if klog else None
+    res["wall"] = wall
     return res
 
 
@@ -608,10 +619,19 @@ def our_arm(args) -> None:
     order = sorted(range(len(runs)),
                    key=lambda k: -case_ms[k] / (runs[k]["q"].numel() * 8))
 
+    klog: list = []          # kernel-end events of a logged step
+    logging = [False]
+
     def e2e_step():
         # every case's call first (host->device copies on the context's copy
         # stream overlap the kernels of earlier cases), then every result back
-        outs = [runs[k]["compiled"](*host_states[k]) for k in order]
+        outs = []
+        for k in order:
+            outs.append(runs[k]["compiled"](*host_states[k]))
+            if logging[0]:   # when the step is logged: end of its kernel
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record(torch.cuda.current_stream())
+                klog.append(ev)
         # read back in the same order, each copy behind its own kernel, with
         # one wait at the end
         host = dict(zip(order, actx.to_numpy_batch(outs)))
@@ -635,10 +655,21 @@ def our_arm(args) -> None:
         e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / ke, dev)
-    # the copies' busy time within one more step taken like the timed ones,
-    # beside the kernels' time (the device-resident step above) and the
-    # timed steps' median
-    split = transfer_split(actx, e2e_step)
+    # where the time goes: the same number of steps again with the transfer
+    # log on (copy busy times and rates, span, end of the last kernel), beside
+    # the kernels' time (the device-resident step above); `split_ms` is the
+    # logged step of median wall time
+    keep = [host_out]
+    host_out = None
+
+    def logged_step():   # the timed loop's lifetimes: the previous results live on
+        keep[0] = e2e_step()
+
+    logging[0] = True
+    logged = [transfer_split(actx, logged_step, klog) for _ in range(ke)]
+    logging[0] = False
+    host_out = keep[0]
+    split = dict(sorted(logged, key=lambda r: r["wall"])[len(logged) // 2])
     split["compute"] = ms_step
     split["step"] = statistics.median(e2e_step_ms)
     # sanity: the host result equals the device-resident result
@@ -726,6 +757,8 @@ def our_arm(args) -> None:
                     "step_ms": [round(x, 1) for x in e2e_step_ms],
                     "split_ms": {k: (round(v, 2) if v is not None else None)
                                  for k, v in split.items()},
+                    "logged_steps": [{k: (round(v, 1) if v is not None else None)
+                                      for k, v in r.items()} for r in logged],
                     "overlap": ("all cases' calls issued before their results are read "
                                 "(highest kernel time per input byte first), then every "
                                 "result's copy back in the same order (to_numpy_batch, "
