@@ -550,6 +550,25 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
   };
   if (blockIdx.x < ntiles) stage_geometry(blockIdx.x);
   __syncthreads();
+  // the next tile's state rows and gather indices into L2 (prefetch hints on
+  // addresses inside the arrays), so that its phase-1 and face loads wait for
+  // L2 rather than HBM
+  auto prefetch_next = [&](int64_t nt) {
+    const int64_t g0 = nt * E;
+    const int cnt = (nel - g0) < (int64_t)E ? (int)(nel - g0) : E;
+    const int qlines = (cnt * NP * 8 + 127) / 128;
+    const int glines = (cnt * NFPT * 4 + 127) / 128;
+    for (int idx = t; idx < NF * qlines + glines; idx += THREADS) {
+      const char* ptr;
+      if (idx < NF * qlines) {
+        const int k = idx / qlines, l = idx - k * qlines;
+        ptr = reinterpret_cast<const char*>(a.q + k * nelnp + g0 * NP) + l * 128;
+      } else {
+        ptr = reinterpret_cast<const char*>(a.gather + g0 * NFPT) + (idx - NF * qlines) * 128;
+      }
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(ptr));
+    }
+  };
 
   int it = 0;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
@@ -705,6 +724,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
 
     // {{{ 3. volume products (one thread); face fluxes (registers) and their
     //        row maxima; then X_L and the LIFT products
+    if (tile + gridDim.x < ntiles) prefetch_next(tile + gridDim.x);
     if (t == 0) {
       if constexpr (TF)
         tcm::issue_phase_tf32<P::KV, P::SBO_V, P::A_SLICE_V, P::B_SLICE_V, NB>(
