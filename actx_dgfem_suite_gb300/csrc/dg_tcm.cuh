@@ -49,17 +49,20 @@
 // Per tile of E = 128 / NF elements (8 elements x 4 pairs of nodes or face
 // points per warp; a pair's digits are one 4-byte word per digit slice, and
 // the 32 words a warp stores fall in 32 distinct banks):
-//   1. per node: the FP64 state -> FP32 copy, metric, (Euler: the pressure
-//      from the per-node table, which dg_euler_pressure_f32_kernel fills by
-//      the FP64 recovery from total energy), the inputs w -> row maxima
-//      (shuffles + shared atomics);
-//   2. per node again: w -> digits of X_V;
-//   3. one thread issues the volume products (asynchronous, completion on an
+//   0. (during the previous tile's LIFT products) the tile's metric and face
+//      geometry converted once to FP32 in shared memory;
+//   1. per node pair: the FP64 state (one 16-byte load where Np is even) ->
+//      FP32 copy, (Euler: the pressure from the per-node table, which
+//      dg_euler_pressure_f32_kernel fills by the FP64 recovery from total
+//      energy), the inputs w -> row maxima (digits: shuffles + shared
+//      atomics) or straight into X_V as TF32 pairs;
+//   2. (digits) per node again: w -> digits of X_V;
+//   3. L2 prefetch of the next tile's state rows and gather indices; one
+//      thread issues the volume products (asynchronous, completion on an
 //      mbarrier); meanwhile every thread evaluates the numerical flux of its
-//      face points into registers and their row maxima; after the volume
-//      products have read X, the digits of X_L replace it and the LIFT
-//      products run;
-//   4. tcgen05.ld of the eight level sums -> FP32 staging, then coalesced FP64
+//      face points into registers (and their row maxima); after the volume
+//      products have read X, X_L replaces it and the LIFT products run;
+//   4. tcgen05.ld of the accumulators -> FP32 staging, then coalesced FP64
 //      stores (RHS) or the fused low-storage RK stage.
 // Waits on the mbarriers are bounded (DG_ERR_TIMEOUT instead of spinning).
 //
