@@ -5,10 +5,10 @@ The case is built through the public API (``get_rhs(..., definition="baseline")`
 with ``nel_1d`` hexahedra per axis, 6 tetrahedra each); the plan's launch
 variant is set explicitly (``DevicePlan.VARIANTS``: 0 persistent, 1
 tensor-core persistent, 2 one CTA per tile, 3 tensor-core one CTA per tile,
-4 tcgen05 exact digits, 5 tcgen05 3xTF32) instead of autotuned, so a profiler
-can capture one kernel.
+4 tcgen05 exact digits, 5 tcgen05 3xTF32, 6 the same at its other CTA size)
+instead of autotuned, so a profiler can capture one kernel.
 
-``python -m actx_dgfem_suite_gb300.tools.time_variant maxwell 4 --n 20 --variant 4``
+``python -m actx_dgfem_suite_gb300.tools.time_variant maxwell 3 --n 28 --variant 5``
 prints one JSON line.
 """
 
