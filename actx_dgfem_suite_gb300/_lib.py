@@ -29,6 +29,8 @@ DG_MAXWELL = 2
 DG_FP64 = 0
 DG_FP32_MIXED = 1
 DG_FP64_TC = 2
+#: DG_NUM_VARIANTS of the header: entries the autotuners write per call
+NUM_VARIANTS = 7
 
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",

@@ -273,7 +273,7 @@ class DevicePlan:
         self._check_tensor(q, "state")
         out = torch.empty_like(q)
         chosen = ctypes.c_int32()
-        nv = len(self.VARIANTS)
+        nv = _lib.NUM_VARIANTS     # the library writes this many entries
         ms = (ctypes.c_float * nv)()
         if ref is None:
             _lib.check(self._lib.dg_plan_autotune(

@@ -33,6 +33,13 @@ def test_library_exports_all_declared_symbols():
         assert ctypes.cast(getattr(L, name), ctypes.c_void_p).value
 
 
+def test_variant_count_matches_the_header():
+    from actx_dgfem_suite_gb300.plan import DevicePlan
+    text = (ROOT / "include" / "dgfem_gb300.h").read_text()
+    m = re.search(r"#define\s+DG_NUM_VARIANTS\s+(\d+)", text)
+    assert m and int(m.group(1)) == _lib.NUM_VARIANTS == len(DevicePlan.VARIANTS)
+
+
 def test_version_and_error_strings():
     L = _lib.lib()
     assert L.dg_abi_version() == 5
