@@ -169,3 +169,36 @@ def test_tcgen05_mixed_rk_stage_and_element_scale(variant):
         ref_k = outs[0][k]
         assert float(torch.linalg.norm(outs[1][k] - ref_k)) <= \
             RTOL[variant] * float(torch.linalg.norm(ref_k))
+
+
+@pytest.mark.parametrize("variant", [5, 6])
+def test_tcgen05_tf32_nan_stays_local(variant):
+    """A NaN in one element's state reaches that element and its face
+    neighbours only: the results staged over the operand region are
+    replaced, padding included, before the next tile's products read it."""
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem("maxwell", jittered_box_mesh(12), 3, seed=4)
+    dm = DeviceMesh(prob.disc, "cuda:0")
+    mixed = DevicePlan(dm, "maxwell", prob.params, "fp32-mixed")
+    q = torch.from_numpy(prob.fields).cuda()
+    mixed.set_variant(0)
+    ref = mixed.rhs(q)
+    bad = 7
+    qn = q.clone()
+    qn[2, bad, 3] = float("nan")
+    mixed.set_variant(variant)
+    out = mixed.rhs(qn)
+    mixed.finish()
+    # elements sharing a face with the bad one (or the bad one itself)
+    gather = prob.disc.gather_index()          # (Nel, 4, Nfp) flat exterior index
+    np_ = prob.disc.np_
+    ext_el = (gather.astype(np.int64) & 0x7FFFFFFF) // np_
+    bdry = (gather >> 31).astype(bool)
+    touched = {bad}
+    touched |= set(np.nonzero(((ext_el == bad) & ~bdry).any(axis=(1, 2)))[0].tolist())
+    finite = torch.isfinite(out).all(dim=(0, 2)).cpu().numpy()
+    assert not finite[bad]
+    others = np.array([e for e in range(prob.disc.nelements) if e not in touched])
+    assert finite[others].all()
+    n = float(torch.linalg.norm(ref[:, others]))
+    assert float(torch.linalg.norm(out[:, others] - ref[:, others])) <= TF32_RTOL * n
