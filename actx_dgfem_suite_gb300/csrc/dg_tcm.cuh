@@ -208,6 +208,18 @@ __device__ __forceinline__ void put_tf32x2(unsigned char* base, int slice, int o
   *reinterpret_cast<uint2*>(base + slice + off) = make_uint2(l0, l1);
 }
 
+// zeros at columns k, k + 1 (k even) of one row in every slice of X
+template <bool TF>
+__device__ __forceinline__ void zero_pair(unsigned char* base, int slice, int off) {
+  if constexpr (TF) {
+    *reinterpret_cast<uint2*>(base + off) = make_uint2(0u, 0u);
+    *reinterpret_cast<uint2*>(base + slice + off) = make_uint2(0u, 0u);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) *reinterpret_cast<uint32_t*>(base + i * slice + off) = 0u;
+  }
+}
+
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b,
                                          uint32_t idesc, uint32_t accumulate) {
   asm volatile(
@@ -573,6 +585,25 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
     }
   };
 
+  // X's padding columns (k past 3 NPP, or past 4 Nfp) meet zero operator
+  // columns; they are rewritten with zeros every tile, because X shares its
+  // bytes with the other phase's layout (and, for 3xTF32, with the previous
+  // tile's staged results): a NaN left there would reach other elements
+  auto zero_pad_v = [&]() {
+    constexpr int PADV = (P::KV - 3 * NPP) / 2;
+    for (int idx = t; idx < 128 * PADV; idx += THREADS) {
+      const int m = idx / PADV, c = idx - m * PADV;
+      tcm::zero_pair<TF>(sA, P::A_SLICE_V, tcm::kmajor_off<KG>(m, 3 * NPP + 2 * c, P::SBO_V));
+    }
+  };
+  auto zero_pad_l = [&]() {
+    constexpr int PADL = (P::KL - NFPT) / 2;
+    for (int idx = t; idx < 128 * PADL; idx += THREADS) {
+      const int m = idx / PADL, c = idx - m * PADL;
+      tcm::zero_pair<TF>(sA, P::A_SLICE_L, tcm::kmajor_off<KG>(m, NFPT + 2 * c, P::SBO_L));
+    }
+  };
+
   int it = 0;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
     const int64_t e0 = tile * E;
@@ -674,15 +705,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
       }
     }
     if constexpr (TF) {
-      // X_V's padding columns meet zero operator columns; they are rewritten
-      // with zeros every tile because the results of the previous tile were
-      // staged over X (a NaN left there would spread into this tile)
-      constexpr int PADV = (P::KV - 3 * NPP) / 2;
-      for (int idx = t; idx < 128 * PADV; idx += THREADS) {
-        const int m = idx / PADV, c = idx - m * PADV;
-        tcm::put_tf32x2(sA, P::A_SLICE_V, tcm::kmajor_off<KG>(m, 3 * NPP + 2 * c, P::SBO_V),
-                        0.f, 0.f);
-      }
+      zero_pad_v();
       tc::fence_async_smem();
     }
     __syncthreads();
@@ -720,6 +743,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
       }
     }
     if constexpr (!TF) {
+      zero_pad_v();
       tc::fence_async_smem();
       __syncthreads();
     }
@@ -808,14 +832,7 @@ __global__ void __launch_bounds__(tcm::MPlan<N, EQ, TF, ALT>::THREADS,
                            fv[rd][1][c], tcm::row_exp_bits(rmaxL[m]));
       }
     }
-    if constexpr (TF) {  // X_L's padding columns, as X_V's above
-      constexpr int PADL = (P::KL - NFPT) / 2;
-      for (int idx = t; idx < 128 * PADL; idx += THREADS) {
-        const int m = idx / PADL, c = idx - m * PADL;
-        tcm::put_tf32x2(sA, P::A_SLICE_L, tcm::kmajor_off<KG>(m, NFPT + 2 * c, P::SBO_L),
-                        0.f, 0.f);
-      }
-    }
+    zero_pad_l();
     tc::fence_async_smem();
     __syncthreads();
     if (t == 0) {

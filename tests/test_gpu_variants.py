@@ -171,11 +171,12 @@ def test_tcgen05_mixed_rk_stage_and_element_scale(variant):
             RTOL[variant] * float(torch.linalg.norm(ref_k))
 
 
-@pytest.mark.parametrize("variant", [5, 6])
-def test_tcgen05_tf32_nan_stays_local(variant):
+@pytest.mark.parametrize("variant", [4, 5, 6])
+def test_tcgen05_nan_stays_local(variant):
     """A NaN in one element's state reaches that element and its face
-    neighbours only: the results staged over the operand region are
-    replaced, padding included, before the next tile's products read it."""
+    neighbours only: X's padding columns, which share bytes with the other
+    phase's layout and (3xTF32) with the previous tile's staged results, are
+    rewritten with zeros before every product reads them."""
     from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
     prob = make_problem("maxwell", jittered_box_mesh(12), 3, seed=4)
     dm = DeviceMesh(prob.disc, "cuda:0")
@@ -201,4 +202,4 @@ def test_tcgen05_tf32_nan_stays_local(variant):
     others = np.array([e for e in range(prob.disc.nelements) if e not in touched])
     assert finite[others].all()
     n = float(torch.linalg.norm(ref[:, others]))
-    assert float(torch.linalg.norm(out[:, others] - ref[:, others])) <= TF32_RTOL * n
+    assert float(torch.linalg.norm(out[:, others] - ref[:, others])) <= RTOL[variant] * n
