@@ -228,3 +228,30 @@ def test_tc_rk_stage_matches_fma_path(equation, order):
         outs.append((qo, res, un))
     for a, b in zip(outs[0], outs[1]):
         assert float(torch.linalg.norm(a - b)) <= FP64_RTOL * float(torch.linalg.norm(b))
+
+
+@pytest.mark.parametrize("equation", EQUATIONS)
+@pytest.mark.parametrize("order", (3, 4))
+def test_tc_nan_propagates_like_fp64(equation, order):
+    """A NaN in one element's state: the tensor-core FP64 emulation returns
+    NaN where the FMA path does (that element and its face neighbours), not
+    finite values from the fixed-point split, and the same RHS elsewhere."""
+    import torch
+
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    prob = make_problem(equation, jittered_box_mesh(5), order, seed=2)
+    dm = DeviceMesh(prob.disc, "cuda:0", with_partner=True)
+    q = torch.from_numpy(prob.fields).to("cuda:0")
+    q[1, 11, 2] = float("nan")
+    outs = {}
+    for prec in ("fp64-tc", "fp64"):
+        plan = DevicePlan(dm, equation, prob.params, prec)
+        outs[prec] = plan.rhs(q)
+        plan.finish()
+    tc, fma = outs["fp64-tc"], outs["fp64"]
+    bad_tc = ~torch.isfinite(tc).all(dim=(0, 2))
+    bad_fma = ~torch.isfinite(fma).all(dim=(0, 2))
+    assert bool(bad_fma[11]) and torch.equal(bad_tc, bad_fma)
+    ok = ~bad_fma
+    n = float(torch.linalg.norm(fma[:, ok]))
+    assert float(torch.linalg.norm(tc[:, ok] - fma[:, ok])) <= FP64_RTOL * n
