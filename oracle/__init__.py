@@ -26,9 +26,10 @@ Independence from the product: no module here imports the product package.
 The reference element is the oracle's own (``oracle.refelem``): GLL points
 from NumPy's Legendre roots, the recursive node family placed from its
 definition (vertices, GLL edge points, centroids, and the order-4
-face-interior nodes in closed form), a monomial basis and collapsed
-Gauss-Legendre quadrature; the matrices are assembled by quadrature
-(``oracle.refops``); exterior face values are found by matching physical node
+face-interior nodes in closed form), products of Legendre polynomials as
+the modal basis and collapsed Gauss-Legendre quadrature, all in 32-digit
+arithmetic (mpmath); the matrices are assembled by quadrature in the same
+precision (``oracle.refops``); exterior face values are found by matching physical node
 coordinates (``oracle.geometry``), not through the product's gather index.
 Only the mesh (vertex coordinates and element vertex lists) and the state
 arrays are inputs shared with the product; the tests check that the product's
