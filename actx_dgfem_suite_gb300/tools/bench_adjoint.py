@@ -10,7 +10,11 @@ Reports the forward and adjoint cost per step, the checkpoint memory, and
 central finite-difference checks of the gradient with respect to c_e and the
 initial state along random directions (FP64).
 
-``python -m actx_dgfem_suite_gb300.tools.bench_adjoint [--n 40 --steps 300]``
+``--equation euler``: the Euler P3 adjoint instead (6 * 24^3 tetrahedra,
+100 LSRK45 steps, 64 density receivers, gradient with respect to the initial
+state, see :func:`run_euler`).
+
+``python -m actx_dgfem_suite_gb300.tools.bench_adjoint [--equation euler] [--n N --steps S]``
 prints one JSON line.
 """
 
@@ -213,12 +217,20 @@ def run_euler(n: int = 24, order: int = 3, nsteps: int = 100, nrec: int = 64,
 
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m actx_dgfem_suite_gb300.tools.bench_adjoint")
-    ap.add_argument("--n", type=int, default=40)
+    ap.add_argument("--equation", choices=("wave", "euler"), default="wave")
+    ap.add_argument("--n", type=int, default=None,
+                    help="hexahedra per axis (default 40 for wave, 24 for Euler)")
     ap.add_argument("--order", type=int, default=3)
-    ap.add_argument("--steps", type=int, default=300)
-    ap.add_argument("--receivers", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="LSRK45 steps (default 300 for wave, 100 for Euler)")
+    ap.add_argument("--receivers", type=int, default=None,
+                    help="receivers (default 256 for wave, 64 for Euler)")
     a = ap.parse_args(argv)
-    print(json.dumps(run(a.n, a.order, a.steps, a.receivers)))
+    if a.equation == "wave":
+        res = run(a.n or 40, a.order, a.steps or 300, a.receivers or 256)
+    else:
+        res = run_euler(a.n or 24, a.order, a.steps or 100, a.receivers or 64)
+    print(json.dumps(res))
 
 
 if __name__ == "__main__":
