@@ -482,11 +482,11 @@ __device__ __forceinline__ void fold_products(uint32_t tmem, const int* row_exp,
           // C = W 2^(e_m + e_n - 60), e_n = col_emax - 1022; RN(W) 2^(sc - 28)
           const int sc = e_row + col_emax[col] - 1022 - 32;
           double r;
-          if (col_emax[col] == 0x7ff)   // a NaN or infinity in the column: as FP64
-            r = __longlong_as_double(0x7ff8000000000000LL);   // products would, NaN
-          else if (!fixed_to_double(wt[j], wf[j], sc - 28, &r))  // not a normal double
+          if (!fixed_to_double(wt[j], wf[j], sc - 28, &r))  // not a normal double
             r = fma((double)wf[j], 0x1p-28, i64_exact_double(wt[j])) * pow2(sc);
-          out[row * G::NC + col] = r;
+          // a NaN or infinity in the column gives NaN, as the FP64 products would
+          out[row * G::NC + col] =
+              col_emax[col] == 0x7ff ? __longlong_as_double(0x7ff8000000000000LL) : r;
         }
       }
     }
