@@ -40,5 +40,8 @@ fixtures for this path (``test/test_dgfem_opt_freeze.py:1-4`` is a
 placeholder) and cannot run here, so parity with the reference's own numbers
 is UNPINNED.  The oracle is pinned instead by known-answer tests
 (polynomial exactness, free-stream preservation, discrete conservation,
-convergence to the analytic cavity mode) in ``tests/test_oracle_kat.py``.
+convergence to the analytic cavity mode) in ``tests/test_oracle_kat.py``,
+and its wave operator by the reference's own ``wave_operator`` code, run
+on stand-in modules over this package's primitives
+(``tests/golden/make_reference_equations.py``): same result to the bit.
 """
