@@ -70,5 +70,11 @@ def test_argument_errors_without_device():
     assert L.dg_fp64_fma_probe(None, 1, 1, 1, None) == _lib.DG_ERR_ARGUMENT
     assert L.dg_plan_set_element_scale(None, None) == _lib.DG_ERR_ARGUMENT
     assert L.dg_rhs_adjoint(None, None, None, None, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_rhs_vjp(None, None, None, None, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_rhs_vjp_stage(None, None, None, 1.0, None, None, 0.0, 0.0, 0.0, None,
+                              None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_rhs_adjoint_stage(None, None, 1.0, None, None, None, None, 0.0, 0.0, 0.0,
+                                  None, None) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_plan_set_variant(None, 0) == _lib.DG_ERR_ARGUMENT
     with pytest.raises(_lib.DGError):
         _lib.check(L.dg_rhs(None, None, None, None))
