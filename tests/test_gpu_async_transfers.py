@@ -97,3 +97,21 @@ def test_result_readback_waits_only_for_its_own_call(actx):
     torch.cuda.synchronize()
     assert np.array_equal(got, ref)
     assert still_running
+
+
+def test_batched_readback_pageable_and_host_inputs():
+    """to_numpy_batch with pageable results (pinned_results=False), and with
+    host tensors among the inputs (returned as they are)."""
+    from actx_dgfem_suite_gb300.array_context import GB300DGArrayContext
+    from actx_dgfem_suite_gb300.containers import leaves
+    from actx_dgfem_suite_gb300.rhs_builder import get_rhs
+    ctx = GB300DGArrayContext("cuda:0", pinned_results=False)
+    rhs, args = get_rhs("euler", ctx, 3, 2, definition="baseline", nel_1d=3)
+    compiled = ctx.compile(rhs)
+    outs = [compiled(*args) for _ in range(3)]
+    ref = np.stack([d[0] for d in leaves(ctx.to_numpy(outs[0]))])
+    got = ctx.to_numpy_batch(outs)
+    for g in got:
+        assert np.array_equal(np.stack([d[0] for d in leaves(g)]), ref)
+    h = torch.arange(6.0, dtype=torch.float64)
+    assert np.array_equal(ctx.to_numpy_batch([h])[0], h.numpy())
