@@ -13,7 +13,7 @@ _LIB_PATH = Path(__file__).resolve().parent / "libdgfem_gb300.so"
 _lib = None
 
 #: ABI version this binding is written for (dg_abi_version() of the library)
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 DG_OK = 0
 DG_ERR_ARGUMENT = 1
@@ -30,7 +30,7 @@ DG_FP64 = 0
 DG_FP32_MIXED = 1
 DG_FP64_TC = 2
 #: DG_NUM_VARIANTS of the header: entries the autotuners write per call
-NUM_VARIANTS = 7
+NUM_VARIANTS = 11
 
 #: every entry point declared in include/dgfem_gb300.h
 EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",

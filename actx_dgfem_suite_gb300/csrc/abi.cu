@@ -200,7 +200,8 @@ struct dg_plan {
   int64_t ntiles = 0;      // tiles of the main kernel
   int grid_mtc = 0;        // mixed precision with tensor-core products
   int variant = 0;         // bit 0: tensor-core products (mixed); bit 1: one CTA per
-                           // tile; 4: the mixed kernel on tcgen05
+                           // tile; 4-6: the mixed kernel on tcgen05; 7-10: the
+                           // mma.sync products at the other tile shapes
   dg::LaunchShape shape;
   int device = 0;
   int nsm = 0;
@@ -231,6 +232,13 @@ struct dg_plan {
   uint32_t tcm_ops_bytes[3] = {0u, 0u, 0u};
   dg::LaunchShape tcm_shape[3];
   int tcm_grid[3] = {0, 0, 0};
+  // mixed precision, mma.sync products at the other tile shapes: [0] 128
+  // threads and 128 / Np elements per tile (variants 7 persistent, 8 one CTA
+  // per tile), [1] 512 threads and 512 / Np elements (variants 9, 10)
+  bool tcb[2] = {false, false};
+  dg::LaunchShape tcb_shape[2];
+  int tcb_grid[2] = {0, 0};
+  int64_t tcb_ntiles[2] = {0, 0};
   // face-shared path and adjoint (wave, FP64): the mesh's face_partner
   const int32_t* face_partner = nullptr;
   void* d_adj_ops = nullptr;
@@ -358,11 +366,27 @@ int setup_split(dg_plan* p, const int32_t* partner, const int32_t* d_face_nodes)
   return DG_OK;
 }
 
+// Variants 7-10: the mma.sync kernel at tile shape (v - 7) / 2, one CTA per
+// tile when v - 7 is odd.
+constexpr int kFirstShapeVariant = 7;
+bool is_tcm_variant(int v) { return v >= 4 && v < kFirstShapeVariant; }
+bool is_shape_variant(int v) { return v >= kFirstShapeVariant && v < DG_NUM_VARIANTS; }
+int shape_index(int v) { return (v - kFirstShapeVariant) / 2; }
+constexpr int kShapeModeBits[2] = {dg::MODE_B128, dg::MODE_B512};
+
 // Mode bits and grid of the main kernel under the plan's variant.
 int main_mode(const dg_plan* p, int base) {
+  if (is_shape_variant(p->variant))
+    return base | dg::MODE_TC | kShapeModeBits[shape_index(p->variant)];
   return base | ((p->variant & 1) && p->precision == DG_FP32_MIXED ? dg::MODE_TC : 0);
 }
 int main_grid(const dg_plan* p) {
+  if (is_shape_variant(p->variant)) {
+    const int k = shape_index(p->variant);
+    if ((p->variant - kFirstShapeVariant) & 1)
+      return (int)(p->tcb_ntiles[k] < 0x7fffffff ? p->tcb_ntiles[k] : 0x7fffffff);
+    return p->tcb_grid[k];
+  }
   if (p->variant & 2) return (int)(p->ntiles < 0x7fffffff ? p->ntiles : 0x7fffffff);
   return (p->variant & 1) && p->precision == DG_FP32_MIXED ? p->grid_mtc : p->grid;
 }
@@ -653,7 +677,7 @@ extern "C" {
 
 const char* dg_last_error(void) { return g_last_error.c_str(); }
 
-int32_t dg_abi_version(void) { return 5; }
+int32_t dg_abi_version(void) { return 6; }
 
 int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,
@@ -792,6 +816,25 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
     const int bps = t1.blocks_per_sm < t0.blocks_per_sm ? t1.blocks_per_sm : t0.blocks_per_sm;
     const int64_t tfull = (int64_t)nsm * (bps > 0 ? bps : 1);
     p->grid_mtc = (int)(ntiles < tfull ? ntiles : tfull);
+    // the same products at the other tile shapes (variants 7-10); a shape
+    // that does not fit on an SM stays unsupported
+    for (int k = 0; k < 2; ++k) {
+      dg::LaunchShape b0, b1;
+      err = shape_of(equation, N, 1, dg::MODE_TC | kShapeModeBits[k], &b0);
+      if (err == cudaSuccess)
+        err = shape_of(equation, N, 1, dg::MODE_TC | dg::MODE_STAGE | kShapeModeBits[k], &b1);
+      if (err != cudaSuccess) {
+        dg_plan_destroy(p);
+        return cuda_fail(err, "tensor-core mixed kernel tile shapes");
+      }
+      if (b1.blocks_per_sm < b0.blocks_per_sm) b0.blocks_per_sm = b1.blocks_per_sm;
+      if (b0.blocks_per_sm < 1 || b0.elems_per_tile < 1) continue;
+      p->tcb[k] = true;
+      p->tcb_shape[k] = b0;
+      p->tcb_ntiles[k] = (p->nel + b0.elems_per_tile - 1) / b0.elems_per_tile;
+      const int64_t bfull = (int64_t)nsm * b0.blocks_per_sm;
+      p->tcb_grid[k] = (int)(p->tcb_ntiles[k] < bfull ? p->tcb_ntiles[k] : bfull);
+    }
     // the tcgen05 forms (variants 4, 5 and 6)
     for (int k = 0; k < 3; ++k) {
       dg::LaunchShape m0, m1;
@@ -929,11 +972,13 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
 int dg_plan_set_variant(dg_plan* p, int32_t variant) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
   if (variant < 0 || variant >= DG_NUM_VARIANTS)
-    return fail(DG_ERR_ARGUMENT, "variant must be 0..6");
-  if ((variant & 1) && p->precision != DG_FP32_MIXED)
+    return fail(DG_ERR_ARGUMENT, "variant must be 0..10");
+  if (((variant & 1) || is_shape_variant(variant)) && p->precision != DG_FP32_MIXED)
     return fail(DG_ERR_UNSUPPORTED, "tensor-core products are a mixed-precision variant");
-  if (variant >= 4 && !p->tcm[variant - 4])
+  if (is_tcm_variant(variant) && !p->tcm[variant - 4])
     return fail(DG_ERR_UNSUPPORTED, "the tcgen05 kernels are mixed-precision variants");
+  if (is_shape_variant(variant) && !p->tcb[shape_index(variant)])
+    return fail(DG_ERR_UNSUPPORTED, "this tile shape does not fit on an SM");
   if (p->tc) return fail(DG_ERR_UNSUPPORTED, "DG_FP64_TC plans have one variant");
   p->variant = variant;
   return DG_OK;
@@ -1003,8 +1048,10 @@ int autotune_impl(dg_plan* p, const double* q, double* rhs, const double* ref,
   for (int v = 0; v < DG_NUM_VARIANTS && code == DG_OK; ++v) {
     float ms = -1.f;
     double rel = -1.0;
-    const bool have = v < 4 || p->tcm[v - 4];
-    if (v < nvar && have && ((v & 1) == 0 || p->precision == DG_FP32_MIXED)) {
+    const bool have = v < 4 || (is_tcm_variant(v) && p->tcm[v - 4]) ||
+                      (is_shape_variant(v) && p->tcb[shape_index(v)]);
+    const bool mixed_only = (v & 1) || is_shape_variant(v);
+    if (v < nvar && have && (!mixed_only || p->precision == DG_FP32_MIXED)) {
       p->variant = v;
       code = dg_rhs(p, q, rhs, stream);  // warm-up
       if (code == DG_OK) err = cudaEventRecord(e0, s);
@@ -1275,7 +1322,7 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
     a.ops = p->d_tc_ops;
     a.ops_bytes = p->tc_ops_bytes;
     err = tc_launch_of(p->equation, p->order, 0, a, p->tc_grid, s);
-  } else if (p->variant >= 4) {
+  } else if (is_tcm_variant(p->variant)) {
     const int k = p->variant - 4;
     a.ops = p->d_tcm_ops[k];
     a.ops_bytes = p->tcm_ops_bytes[k];
@@ -1327,7 +1374,7 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     a.ops = p->d_tc_ops;
     a.ops_bytes = p->tc_ops_bytes;
     err = tc_launch_of(p->equation, p->order, 1, a, p->tc_grid, s);
-  } else if (p->variant >= 4) {
+  } else if (is_tcm_variant(p->variant)) {
     const int k = p->variant - 4;
     a.ops = p->d_tcm_ops[k];
     a.ops_bytes = p->tcm_ops_bytes[k];
@@ -1545,14 +1592,19 @@ int dg_plan_info(const dg_plan* p, int64_t* nelements, int32_t* order,
   if (nelements) *nelements = p->nel;
   if (order) *order = p->order;
   if (nfields) *nfields = p->nfields;
-  const bool m4 = !p->tc && p->variant >= 4;
+  const bool m4 = !p->tc && is_tcm_variant(p->variant);
+  const bool mb = !p->tc && is_shape_variant(p->variant);
   const int k = m4 ? p->variant - 4 : 0;
+  const int kb = mb ? shape_index(p->variant) : 0;
   if (grid) *grid = p->tc ? p->tc_grid : (m4 ? p->tcm_grid[k] : main_grid(p));
   if (block)
-    *block = p->tc ? p->tc_shape.threads : (m4 ? p->tcm_shape[k].threads : dg::kBlock);
+    *block = p->tc ? p->tc_shape.threads
+                   : (m4 ? p->tcm_shape[k].threads
+                         : (mb ? p->tcb_shape[kb].threads : dg::kBlock));
   if (smem_bytes)
     *smem_bytes = p->tc ? p->tc_shape.smem_bytes
-                        : (m4 ? p->tcm_shape[k].smem_bytes : p->shape.smem_bytes);
+                        : (m4 ? p->tcm_shape[k].smem_bytes
+                              : (mb ? p->tcb_shape[kb].smem_bytes : p->shape.smem_bytes));
   return DG_OK;
 }
 

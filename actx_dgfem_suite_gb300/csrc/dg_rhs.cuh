@@ -49,8 +49,16 @@ namespace dg {
 
 // bit 0: RK stage epilogue; bit 1: face values from the face-shared kernels;
 // bit 2: mixed precision with the volume and LIFT contractions on the tensor
-// cores (3xTF32 split, FP32 accumulation)
-enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_SPLIT = 2, MODE_TC = 4 };
+// cores (3xTF32 split, FP32 accumulation); bits 3 and 4 (MODE_TC only): the
+// tile shape, 128 or 512 threads per CTA and E = 128 / Np or 512 / Np
+// elements per tile instead of kBlock = 256 threads and 256 / Np elements
+enum { MODE_RHS = 0, MODE_STAGE = 1, MODE_SPLIT = 2, MODE_TC = 4, MODE_B128 = 8,
+       MODE_B512 = 16 };
+
+// threads per CTA (one per (element, node) of the tile) of a mode
+constexpr int block_of(int mode) {
+  return (mode & MODE_B128) ? 128 : ((mode & MODE_B512) ? 512 : kBlock);
+}
 
 struct RhsArgs {
   const double* q;
@@ -136,12 +144,12 @@ struct OpsLayout {
 // staged, and for Euler the face values reuse the flux-input buffer of the
 // volume term (they are loaded after the volume contractions), which keeps
 // more CTAs resident at the low orders.
-template <int N, int EQ, typename Real, bool SPLIT = false>
+template <int N, int EQ, typename Real, bool SPLIT = false, int BLOCK = kBlock>
 struct Tile {
   static constexpr int NP = Shape<N>::NP, NFP = Shape<N>::NFP,
                        NFPT = Shape<N>::NFPT;
   static constexpr int NF = EqInfo<EQ>::NF, NAUX = EqInfo<EQ>::NAUX;
-  static constexpr int E = kBlock / NP;
+  static constexpr int E = BLOCK / NP;
   static constexpr bool MIXED = !std::is_same<Real, double>::value;
   static constexpr int RS = (int)sizeof(Real);
   static constexpr int ROW = Pitch<N, Real>::ROW, FROW = Pitch<N, Real>::FROW;
@@ -195,13 +203,14 @@ __device__ __forceinline__ void mma_tf32(float* c, const uint32_t* a, uint32_t b
 // C (M x NC, FP32, row-major with leading dimension NC) = A (M x K) B (K x NC)
 // with A(m, k), B(k, n) read through accessors (zero outside the ranges),
 // a b = a_hi b_hi + a_hi b_lo + a_lo b_hi in FP32 (relative error ~2^-21,
-// the accuracy of FP32 arithmetic).  Warp units: one m-tile x two n-tiles.
-template <int M, int K, int NC, class FA, class FB>
+// the accuracy of FP32 arithmetic).  Warp units: one m-tile x two n-tiles,
+// spread over the CTA's NWARPS warps.
+template <int M, int K, int NC, int NWARPS, class FA, class FB>
 __device__ __forceinline__ void tf32x3_gemm(FA fa, FB fb, float* out) {
   constexpr int MT = (M + 15) / 16, KT = (K + 7) / 8, NT = (NC + 7) / 8;
   constexpr int NB = (NT + 1) / 2, UNITS = MT * NB;
   const int lane = threadIdx.x & 31, g = lane >> 2, tq = lane & 3;
-  for (int u = threadIdx.x >> 5; u < UNITS; u += kBlock / 32) {
+  for (int u = threadIdx.x >> 5; u < UNITS; u += NWARPS) {
     const int mt = u / NB, nt0 = 2 * (u - mt * NB);
     const bool two = nt0 + 1 < NT;
     float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
@@ -263,14 +272,17 @@ __device__ __forceinline__ Real to_real(double v) {
 }
 
 template <int N, int EQ, typename Real, int MODE>
-__global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
-  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0>;
+__global__ void __launch_bounds__(block_of(MODE)) dg_rhs_kernel(const RhsArgs a) {
+  constexpr int BLOCK = block_of(MODE);
+  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0, BLOCK>;
   using Ops = OpsLayout<N, Real>;
   constexpr bool STAGE = (MODE & MODE_STAGE) != 0;
   constexpr bool SPLIT = (MODE & MODE_SPLIT) != 0;
   constexpr bool TCM = (MODE & MODE_TC) != 0;
   static_assert(!(SPLIT && T::MIXED), "the face-shared path is FP64 only");
   static_assert(!TCM || T::MIXED, "tensor-core products are a mixed-precision mode");
+  static_assert(BLOCK == kBlock || TCM, "other tile shapes are MODE_TC variants");
+  static_assert(T::E >= 1, "at least one element per tile");
   constexpr int NP = T::NP, NFPT = T::NFPT, NF = T::NF, E = T::E;
   constexpr int ROW = T::ROW, FROW = T::FROW;  // shared-memory row pitches
   extern __shared__ __align__(128) unsigned char smem[];
@@ -306,7 +318,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     // padded rows are read by the vector loads: give the pads a value once
     float* z = reinterpret_cast<float*>(smem + T::QR);
     const int nz = (T::GEO - T::QR) / 4;
-    for (int idx = t; idx < nz; idx += kBlock) z[idx] = 0.0f;
+    for (int idx = t; idx < nz; idx += BLOCK) z[idx] = 0.0f;
   }
   __syncthreads();
   if (!ops_ok) return;
@@ -331,7 +343,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       const double* qk = a.q + e0 * NP;
 #pragma unroll
       for (int k = 0; k < NF; ++k, qk += nelnp) {
-        for (int rem = t; rem < E * NP; rem += kBlock) {
+        for (int rem = t; rem < E * NP; rem += BLOCK) {
           const double v = rem < ecount * NP ? __ldg(qk + rem) : 0.0;
           sQ[k * (E * NP) + rem] = v;
           if constexpr (T::MIXED) {
@@ -343,11 +355,11 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     }
     {
       const double* mt = a.metric + e0 * 9;
-      for (int idx = t; idx < 9 * E; idx += kBlock)
+      for (int idx = t; idx < 9 * E; idx += BLOCK)
         sG[idx] = idx < 9 * ecount ? to_real<Real>(__ldg(mt + idx)) : zero;
       if constexpr (!SPLIT) {  // face geometry: the fused path's fluxes only
         const double* ft = a.face_geom + e0 * 16;
-        for (int idx = t; idx < 16 * E; idx += kBlock)
+        for (int idx = t; idx < 16 * E; idx += BLOCK)
           sFG[idx] = idx < 16 * ecount ? to_real<Real>(__ldg(ft + idx)) : zero;
       }
     }
@@ -358,7 +370,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       const double* fk = a.flux_in + e0 * NFPT;
 #pragma unroll
       for (int k = 0; k < NF; ++k, fk += nfpt_all)
-        for (int rem = t; rem < E * NFPT; rem += kBlock)
+        for (int rem = t; rem < E * NFPT; rem += BLOCK)
           sFlux[k * (E * FROW) + rem] = rem < ecount * NFPT ? __ldg(fk + rem) : zero;
     };
     if constexpr (SPLIT && !T::LATE_FLUX) load_face_values();
@@ -441,15 +453,15 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
       // tensor-core products into sTC, then the per-node combinations
       constexpr int VNC = T::VOL_NC;
       if constexpr (EQ == DG_WAVE) {
-        tf32x3_gemm<3 * NP, NP, E>(
+        tf32x3_gemm<3 * NP, NP, E, BLOCK / 32>(
             [&](int m, int k) { return sW[m * ROW + k]; },
             [&](int k, int n) { return sQr[n * ROW + k]; }, sTC);
-        tf32x3_gemm<NP, 3 * NP, E>(
+        tf32x3_gemm<NP, 3 * NP, E, BLOCK / 32>(
             [&](int m, int k) { const int r = k / NP; return sW[(r * NP + m) * ROW + k - r * NP]; },
             [&](int k, int n) { const int r = k / NP; return sAux[(r * E + n) * ROW + k - r * NP]; },
             sTC + 3 * NP * E);
       } else if constexpr (EQ == DG_EULER) {
-        tf32x3_gemm<NP, 3 * NP, VNC>(
+        tf32x3_gemm<NP, 3 * NP, VNC, BLOCK / 32>(
             [&](int m, int k) { const int r = k / NP; return sW[(r * NP + m) * ROW + k - r * NP]; },
             [&](int k, int n) {
               const int r = k / NP, f = n / E, e = n - f * E;
@@ -457,7 +469,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
             },
             sTC);
       } else {
-        tf32x3_gemm<3 * NP, NP, VNC>(
+        tf32x3_gemm<3 * NP, NP, VNC, BLOCK / 32>(
             [&](int m, int k) { return sW[m * ROW + k]; },
             [&](int k, int n) { return sQr[n * ROW + k]; }, sTC);
       }
@@ -625,7 +637,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
     // {{{ 4. face gather + numerical flux (fused path only)
     const uint32_t* gt = a.gather + e0 * NFPT;
     const uint32_t tile_node0 = (uint32_t)(e0 * NP);
-    for (int pidx = t; pidx < (SPLIT ? 0 : ecount * NFPT); pidx += kBlock) {
+    for (int pidx = t; pidx < (SPLIT ? 0 : ecount * NFPT); pidx += BLOCK) {
       const int elp = pidx / NFPT;
       const int fj = pidx - elp * NFPT;
       const int f = fj / Shape<N>::NFP;
@@ -781,7 +793,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs_kernel(const RhsArgs a) {
 
     // {{{ 5. LIFT, then store or fold into the RK stage
     if constexpr (TCM) {
-      tf32x3_gemm<NP, NFPT, NF * E>(
+      tf32x3_gemm<NP, NFPT, NF * E, BLOCK / 32>(
           [&](int m, int k) { return sL[m * FROW + k]; },
           [&](int k, int n) { return sFlux[n * FROW + k]; }, sTC);
       __syncthreads();

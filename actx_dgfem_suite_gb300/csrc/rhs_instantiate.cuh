@@ -1,8 +1,9 @@
 // Instantiates the RHS kernel of one equation for orders 1..4, FP64 and
 // mixed precision, plain RHS and fused RK stage (FP64 also in the
 // face-shared split form, with its face kernel; mixed precision also with
-// the contractions on tcgen05), and defines the equation's shape/launch
-// entry points.  Included by exactly one .cu file per equation.
+// the contractions on mma.sync tensor cores at three tile shapes, and on
+// tcgen05), and defines the equation's shape/launch entry points.  Included
+// by exactly one .cu file per equation.
 #pragma once
 
 #include <type_traits>
@@ -18,31 +19,47 @@ namespace {
 
 template <int N, int EQ, typename Real, int MODE>
 constexpr int smem_of() {
-  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0>;
+  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0, block_of(MODE)>;
   return (MODE & MODE_TC) ? T::SMEM_BYTES_TC : T::SMEM_BASE;
 }
 
+// dynamic shared memory a CTA may request (227 KB on sm_100 / sm_103)
+constexpr int kMaxDynSmem = 227 * 1024;
+
+// A tile shape whose shared memory exceeds the CTA limit is reported with
+// blocks_per_sm = 0 (not supported) instead of an error, and never launched.
 template <int N, int EQ, typename Real, int MODE>
 cudaError_t shape_impl(LaunchShape* out) {
-  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0>;
+  using T = Tile<N, EQ, Real, (MODE & MODE_SPLIT) != 0, block_of(MODE)>;
   constexpr int SMEM = smem_of<N, EQ, Real, MODE>();
-  auto kern = dg_rhs_kernel<N, EQ, Real, MODE>;
-  cudaError_t err = cudaFuncSetAttribute(
-      kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
-  if (err != cudaSuccess) return err;
-  int nb = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kBlock, SMEM);
   out->smem_bytes = SMEM;
-  out->blocks_per_sm = nb;
+  out->blocks_per_sm = 0;
   out->elems_per_tile = T::E;
   out->ops_bytes = OpsLayout<N, Real>::SIZE;
-  return err;
+  out->threads = block_of(MODE);
+  if constexpr (SMEM > kMaxDynSmem) {
+    return cudaSuccess;
+  } else {
+    auto kern = dg_rhs_kernel<N, EQ, Real, MODE>;
+    cudaError_t err = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    if (err != cudaSuccess) return err;
+    int nb = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, block_of(MODE), SMEM);
+    out->blocks_per_sm = nb;
+    return err;
+  }
 }
 
 template <int N, int EQ, typename Real, int MODE>
 cudaError_t launch_impl(const RhsArgs& a, int grid, cudaStream_t s) {
-  dg_rhs_kernel<N, EQ, Real, MODE><<<grid, kBlock, smem_of<N, EQ, Real, MODE>(), s>>>(a);
-  return cudaGetLastError();
+  constexpr int SMEM = smem_of<N, EQ, Real, MODE>();
+  if constexpr (SMEM > kMaxDynSmem) {
+    return cudaErrorInvalidConfiguration;
+  } else {
+    dg_rhs_kernel<N, EQ, Real, MODE><<<grid, block_of(MODE), SMEM, s>>>(a);
+    return cudaGetLastError();
+  }
 }
 
 template <int N, int EQ, typename Real>
@@ -60,9 +77,14 @@ cudaError_t shape_mode(int mode, LaunchShape* out) {
       default: break;
     }
   } else {
+    constexpr int T1 = MODE_TC | MODE_B128, T5 = MODE_TC | MODE_B512;
     switch (mode) {
       case MODE_TC: return shape_impl<N, EQ, Real, MODE_TC>(out);
       case MODE_TC | MODE_STAGE: return shape_impl<N, EQ, Real, MODE_TC | MODE_STAGE>(out);
+      case T1: return shape_impl<N, EQ, Real, T1>(out);
+      case T1 | MODE_STAGE: return shape_impl<N, EQ, Real, T1 | MODE_STAGE>(out);
+      case T5: return shape_impl<N, EQ, Real, T5>(out);
+      case T5 | MODE_STAGE: return shape_impl<N, EQ, Real, T5 | MODE_STAGE>(out);
       default: break;
     }
   }
@@ -84,10 +106,15 @@ cudaError_t launch_mode(int mode, const RhsArgs& a, int grid, cudaStream_t s) {
       default: break;
     }
   } else {
+    constexpr int T1 = MODE_TC | MODE_B128, T5 = MODE_TC | MODE_B512;
     switch (mode) {
       case MODE_TC: return launch_impl<N, EQ, Real, MODE_TC>(a, grid, s);
       case MODE_TC | MODE_STAGE:
         return launch_impl<N, EQ, Real, MODE_TC | MODE_STAGE>(a, grid, s);
+      case T1: return launch_impl<N, EQ, Real, T1>(a, grid, s);
+      case T1 | MODE_STAGE: return launch_impl<N, EQ, Real, T1 | MODE_STAGE>(a, grid, s);
+      case T5: return launch_impl<N, EQ, Real, T5>(a, grid, s);
+      case T5 | MODE_STAGE: return launch_impl<N, EQ, Real, T5 | MODE_STAGE>(a, grid, s);
       default: break;
     }
   }
@@ -109,7 +136,7 @@ cudaError_t launch_n(int precision, int mode, const RhsArgs& a, int grid,
 
 template <int EQ>
 cudaError_t shape_any(int order, int precision, int mode, LaunchShape* out) {
-  if ((precision != 0 && precision != 1) || mode < 0 || mode > 7)
+  if ((precision != 0 && precision != 1) || mode < 0 || mode > 31)
     return cudaErrorInvalidValue;
   switch (order) {
     case 1: return shape_n<1, EQ>(precision, mode, out);
@@ -123,7 +150,7 @@ cudaError_t shape_any(int order, int precision, int mode, LaunchShape* out) {
 template <int EQ>
 cudaError_t launch_any(int order, int precision, int mode, const RhsArgs& a,
                        int grid, cudaStream_t s) {
-  if ((precision != 0 && precision != 1) || mode < 0 || mode > 7)
+  if ((precision != 0 && precision != 1) || mode < 0 || mode > 31)
     return cudaErrorInvalidValue;
   switch (order) {
     case 1: return launch_n<1, EQ>(precision, mode, a, grid, s);

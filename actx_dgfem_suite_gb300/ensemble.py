@@ -45,9 +45,11 @@ class Ensemble:
     def autotune(self, q: torch.Tensor, reps: int = 3,
                  max_rel_l2: float | None = None) -> dict:
         """Pick the launch variant of the batched kernel (CUDA-core or
-        ``mma.sync`` products, persistent or one-CTA-per-tile grid, tcgen05
-        exact-digit or 3xTF32 products, the latter at two CTA sizes) by
-        timing it on the ensemble state ``q``; call before :meth:`capture`.
+        ``mma.sync`` products, the latter at three tile shapes of 128, 256
+        or 512 threads and as many nodes per tile; persistent or
+        one-CTA-per-tile grid; tcgen05 exact-digit or 3xTF32 products, the
+        latter at two CTA sizes) by timing it on the ensemble state ``q``;
+        call before :meth:`capture`.
         With ``max_rel_l2``, only variants whose result lies within that
         relative L2 distance of the FP64 RHS of ``q`` (evaluated here by an
         FP64 plan on the same union mesh) compete."""

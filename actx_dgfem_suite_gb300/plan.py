@@ -252,10 +252,16 @@ class DevicePlan:
 
     #: launch variants: bit 0 tensor-core products (fp32-mixed), bit 1 one CTA per
     #: tile; 4 and 5 the tcgen05 kernel (exact digit pairs, 3xTF32), 6 the
-    #: 3xTF32 kernel at its other CTA size
+    #: 3xTF32 kernel at its other CTA size; 7-10 the tensor-core (mma.sync)
+    #: kernel at its other tile shapes (128 or 512 threads, 128 / Np or
+    #: 512 / Np elements per tile; variants 1 and 3 use 256 and 256 / Np)
     VARIANTS = {0: "persistent", 1: "tensor-core, persistent", 2: "one CTA per tile",
                 3: "tensor-core, one CTA per tile", 4: "tcgen05, persistent",
-                5: "tcgen05 3xTF32, persistent", 6: "tcgen05 3xTF32, other CTA size"}
+                5: "tcgen05 3xTF32, persistent", 6: "tcgen05 3xTF32, other CTA size",
+                7: "tensor-core, 128-thread tiles, persistent",
+                8: "tensor-core, 128-thread tiles, one CTA per tile",
+                9: "tensor-core, 512-thread tiles, persistent",
+                10: "tensor-core, 512-thread tiles, one CTA per tile"}
 
     def set_variant(self, variant: int) -> None:
         _lib.check(self._lib.dg_plan_set_variant(self._handle, int(variant)))

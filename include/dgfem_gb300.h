@@ -261,7 +261,7 @@ typedef struct dg_box_desc {
 int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
 
 /* Number of launch variants (0 .. DG_NUM_VARIANTS - 1). */
-#define DG_NUM_VARIANTS 7
+#define DG_NUM_VARIANTS 11
 
 /* Launch variant of the plan's main kernel: bit 0 = contractions on the
  * tensor cores (DG_FP32_MIXED plans: 3xTF32 split with FP32 accumulation,
@@ -275,7 +275,13 @@ int dg_box_mesh_build(const dg_box_desc* desc, void* stream);
  * (FP32 accuracy, far fewer instructions per tile); 6 = variant 5 with the
  * other CTA size for the same 128-row tile (128 threads at orders 2-3, so
  * that more tiles are in flight per SM, 256 at orders 1 and 4): the tile
- * shape the autotuner chooses along with the variant.
+ * shape the autotuner chooses along with the variant; 7-10 = variant 1's
+ * mma.sync products at the two other tile shapes of that kernel, one
+ * thread per (element, node) of the tile: 7 (persistent) and 8 (one CTA
+ * per tile) with 128 threads and 128 / Np elements per tile, 9 and 10 with
+ * 512 threads and 512 / Np elements (variants 1 and 3: 256 / Np).  A
+ * variant the plan does not support (a precision it does not apply to, or
+ * a tile that does not fit on an SM) is refused with DG_ERR_UNSUPPORTED.
  * Default 0.  No counterpart in the reference. */
 int dg_plan_set_variant(dg_plan* plan, int32_t variant);
 
@@ -358,7 +364,8 @@ const char* dg_last_error(void);
  * writes 5 floats to ms_per_variant, variant 4 added; 4: variants that
  * raise a device-side status report -1, dg_plan_autotune_bounded and
  * dg_rhs_adjoint_stage added; 5: dg_rhs_vjp_stage and variants 5 and 6
- * added, the autotuners write DG_NUM_VARIANTS = 7 entries). */
+ * added, the autotuners write DG_NUM_VARIANTS = 7 entries; 6: the tile-shape
+ * variants 7-10, DG_NUM_VARIANTS = 11). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus

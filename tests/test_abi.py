@@ -42,7 +42,7 @@ def test_variant_count_matches_the_header():
 
 def test_version_and_error_strings():
     L = _lib.lib()
-    assert L.dg_abi_version() == 5
+    assert L.dg_abi_version() == 6
     assert isinstance(L.dg_last_error(), bytes)
 
 

@@ -1,7 +1,7 @@
 """Launch variants and the autotuner: the mixed-precision kernel with its
 contractions on the tensor cores (3xTF32, FP32 accumulation; warp-level
-mma.sync or one tcgen05 product per tile) keeps the mixed path's accuracy;
-the one-CTA-per-tile grid gives identical results."""
+mma.sync at three tile shapes, or one tcgen05 product per tile) keeps the
+mixed path's accuracy; the one-CTA-per-tile grid gives identical results."""
 
 from __future__ import annotations
 
@@ -42,19 +42,30 @@ def test_tensor_core_mixed_matches_fp64(equation, order):
     r1 = mixed.rhs(q)
     mixed.set_variant(3)
     r3 = mixed.rhs(q)
+    shaped = {}
+    for v in (7, 8, 9, 10):   # 128- and 512-thread tiles, both grids
+        mixed.set_variant(v)
+        info = mixed.info()
+        assert info["tensor_cores"] and info["block"] == (128 if v <= 8 else 512)
+        shaped[v] = mixed.rhs(q)
     mixed.finish()
     n64 = float(torch.linalg.norm(r64))
     assert float(torch.linalg.norm(r1 - r64)) <= MIXED_RTOL * n64
     assert float(torch.linalg.norm(r1 - r0)) <= MIXED_RTOL * n64
     assert torch.equal(r1, r3)            # same tiles, same arithmetic
+    for v, r in shaped.items():
+        assert float(torch.linalg.norm(r - r64)) <= MIXED_RTOL * n64, v
+    assert torch.equal(shaped[7], shaped[8])
+    assert torch.equal(shaped[9], shaped[10])
 
 
-def test_tensor_core_mixed_rk_stage():
+@pytest.mark.parametrize("variant", [1, 7, 10])
+def test_tensor_core_mixed_rk_stage(variant):
     prob, ref, mixed = _plans("euler", 3, seed=4)
     q = torch.from_numpy(prob.fields).cuda()
     outs = []
-    for plan, variant in ((ref, 0), (mixed, 1)):
-        plan.set_variant(variant)
+    for plan, v in ((ref, 0), (mixed, variant)):
+        plan.set_variant(v)
         res = torch.zeros_like(q)
         qo = torch.empty_like(q)
         plan.rk_stage(q, qo, res, 0.0, 0.5, 1e-3)
@@ -68,14 +79,16 @@ def test_autotune_picks_a_supported_variant():
     prob, ref, mixed = _plans("maxwell", 3)
     q = torch.from_numpy(prob.fields).cuda()
     res = mixed.autotune(q, reps=2)
-    assert res["chosen"] in (0, 1, 2, 3, 4, 5, 6)
+    assert res["chosen"] in range(len(mixed.VARIANTS))
     assert all(v is not None and v > 0 for v in res["ms"].values())
     res64 = ref.autotune(q, reps=2)
     assert res64["chosen"] in (0, 2)
     assert res64["ms"]["tensor-core, persistent"] is None
+    assert all(res64["ms"][mixed.VARIANTS[v]] is None for v in (7, 8, 9, 10))
     from actx_dgfem_suite_gb300._lib import DGError
-    with pytest.raises(DGError):
-        ref.set_variant(1)
+    for v in (1, 7, 10):
+        with pytest.raises(DGError):
+            ref.set_variant(v)
 
 
 def test_bounded_autotune_respects_the_error_budget():
@@ -90,7 +103,7 @@ def test_bounded_autotune_respects_the_error_budget():
     for budget in (1e-3, 0.0):
         res = mixed.autotune(q, reps=1, ref=r64, max_rel_l2=budget)
         errs = {names[k]: v for k, v in res["rel_l2"].items() if v is not None}
-        assert set(errs) == {0, 1, 2, 3, 4, 5, 6}
+        assert set(errs) == set(range(len(mixed.VARIANTS)))
         for v, e in errs.items():  # the reported errors are the real ones
             mixed.set_variant(v)
             got = mixed.rhs(q)
