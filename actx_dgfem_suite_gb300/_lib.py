@@ -13,7 +13,7 @@ _LIB_PATH = Path(__file__).resolve().parent / "libdgfem_gb300.so"
 _lib = None
 
 #: ABI version this binding is written for (dg_abi_version() of the library)
-ABI_VERSION = 6
+ABI_VERSION = 7
 
 DG_OK = 0
 DG_ERR_ARGUMENT = 1
@@ -33,7 +33,7 @@ DG_FP64_TC = 2
 NUM_VARIANTS = 11
 
 #: every entry point declared in include/dgfem_gb300.h
-EXPORTED_SYMBOLS = ("dg_plan_create", "dg_rhs", "dg_rk_stage", "dg_finish",
+EXPORTED_SYMBOLS = ("dg_plan_create", "dg_plan_create_2d", "dg_rhs", "dg_rk_stage", "dg_finish",
                     "dg_plan_destroy", "dg_plan_set_element_scale",
                     "dg_rhs_adjoint", "dg_rhs_adjoint_noalloc",
                     "dg_rhs_adjoint_stage", "dg_rhs_vjp", "dg_rhs_vjp_stage",
@@ -63,6 +63,21 @@ class MeshDesc(ctypes.Structure):
         ("lift", ctypes.c_void_p),
         ("face_nodes", ctypes.c_void_p),
         ("face_partner", ctypes.c_void_p),
+    ]
+
+
+class MeshDesc2D(ctypes.Structure):
+    """``dg_mesh2d_desc``: a triangle mesh."""
+    _fields_ = [
+        ("order", ctypes.c_int32),
+        ("nelements", ctypes.c_int64),
+        ("metric", ctypes.c_void_p),
+        ("face_geom", ctypes.c_void_p),
+        ("gather", ctypes.c_void_p),
+        ("weak_diff", ctypes.c_void_p),
+        ("strong_diff", ctypes.c_void_p),
+        ("lift", ctypes.c_void_p),
+        ("face_nodes", ctypes.c_void_p),
     ]
 
 
@@ -123,6 +138,10 @@ def lib() -> ctypes.CDLL:
                                  ctypes.c_int32, ctypes.POINTER(MeshDesc),
                                  ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
     L.dg_plan_create.restype = ctypes.c_int
+    L.dg_plan_create_2d.argtypes = [ctypes.POINTER(vp), ctypes.c_int32,
+                                    ctypes.POINTER(MeshDesc2D),
+                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int32]
+    L.dg_plan_create_2d.restype = ctypes.c_int
     L.dg_rhs.argtypes = [vp, vp, vp, vp]
     L.dg_rhs.restype = ctypes.c_int
     dbl = ctypes.c_double

@@ -187,6 +187,7 @@ struct dg_plan {
   int32_t equation = 0;
   int32_t precision = 0;
   int32_t order = 0;
+  int dim = 3;             // 2: triangle mesh (dg_plan_create_2d)
   int32_t np = 0, nfp = 0, nfields = 0;
   int64_t nel = 0;
   const double* metric = nullptr;
@@ -677,7 +678,7 @@ extern "C" {
 
 const char* dg_last_error(void) { return g_last_error.c_str(); }
 
-int32_t dg_abi_version(void) { return 6; }
+int32_t dg_abi_version(void) { return 7; }
 
 int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,
@@ -969,8 +970,105 @@ int dg_plan_create(dg_plan** plan_out, int32_t equation, int32_t precision,
   return DG_OK;
 }
 
+int dg_plan_create_2d(dg_plan** plan_out, int32_t equation,
+                      const dg_mesh2d_desc* mesh, const double* params,
+                      int32_t nparams) {
+  g_last_error.clear();
+  if (!plan_out) return fail(DG_ERR_ARGUMENT, "plan output pointer is NULL");
+  *plan_out = nullptr;
+  if (!mesh) return fail(DG_ERR_ARGUMENT, "mesh description is NULL");
+  const int nf = equation == DG_WAVE ? 3 : (equation == DG_EULER ? 4 : (equation == DG_MAXWELL ? 3 : 0));
+  if (nf == 0) return fail(DG_ERR_ARGUMENT, "unknown equation");
+  if (mesh->order < 1 || mesh->order > 4)
+    return fail(DG_ERR_UNSUPPORTED, "order must be 1..4");
+  if (mesh->nelements < 1) return fail(DG_ERR_ARGUMENT, "nelements must be >= 1");
+  const int N = mesh->order;
+  const int np = (N + 1) * (N + 2) / 2, nfp = N + 1;
+  if (mesh->nelements * (int64_t)np >= (int64_t(1) << 31))
+    return fail(DG_ERR_ARGUMENT, "Nel * Np must be < 2^31 (31-bit gather indices)");
+  if (!mesh->metric || !mesh->face_geom || !mesh->gather || !mesh->lift ||
+      !mesh->face_nodes)
+    return fail(DG_ERR_ARGUMENT, "a mesh array pointer is NULL");
+  const double* diff = equation == DG_MAXWELL ? mesh->strong_diff : mesh->weak_diff;
+  if (!diff)
+    return fail(DG_ERR_ARGUMENT, equation == DG_MAXWELL ? "strong_diff is NULL"
+                                                         : "weak_diff is NULL");
+  if (nparams != nparams_of(equation) || (nparams > 0 && !params))
+    return fail(DG_ERR_ARGUMENT, "wrong number of equation parameters");
+  for (int k = 0; k < 3 * nfp; ++k)
+    if (mesh->face_nodes[k] < 0 || mesh->face_nodes[k] >= np)
+      return fail(DG_ERR_ARGUMENT, "face_nodes entry out of range");
+  if (equation == DG_MAXWELL && (params[1] <= 0 || params[2] <= 0))
+    return fail(DG_ERR_ARGUMENT, "epsilon and mu must be positive");
+  for (const void* ptr : {(const void*)mesh->metric, (const void*)mesh->face_geom,
+                          (const void*)mesh->gather}) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, ptr) != cudaSuccess ||
+        attr.type != cudaMemoryTypeDevice) {
+      cudaGetLastError();
+      return fail(DG_ERR_ARGUMENT, "metric, face_geom and gather must be device memory");
+    }
+  }
+  dg::LaunchShape shape, other;
+  cudaError_t err = dg::shape_2d(equation, N, dg::MODE_RHS, &shape);
+  if (err == cudaSuccess) err = dg::shape_2d(equation, N, dg::MODE_STAGE, &other);
+  if (err != cudaSuccess) return cuda_fail(err, "2D kernel configuration");
+  if (other.blocks_per_sm < shape.blocks_per_sm) shape.blocks_per_sm = other.blocks_per_sm;
+  if (shape.blocks_per_sm < 1) return fail(DG_ERR_UNSUPPORTED, "kernel does not fit on an SM");
+  const int ops_bytes = dg::pack_ops_2d(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0);
+  if (ops_bytes != shape.ops_bytes)
+    return fail(DG_ERR_CUDA, "operator layout mismatch between host and kernel");
+  std::vector<unsigned char> ops(ops_bytes, 0);
+  dg::pack_ops_2d(N, diff, mesh->lift, mesh->face_nodes, ops.data(), ops_bytes);
+
+  dg_plan* p = new dg_plan;
+  p->dim = 2;
+  p->equation = equation;
+  p->precision = DG_FP64;
+  p->order = N;
+  p->np = np;
+  p->nfp = nfp;
+  p->nfields = nf;
+  p->nel = mesh->nelements;
+  p->metric = mesh->metric;
+  p->face_geom = mesh->face_geom;
+  p->gather = mesh->gather;
+  p->shape = shape;
+  p->ops_bytes = static_cast<uint32_t>(ops_bytes);
+  for (int k = 0; k < nparams; ++k) p->params[k] = params[k];
+  if (equation == DG_MAXWELL) {  // flux and mass constants, as in 3D
+    const double z = std::sqrt(params[2] / params[1]), y = 1.0 / z;
+    p->k[0] = z;
+    p->k[1] = y;
+    p->k[2] = -1.0 / (z + z);
+    p->k[3] = 1.0 / (y + y);
+    p->k[4] = 1.0 / params[1];
+    p->k[5] = 1.0 / params[2];
+  }
+  cudaGetDevice(&p->device);
+  err = cudaMalloc(&p->d_ops, p->ops_bytes);
+  if (err == cudaSuccess) err = cudaMalloc(&p->d_status, sizeof(int));
+  if (err == cudaSuccess)
+    err = cudaMemcpy(p->d_ops, ops.data(), p->ops_bytes, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemset(p->d_status, 0, sizeof(int));
+  if (err != cudaSuccess) {
+    dg_plan_destroy(p);
+    return cuda_fail(err, "plan buffers");
+  }
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, p->device);
+  p->nsm = nsm;
+  p->ntiles = (p->nel + shape.elems_per_tile - 1) / shape.elems_per_tile;
+  const int64_t full = (int64_t)nsm * shape.blocks_per_sm;
+  p->grid = (int)(p->ntiles < full ? p->ntiles : full);
+  *plan_out = p;
+  return DG_OK;
+}
+
 int dg_plan_set_variant(dg_plan* p, int32_t variant) {
   if (!p) return fail(DG_ERR_ARGUMENT, "plan is NULL");
+  if (p->dim == 2 && variant != 0)
+    return fail(DG_ERR_UNSUPPORTED, "triangle-mesh plans have one variant");
   if (variant < 0 || variant >= DG_NUM_VARIANTS)
     return fail(DG_ERR_ARGUMENT, "variant must be 0..10");
   if (((variant & 1) || is_shape_variant(variant)) && p->precision != DG_FP32_MIXED)
@@ -1033,6 +1131,7 @@ int take_status(dg_plan* p, cudaStream_t s, int* status) {
 int autotune_impl(dg_plan* p, const double* q, double* rhs, const double* ref,
                   double max_rel_l2, int32_t reps, void* stream, int32_t* chosen,
                   float* ms_per_variant, double* err_per_variant) {
+  if (p->dim == 2) return fail(DG_ERR_UNSUPPORTED, "triangle-mesh plans have one variant");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int nvar = p->tc ? 1 : DG_NUM_VARIANTS;
   const int64_t n = (int64_t)p->nfields * p->nel * p->np;
@@ -1308,6 +1407,11 @@ int dg_rhs(dg_plan* p, const double* q, double* rhs, void* stream) {
   a.q = q;
   a.rhs = rhs;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (p->dim == 2) {
+    cudaError_t err = dg::launch_2d(p->equation, p->order, dg::MODE_RHS, a, p->grid, s);
+    if (err != cudaSuccess) return cuda_fail(err, "rhs launch");
+    return DG_OK;
+  }
   if (p->split) {
     cudaError_t err = launch_faces(p, q, s);
     if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");
@@ -1360,6 +1464,11 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
     a.rhs_unscaled = rhs_unscaled;
   }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (p->dim == 2) {
+    cudaError_t err = dg::launch_2d(p->equation, p->order, dg::MODE_STAGE, a, p->grid, s);
+    if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
+    return DG_OK;
+  }
   if (p->split) {
     cudaError_t err = launch_faces(p, q_in, s);
     if (err != cudaSuccess) return cuda_fail(err, "face kernel launch");

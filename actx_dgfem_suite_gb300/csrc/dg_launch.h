@@ -95,6 +95,17 @@ int pack_tcm_ops(int order, const double* diff, const double* lift,
                  const int32_t* face_nodes, unsigned char* out, int out_bytes,
                  bool tf32);
 
+// Triangle meshes (rhs_2d.cu): shape query and launch of dg_rhs2d_kernel
+// for mode MODE_RHS or MODE_STAGE (FP64), and the operator block
+// [Wt (2 Np Np) | Lt (3 Nfp Np) | int32 edge nodes (3 Nfp)] packed from the
+// host arrays diff (2, Np, Np), lift (Np, 3, Nfp), face_nodes (3, Nfp);
+// returns the block size (out == NULL: size only; -1 if out_bytes is short).
+cudaError_t shape_2d(int eq, int order, int mode, LaunchShape* out);
+cudaError_t launch_2d(int eq, int order, int mode, const RhsArgs& a, int grid,
+                      cudaStream_t s);
+int pack_ops_2d(int order, const double* diff, const double* lift,
+                const int32_t* face_nodes, unsigned char* out, int out_bytes);
+
 // Record `msg` as the calling thread's last error (dg_last_error) and
 // return `code`; shared by the translation units behind the C ABI.
 int set_error(int code, const char* msg);

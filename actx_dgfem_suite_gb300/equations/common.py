@@ -25,7 +25,7 @@ from actx_dgfem_suite_gb300.discretization import DGDiscretization
 @dataclass
 class Problem:
     equation: str             # "wave" | "euler" | "maxwell"
-    disc: DGDiscretization
+    disc: DGDiscretization    # or discretization2d.DGDiscretization2D (triangles)
     fields: np.ndarray        # (nfields, Nel, Np) initial state, FP64
     params: tuple             # wave (c,), euler (gamma,), maxwell (alpha, eps, mu)
     t: float | None           # time argument of euler / maxwell operators
@@ -35,17 +35,23 @@ class Problem:
     def nfields(self) -> int:
         return self.fields.shape[0]
 
+    @property
+    def dim(self) -> int:
+        return getattr(self.disc, "dim", 3)
 
-def state_template(equation: str):
-    """An empty container of the equation's state type (for rebuilding)."""
+
+def state_template(equation: str, dim: int = 3):
+    """An empty container of the equation's state type (for rebuilding); on
+    triangle meshes (``dim=2``) vectors have two components and Maxwell
+    carries the TM fields (E_z, H_x, H_y)."""
     ph = DOFArray(None, [None])
     if equation == "wave":
-        return WaveState(u=ph, v=_obj_array([ph, ph, ph]))
+        return WaveState(u=ph, v=_obj_array([ph] * dim))
     if equation == "euler":
         return ConservedEulerField(mass=ph, energy=ph,
-                                   momentum=_obj_array([ph, ph, ph]))
+                                   momentum=_obj_array([ph] * dim))
     if equation == "maxwell":
-        return _obj_array([ph] * 6)
+        return _obj_array([ph] * (6 if dim == 3 else 3))
     raise ValueError(equation)
 
 
@@ -90,10 +96,12 @@ class DGOperator:
 def make_rhs_and_args(problem: Problem, actx):
     """``(rhs, args)`` in the reference's calling convention: wave
     ``(WaveState,)``; euler ``(np.float64(t), ConservedEulerField)``; maxwell
-    ``(np.float64(t), object ndarray of 6 DOFArrays)``."""
+    ``(np.float64(t), object ndarray of 6 DOFArrays)`` (3 on triangle
+    meshes)."""
     from actx_dgfem_suite_gb300.array_context import stacked_state
     op = DGOperator(problem, actx)
-    state = stacked_state(actx, state_template(problem.equation), problem.fields)
+    state = stacked_state(actx, state_template(problem.equation, problem.dim),
+                          problem.fields)
     if problem.equation == "wave":
         return op, (state,)
     return op, (np.float64(problem.t), state)

@@ -12,6 +12,12 @@ Problem definitions:
 * ``"baseline"``: box [0, 1]^3, epsilon = mu = 1, alpha = 1 (upwind), state =
   a seeded mix of eight plane waves with random directions, polarisations and
   phases.
+
+With ``dim=2`` (triangles on [0, 1]^2) the operator is the TM restriction,
+grudge's field subset for ``dimensions=2``: state (E_z, H_x, H_y).  The
+reference definition uses the cavity mode (2, 3) (``maxwell.py:62-66``),
+whose real part at t = 0 is E_z = sin(2 pi x) sin(3 pi y), H = 0; the
+benchmark one a seeded mix of in-plane TM plane waves.
 """
 
 from __future__ import annotations
@@ -19,6 +25,7 @@ from __future__ import annotations
 import numpy as np
 
 from actx_dgfem_suite_gb300.discretization import make_box_discretization
+from actx_dgfem_suite_gb300.discretization2d import make_box_discretization_2d
 from actx_dgfem_suite_gb300.equations.common import Problem, make_rhs_and_args
 from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
 from actx_dgfem_suite_gb300.xp import array_module, zeros
@@ -92,29 +99,67 @@ def plane_wave_mix(nodes, seed: int = 0, nwaves: int = 8):
     return out
 
 
+def cavity_mode_tm_real_t0(nodes, mode=(2, 3)):
+    """Real part at t = 0 of the 2D TM cavity mode of the unit square:
+    (E_z, H_x, H_y) = (sin(kx x) sin(ky y), 0, 0)."""
+    xp = array_module(nodes)
+    kx, ky = (m * np.pi for m in mode)
+    x, y = nodes[0], nodes[1]
+    out = zeros(x, (3,) + tuple(x.shape))
+    out[0] = xp.sin(kx * x) * xp.sin(ky * y)
+    return out
+
+
+def plane_wave_mix_tm(nodes, seed: int = 0, nwaves: int = 8):
+    """Sum of in-plane TM vacuum plane waves E_z = a cos(k.x + phi),
+    (H_x, H_y) = (k^_y, -k^_x) E_z, |k| in 2 pi [1, 3], from a fixed seed."""
+    xp = array_module(nodes)
+    rng = np.random.default_rng(seed)
+    out = zeros(nodes, (3,) + tuple(nodes.shape[1:]))
+    for _ in range(nwaves):
+        theta = rng.uniform(0.0, 2 * np.pi)
+        kx, ky = np.cos(theta), np.sin(theta)
+        kmag = 2 * np.pi * rng.uniform(1.0, 3.0)
+        amp = rng.uniform(0.5, 1.0)
+        phase = rng.uniform(0.0, 2 * np.pi)
+        ez = amp * xp.cos(kmag * (kx * nodes[0] + ky * nodes[1]) + phase)
+        out[0] += ez
+        out[1] += ky * ez
+        out[2] += -kx * ez
+    return out
+
+
 def maxwell_problem(order: int, nel_1d: int, definition: str = "reference",
-                    epsilon: float = 1.0, mu: float = 1.0, seed: int = 0) -> Problem:
+                    epsilon: float = 1.0, mu: float = 1.0, seed: int = 0,
+                    dim: int = 3) -> Problem:
     if definition not in ALPHA:
         raise ValueError(f"unknown problem definition {definition!r}")
-    disc = make_box_discretization(order, nel_1d, 0.0, 1.0)
+    disc = (make_box_discretization(order, nel_1d, 0.0, 1.0) if dim == 3
+            else make_box_discretization_2d(order, nel_1d, 0.0, 1.0))
     fields = initial_state(disc.nodes(), definition, seed)
     return Problem("maxwell", disc, fields,
                    (ALPHA[definition], float(epsilon), float(mu)), 0.5, definition)
 
 
 def initial_state(nodes, definition: str, seed: int = 0):
-    if definition == "reference":
+    if len(nodes) == 2:   # triangle meshes: TM fields
+        if definition == "reference":
+            return cavity_mode_tm_real_t0(nodes)
+        if definition == "baseline":
+            return plane_wave_mix_tm(nodes, seed=seed)
+    elif definition == "reference":
         return cavity_mode_real_t0(nodes)
-    if definition == "baseline":
+    elif definition == "baseline":
         return plane_wave_mix(nodes, seed=seed)
     raise ValueError(f"unknown problem definition {definition!r}")
 
 
 def get_maxwell_rhs(*, actx, dim: int, order: int, ndofs: int,
                     definition: str = "reference", nel_1d: int | None = None):
-    """``(rhs, (t, w))`` as ``maxwell.py:43-74``."""
-    if dim != 3:
-        raise NotImplementedError("only 3D tetrahedral meshes are implemented")
+    """``(rhs, (t, w))`` as ``maxwell.py:43-74`` (``dim`` 3: tetrahedra, 2:
+    triangles with the TM fields)."""
+    if dim not in (2, 3):
+        raise NotImplementedError("dim must be 2 or 3")
     if nel_1d is None:
         nel_1d = get_nel_1d_for_regular_rect_mesh(dim, order, int(ndofs))
-    return make_rhs_and_args(maxwell_problem(order, nel_1d, definition), actx)
+    return make_rhs_and_args(maxwell_problem(order, nel_1d, definition, dim=dim), actx)

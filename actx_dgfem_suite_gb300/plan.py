@@ -19,6 +19,8 @@ from actx_dgfem_suite_gb300.discretization import DGDiscretization
 EQUATIONS = {"wave": _lib.DG_WAVE, "euler": _lib.DG_EULER,
              "maxwell": _lib.DG_MAXWELL}
 NFIELDS = {"wave": 4, "euler": 5, "maxwell": 6}
+#: fields on triangle meshes: (u, v_x, v_y); (rho, E, m_x, m_y); TM (E_z, H_x, H_y)
+NFIELDS_2D = {"wave": 3, "euler": 4, "maxwell": 3}
 
 
 def _stream_handle(stream) -> ctypes.c_void_p:
@@ -42,6 +44,8 @@ class DeviceMesh:
         if not torch.cuda.is_available():
             raise RuntimeError("DeviceMesh needs a CUDA device")
         self.disc = disc
+        #: 3 (tetrahedra) or 2 (triangles)
+        self.dim = getattr(disc, "dim", 3)
         dev = torch.device(device or "cuda")
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
@@ -61,9 +65,12 @@ class DeviceMesh:
                 np.ascontiguousarray(disc.face_geometry())).to(self.device)
             self.gather = torch.from_numpy(
                 disc.gather_index().view(np.int32)).to(self.device)
-            # glued face-point index (face-shared path, adjoint)
+            # glued face-point index (face-shared path, adjoint; 3D only)
             self.partner = None
-            if with_partner is not False and (with_partner or disc.perm_id is not None):
+            if with_partner and self.dim == 2:
+                raise ValueError("triangle meshes carry no face partners")
+            if (self.dim == 3 and with_partner is not False
+                    and (with_partner or disc.perm_id is not None)):
                 self.partner = torch.from_numpy(disc.face_partner()).to(self.device)
         ref = disc.ref
         self._weak = np.ascontiguousarray(ref.weak_diff, dtype=np.float64)
@@ -79,7 +86,19 @@ class DeviceMesh:
     def np_(self) -> int:
         return self.disc.np_
 
-    def desc(self) -> _lib.MeshDesc:
+    def desc(self):
+        if self.dim == 2:
+            d = _lib.MeshDesc2D()
+            d.order = self.disc.order
+            d.nelements = self.nelements
+            d.metric = self.metric.data_ptr()
+            d.face_geom = self.face_geom.data_ptr()
+            d.gather = self.gather.data_ptr()
+            d.weak_diff = self._weak.ctypes.data
+            d.strong_diff = self._strong.ctypes.data
+            d.lift = self._lift.ctypes.data
+            d.face_nodes = self._fnodes.ctypes.data
+            return d
         d = _lib.MeshDesc()
         d.order = self.disc.order
         d.nelements = self.nelements
@@ -120,16 +139,24 @@ class DevicePlan:
         self.mesh = mesh
         self.equation = equation
         self.precision = precision
-        self.nfields = NFIELDS[equation]
+        self.dim = mesh.dim
+        if self.dim == 2 and precision != "fp64":
+            raise ValueError("triangle-mesh plans evaluate in FP64 only")
+        self.nfields = (NFIELDS_2D if self.dim == 2 else NFIELDS)[equation]
         self.params = tuple(float(p) for p in params)
         L = _lib.lib()
         handle = ctypes.c_void_p()
         parr = (ctypes.c_double * max(1, len(self.params)))(*self.params)
         with torch.cuda.device(mesh.device):
-            _lib.check(L.dg_plan_create(ctypes.byref(handle), EQUATIONS[equation],
-                                        PRECISIONS[precision],
-                                        ctypes.byref(mesh.desc()), parr,
-                                        len(self.params)))
+            if self.dim == 2:
+                _lib.check(L.dg_plan_create_2d(ctypes.byref(handle), EQUATIONS[equation],
+                                               ctypes.byref(mesh.desc()), parr,
+                                               len(self.params)))
+            else:
+                _lib.check(L.dg_plan_create(ctypes.byref(handle), EQUATIONS[equation],
+                                            PRECISIONS[precision],
+                                            ctypes.byref(mesh.desc()), parr,
+                                            len(self.params)))
         self._handle = handle
         self._lib = L
 

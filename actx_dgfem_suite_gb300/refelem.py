@@ -477,3 +477,119 @@ def reference_tet(order: int) -> ReferenceTet:
 
 
 # }}}
+
+
+# {{{ the reference triangle (2D meshes)
+
+#: local vertex indices of each edge of a triangle, meshmode's order (edge k
+#: leaves out vertex 2 - k, like the tetrahedron's face k leaves out 3 - k)
+TRI_FACE_VERTICES = ((0, 1), (2, 0), (1, 2))
+TRI_FACE_OPPOSITE_VERTEX = (2, 1, 0)
+TRI_NFACES = 3
+
+
+def pkdo_tri_grad_interior(order: int, x: np.ndarray) -> np.ndarray:
+    """(2, npoints, Np) gradient of :func:`pkdo_tri` at points strictly
+    inside the triangle, by dual numbers."""
+    npt = x.shape[0]
+    eye = np.eye(2)
+    r = Dual(x[:, 0], np.outer(eye[0], np.ones(npt)))
+    s = Dual(x[:, 1], np.outer(eye[1], np.ones(npt)))
+    a = 2.0 * (1.0 + r) / (1.0 - s) - 1.0
+    b = s
+    cols = []
+    for (i, j) in multi_indices(2, order):
+        pa = jacobi_orthonormal(a, 0.0, 0.0, i)[i]
+        pb = jacobi_orthonormal(b, 2 * i + 1.0, 0.0, j)[j]
+        cols.append((math.sqrt(2.0) * pa * pb * (1 - b) ** i).grad)
+    return np.stack(cols, axis=2)
+
+
+def legendre_orthonormal_1d(order: int, x: np.ndarray) -> np.ndarray:
+    """(npoints, N+1) orthonormal Legendre polynomials on [-1, 1]."""
+    return np.stack(jacobi_orthonormal(x, 0.0, 0.0, order), axis=1)
+
+
+@dataclass(frozen=True)
+class ReferenceTri:
+    """Per-order constants of the nodal DG discretisation on triangles.
+
+    Array shapes use Np = (N+1)(N+2)/2 volume nodes and Nfp = N+1 nodes per
+    edge; the fields match :class:`ReferenceTet` with 2 reference axes and
+    3 faces."""
+
+    order: int
+    nodes: np.ndarray            # (Np, 2) biunit-triangle coordinates
+    vdm: np.ndarray              # (Np, Np)
+    mass: np.ndarray             # (Np, Np)
+    diff: np.ndarray             # (2, Np, Np) strong D_r
+    weak_diff: np.ndarray        # (2, Np, Np) M^-1 S_r^T
+    face_nodes: np.ndarray       # (3, Nfp) volume-node index of each edge node
+    face_mass: np.ndarray        # (Nfp, Nfp) biunit-segment mass on the edge nodes
+    lift: np.ndarray             # (Np, 3, Nfp) M^-1 E
+    face_perm: dict              # vertex permutation of an edge -> (Nfp,) node map
+
+    @property
+    def np_(self) -> int:
+        return self.nodes.shape[0]
+
+    @property
+    def nfp(self) -> int:
+        return self.face_nodes.shape[1]
+
+
+def _tri_face_node_lists(order: int) -> np.ndarray:
+    """(3, Nfp): for edge k with local vertices (a, b), the volume nodes with
+    barycentric multi-index (N - i at a, i at b), i = 0..N (from a to b)."""
+    bary_mi = {(order - sum(mi),) + tuple(mi): idx
+               for idx, mi in enumerate(multi_indices(2, order))}
+    out = []
+    for (a, b) in TRI_FACE_VERTICES:
+        row = []
+        for i in range(order + 1):
+            alpha = [0, 0, 0]
+            alpha[a] = order - i
+            alpha[b] = i
+            row.append(bary_mi[tuple(alpha)])
+        out.append(row)
+    return np.array(out, dtype=np.int64)
+
+
+@lru_cache(maxsize=None)
+def reference_tri(order: int) -> ReferenceTri:
+    if order < 1:
+        raise ValueError("order must be >= 1")
+    nodes = barycentric_to_biunit(recursive_barycentric_nodes(2, order))
+    npn = nodes.shape[0]
+    vdm = pkdo_tri(order, nodes)
+    vinv = np.linalg.inv(vdm)
+    mass = vinv.T @ vinv
+    qpts, qw = tri_quadrature(order + 1)
+    psi_q = pkdo_tri(order, qpts)
+    dpsi_q = pkdo_tri_grad_interior(order, qpts)
+    cmod = np.einsum("q,qm,rqn->rmn", qw, psi_q, dpsi_q)
+    diff = np.einsum("pm,rmn,nk->rpk", vdm, cmod, vinv)
+    weak_diff = np.einsum("pm,rnm,nk->rpk", vdm, cmod, vinv)
+
+    fnodes = _tri_face_node_lists(order)
+    g = 2.0 * np.array(gll_points_01(order)) - 1.0       # edge nodes on [-1, 1]
+    v1 = legendre_orthonormal_1d(order, g)
+    v1inv = np.linalg.inv(v1)
+    fmass = v1inv.T @ v1inv
+    nfp = order + 1
+    emat = np.zeros((npn, TRI_NFACES, nfp))
+    for f in range(TRI_NFACES):
+        emat[fnodes[f], f, :] = fmass
+    lift = np.einsum("ik,kfj->ifj", vdm @ vdm.T, emat)
+    # edge gluing: the neighbour runs its edge in the opposite direction
+    # (conforming meshes) or in the same one
+    perm = {(0, 1): np.arange(nfp, dtype=np.int64),
+            (1, 0): np.arange(nfp, dtype=np.int64)[::-1].copy()}
+    arrs = dict(nodes=nodes, vdm=vdm, mass=mass, diff=diff, weak_diff=weak_diff,
+                face_nodes=fnodes, face_mass=fmass, lift=lift)
+    for v in arrs.values():
+        v.setflags(write=False)
+    return ReferenceTri(order=order, face_perm=perm, **arrs)
+
+
+# }}}

@@ -29,15 +29,17 @@ def get_rhs(equation: str, actx, dim: int, degree: int, *,
             device_setup: bool = False) -> tuple[Any, tuple[Any, ...]]:
     """Return ``(rhs_callable, call_args)`` for ``equation``.
 
-    ``device_setup=True`` builds the box mesh, geometry, connectivity and
-    initial state on the array context's GPU instead of on the host."""
+    ``dim`` 3 builds tetrahedral box meshes, 2 triangle meshes (the suite's
+    CI runs both, ``--dims 2,3``).  ``device_setup=True`` builds the 3D box
+    mesh, geometry, connectivity and initial state on the array context's
+    GPU instead of on the host."""
     base, ndofs = split_equation_name(equation)
     if device_setup:
         from actx_dgfem_suite_gb300.device_setup import device_problem
         from actx_dgfem_suite_gb300.equations.common import make_rhs_and_args
         from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
         if dim != 3:
-            raise NotImplementedError("only 3D tetrahedral meshes are implemented")
+            raise NotImplementedError("device-side setup builds 3D meshes only")
         if base not in ("wave", "euler", "maxwell"):
             raise NotImplementedError(f"equation '{equation}' not supported")
         n = nel_1d or get_nel_1d_for_regular_rect_mesh(dim, degree, ndofs)
@@ -61,18 +63,18 @@ def get_problem(equation: str, dim: int, degree: int, *,
                 definition: str = "reference", nel_1d: int | None = None):
     """Host-side setup only (mesh, geometry, initial state), no device."""
     from actx_dgfem_suite_gb300.utils import get_nel_1d_for_regular_rect_mesh
-    if dim != 3:
-        raise NotImplementedError("only 3D tetrahedral meshes are implemented")
+    if dim not in (2, 3):
+        raise NotImplementedError("dim must be 2 or 3")
     base, ndofs = split_equation_name(equation)
     if nel_1d is None:
         nel_1d = get_nel_1d_for_regular_rect_mesh(dim, degree, ndofs)
     if base == "wave":
         from actx_dgfem_suite_gb300.equations.wave import wave_problem
-        return wave_problem(degree, nel_1d, definition)
+        return wave_problem(degree, nel_1d, definition, dim=dim)
     if base == "euler":
         from actx_dgfem_suite_gb300.equations.euler import euler_problem
-        return euler_problem(degree, nel_1d, definition)
+        return euler_problem(degree, nel_1d, definition, dim=dim)
     if base == "maxwell":
         from actx_dgfem_suite_gb300.equations.maxwell import maxwell_problem
-        return maxwell_problem(degree, nel_1d, definition)
+        return maxwell_problem(degree, nel_1d, definition, dim=dim)
     raise NotImplementedError(f"equation '{equation}' not supported")

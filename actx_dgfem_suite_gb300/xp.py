@@ -25,6 +25,6 @@ def zeros(like, shape):
 
 
 def r2(nodes, center=(0.0, 0.0, 0.0)):
-    """|x - center|^2 of (3, ...) node coordinates."""
-    return ((nodes[0] - center[0]) ** 2 + (nodes[1] - center[1]) ** 2
-            + (nodes[2] - center[2]) ** 2)
+    """|x - center|^2 of (dim, ...) node coordinates (dim 2 or 3; the center's
+    leading ``dim`` entries are used)."""
+    return sum((nodes[x] - center[x]) ** 2 for x in range(len(nodes)))

@@ -98,6 +98,40 @@ int dg_plan_create(dg_plan** plan, int32_t equation, int32_t precision,
                    const dg_mesh_desc* mesh, const double* params,
                    int32_t nparams);
 
+/* Triangle meshes (the suite's dim = 2 runs).  Layouts (FP64, C order;
+ * Np = (N+1)(N+2)/2 nodes, Nfp = N+1 nodes per edge, 3 edges):
+ *   state / rhs : (nfields, Nel, Np)
+ *                 wave:    u, v_x, v_y                         (nfields = 3)
+ *                 euler:   mass, energy, momentum_x, _y        (nfields = 4)
+ *                 maxwell: E_z, H_x, H_y (TM fields, grudge's
+ *                          subset for dimensions = 2)          (nfields = 3)
+ *   metric      : (Nel, 2, 2)  dr_r/dx_x per element
+ *   face_geom   : (Nel, 3, 4)  n_x, n_y, sJ/J and a zero pad per edge
+ *   gather      : (Nel, 3, Nfp) uint32, as in 3D (bit 31 = boundary) */
+typedef struct dg_mesh2d_desc {
+  int32_t order;             /* polynomial degree N, 1..4 */
+  int64_t nelements;         /* Nel >= 1, Nel * Np < 2^31 */
+  const double* metric;      /* device, (Nel, 2, 2) */
+  const double* face_geom;   /* device, (Nel, 3, 4) */
+  const uint32_t* gather;    /* device, (Nel, 3, Nfp) */
+  const double* weak_diff;   /* host, (2, Np, Np): M^-1 S_r^T (wave, euler) */
+  const double* strong_diff; /* host, (2, Np, Np): D_r (maxwell) */
+  const double* lift;        /* host, (Np, 3, Nfp): M^-1 E */
+  const int32_t* face_nodes; /* host, (3, Nfp): volume node of each edge node */
+} dg_mesh2d_desc;
+
+/* Build a plan for a triangle mesh: FP64 arithmetic, one fused persistent
+ * launch per RHS (dg_rhs2d_kernel).  params as for dg_plan_create.  The plan
+ * works with dg_rhs, dg_rk_stage, dg_plan_set_element_scale, dg_finish,
+ * dg_plan_info, dg_plan_path and dg_plan_destroy; dg_plan_set_variant
+ * accepts variant 0 only, and the adjoint entry points and autotuners return
+ * DG_ERR_UNSUPPORTED.  Replaces actx.compile(rhs) for the builders' dim = 2
+ * meshes (actx_dgfem_suite/equations/wave.py:248-285, euler.py:140-186,
+ * maxwell.py:43-74). */
+int dg_plan_create_2d(dg_plan** plan, int32_t equation,
+                      const dg_mesh2d_desc* mesh, const double* params,
+                      int32_t nparams);
+
 /* One RHS evaluation: rhs = L(q), state and result FP64.  Enqueued on `stream` (a cudaStream_t,
  * NULL = legacy default stream); returns without synchronising.
  * q and rhs are device arrays of nfields * Nel * Np doubles and must not overlap.
@@ -365,7 +399,7 @@ const char* dg_last_error(void);
  * raise a device-side status report -1, dg_plan_autotune_bounded and
  * dg_rhs_adjoint_stage added; 5: dg_rhs_vjp_stage and variants 5 and 6
  * added, the autotuners write DG_NUM_VARIANTS = 7 entries; 6: the tile-shape
- * variants 7-10, DG_NUM_VARIANTS = 11). */
+ * variants 7-10, DG_NUM_VARIANTS = 11; 7: dg_plan_create_2d). */
 int32_t dg_abi_version(void);
 
 #ifdef __cplusplus

@@ -28,7 +28,10 @@ reference's discretisation follows): the biunit tetrahedron with vertices
 (-1,-1,-1), (1,-1,-1), (-1,1,-1), (-1,-1,1); node (i, j, k) (multi-indices
 with i + j + k <= N, first index fastest) has barycentric multi-index
 (N-i-j-k, i, j, k); the faces are the vertex triples (0,2,1), (0,1,3),
-(0,3,2), (1,2,3).
+(0,3,2), (1,2,3).  For 2D meshes the same constructions give the reference
+triangle: vertices (-1,-1), (1,-1), (-1,1), node (i, j) with barycentric
+multi-index (N-i-j, i, j), edges (0,1), (2,0), (1,2), and GLL points on the
+edges.
 """
 
 from __future__ import annotations
@@ -49,6 +52,8 @@ TET_VERTICES = np.array([[-1.0, -1.0, -1.0], [1.0, -1.0, -1.0],
                          [-1.0, 1.0, -1.0], [-1.0, -1.0, 1.0]])
 TRI_VERTICES = np.array([[-1.0, -1.0], [1.0, -1.0], [-1.0, 1.0]])
 FACES = ((0, 2, 1), (0, 1, 3), (0, 3, 2), (1, 2, 3))
+#: the edges of the triangle (2D meshes), meshmode's order
+TRI_EDGES = ((0, 1), (2, 0), (1, 2))
 
 
 # {{{ Legendre polynomials, Gauss and Gauss-Lobatto points (extended precision)
@@ -236,13 +241,15 @@ def modal_basis(order: int, x) -> list:
 
 
 def modal_basis_grads(order: int, x) -> list:
-    """[r][point][basis]: derivatives of the tetrahedron basis functions."""
-    out = [[], [], []]
+    """[r][point][basis]: derivatives of the basis functions (tetrahedron or,
+    for 2-coordinate points, triangle)."""
+    dim = len(x[0])
+    out = [[] for _ in range(dim)]
     for p in x:
-        v = [[legendre(k, p[d]) for k in range(order + 1)] for d in range(3)]
-        for r in range(3):
-            out[r].append([MP.fprod(v[d][e[d]][1 if d == r else 0] for d in range(3))
-                           for e in _exponents(3, order)])
+        v = [[legendre(k, p[d]) for k in range(order + 1)] for d in range(dim)]
+        for r in range(dim):
+            out[r].append([MP.fprod(v[d][e[d]][1 if d == r else 0] for d in range(dim))
+                           for e in _exponents(dim, order)])
     return out
 
 

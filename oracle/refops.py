@@ -30,11 +30,17 @@ from oracle.refelem import (
     FACES,
     MP,
     TET_VERTICES,
+    TRI_EDGES,
+    TRI_VERTICES,
+    gauss_01_mp,
+    gll_01_mp,
+    legendre,
     modal_basis,
     modal_basis_grads,
     tet_nodes,
     tet_nodes_mp,
     tet_rule,
+    tri_nodes,
     tri_nodes_mp,
     tri_rule,
 )
@@ -101,6 +107,49 @@ def oracle_ref_ops(order: int) -> OracleRefOps:
         fcoords[f] = np.array([[float(v) for v in on_face(x)] for x in fref])
     del nq
     return OracleRefOps(order=order, nodes=tet_nodes(order), mass=_f64(mass),
+                        stiff_t=np.stack([_f64(st) for st in stiff_t]),
+                        diff=np.stack([_f64(d) for d in diff]), face_mass=emat,
+                        face_node_coords=fcoords)
+
+
+@lru_cache(maxsize=None)
+def oracle_ref_ops_2d(order: int) -> OracleRefOps:
+    """The reference-triangle matrices (2D meshes), assembled like
+    :func:`oracle_ref_ops`: volume integrals by the collapsed rule, edge
+    integrals by Gauss-Legendre over each edge's own [-1, 1]
+    parametrisation with the Lagrange basis on the edge's GLL points."""
+    nodes_mp = tri_nodes_mp(order)
+    np_ = len(nodes_mp)
+    q, w = tri_rule(order + 1)                               # exact to degree 2N
+    vinv = _mat(modal_basis(order, nodes_mp)) ** -1
+    lag = _mat(modal_basis(order, q)) * vinv
+    dlag = [_mat(g) * vinv for g in modal_basis_grads(order, q)]
+    wd = MP.diag(w)
+    mass = lag.T * wd * lag
+    stiff_t = [d.T * wd * lag for d in dlag]
+    minv = mass ** -1
+    diff = [minv * st.T for st in stiff_t]
+
+    # edge nodes: GLL points on [-1, 1]; Lagrange basis through them
+    g = [2 * x - 1 for x in gll_01_mp(order)]
+    nfp = len(g)
+    v1inv = _mat([[legendre(k, x)[0] for k in range(order + 1)] for x in g]) ** -1
+    u, wu = gauss_01_mp(order + 1)                           # exact to degree 2N + 1
+    s1 = [2 * x - 1 for x in u]
+    w1 = MP.diag([2 * x for x in wu])
+    lag1 = _mat([[legendre(k, x)[0] for k in range(order + 1)] for x in s1]) * v1inv
+    emat = np.zeros((np_, 3, nfp))
+    fcoords = np.zeros((3, nfp, 2))
+    for f, (a, b) in enumerate(TRI_EDGES):
+        va, vb = [int(v) for v in TRI_VERTICES[a]], [int(v) for v in TRI_VERTICES[b]]
+
+        def on_edge(t):   # t in [-1, 1] from vertex a to vertex b
+            return tuple(((1 - t) * va[x] + (1 + t) * vb[x]) / 2 for x in range(2))
+
+        vol_lag = _mat(modal_basis(order, [on_edge(t) for t in s1])) * vinv
+        emat[:, f, :] = _f64(vol_lag.T * w1 * lag1)
+        fcoords[f] = np.array([[float(v) for v in on_edge(t)] for t in g])
+    return OracleRefOps(order=order, nodes=tri_nodes(order), mass=_f64(mass),
                         stiff_t=np.stack([_f64(st) for st in stiff_t]),
                         diff=np.stack([_f64(d) for d in diff]), face_mass=emat,
                         face_node_coords=fcoords)

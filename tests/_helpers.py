@@ -5,8 +5,14 @@ from __future__ import annotations
 import numpy as np
 
 from actx_dgfem_suite_gb300.discretization import make_discretization
+from actx_dgfem_suite_gb300.discretization2d import make_discretization_2d
 from actx_dgfem_suite_gb300.equations.common import Problem
-from actx_dgfem_suite_gb300.mesh import TetMesh, generate_box_tet_mesh
+from actx_dgfem_suite_gb300.mesh import (
+    TetMesh,
+    TriMesh,
+    generate_box_tet_mesh,
+    generate_box_tri_mesh,
+)
 
 #: relative L2 parity bound for the FP64 path against the CPU oracle
 FP64_RTOL = 1e-12
@@ -16,15 +22,17 @@ def oracle_rhs(problem: Problem, od=None, parts: bool = False):
     """Oracle RHS of ``problem``; with ``parts=True`` returns
     ``(rhs, scale)``, ``scale`` the L2 norm of the volume and surface terms
     that cancel into the RHS (see :func:`parity_error`)."""
-    from oracle.geometry import build_oracle_disc
+    from oracle.geometry import build_oracle_disc, build_oracle_disc_2d
     from oracle.rhs import euler_rhs, maxwell_rhs, wave_rhs
     d = problem.disc
+    dim = getattr(d, "dim", 3)
     if od is None:
-        od = build_oracle_disc(d.mesh.vertices, d.mesh.elements, d.order)
+        build = build_oracle_disc if dim == 3 else build_oracle_disc_2d
+        od = build(d.mesh.vertices, d.mesh.elements, d.order)
     check_node_layout(d, od)
     q = problem.fields
     if problem.equation == "wave":
-        rhs, vol, surf = wave_rhs(od, q[0], q[1:4], *problem.params, parts=True)
+        rhs, vol, surf = wave_rhs(od, q[0], q[1:1 + dim], *problem.params, parts=True)
     elif problem.equation == "euler":
         rhs, vol, surf = euler_rhs(od, q, *problem.params, parts=True)
     else:
@@ -72,6 +80,18 @@ def jittered_box_mesh(n: int, amp: float = 0.15, seed: int = 1) -> TetMesh:
     return TetMesh(vertices=v, elements=m.elements)
 
 
+def jittered_square_mesh(n: int, amp: float = 0.15, seed: int = 1) -> TriMesh:
+    """Triangle mesh on [0,1]^2 with interior vertices moved randomly
+    (counter-clockwise elements for amp < 0.25)."""
+    m = generate_box_tri_mesh(0.0, 1.0, n)
+    v = m.vertices.copy()
+    h = 1.0 / n
+    interior = np.all((v > 1e-12) & (v < 1 - 1e-12), axis=1)
+    rng = np.random.default_rng(seed)
+    v[interior] += amp * h * rng.uniform(-1, 1, size=(interior.sum(), 2))
+    return TriMesh(vertices=v, elements=m.elements)
+
+
 def single_tet_mesh() -> TetMesh:
     v = np.array([[0.0, 0, 0], [1.0, 0.1, 0], [0.2, 0.9, 0.1], [0.1, 0.2, 0.8]])
     return TetMesh(vertices=v, elements=np.array([[0, 1, 2, 3]], dtype=np.int64))
@@ -80,17 +100,18 @@ def single_tet_mesh() -> TetMesh:
 def smooth_fields(disc, nfields: int, equation: str, seed: int = 0) -> np.ndarray:
     """Smooth random-ish state; Euler gets positive density and pressure."""
     x = disc.nodes()
+    dim = x.shape[0]
     rng = np.random.default_rng(seed)
     out = np.empty((nfields,) + x.shape[1:])
     for k in range(nfields):
         a = rng.uniform(0.5, 2.0, size=3)
         ph = rng.uniform(0, 2 * np.pi, size=3)
         out[k] = np.sin(a[0] * 3 * x[0] + ph[0]) * np.cos(a[1] * 2 * x[1] + ph[1]) \
-            + 0.3 * np.sin(a[2] * 4 * x[2] + ph[2])
+            + 0.3 * np.sin(a[2] * 4 * x[dim - 1] + ph[2])
     if equation == "euler":
         out[0] = 1.0 + 0.2 * out[0] ** 2
-        out[2:5] *= 0.2
-        kinetic = 0.5 * (out[2:5] ** 2).sum(axis=0) / out[0]
+        out[2:2 + dim] *= 0.2
+        kinetic = 0.5 * (out[2:2 + dim] ** 2).sum(axis=0) / out[0]
         out[1] = 2.5 + 0.3 * out[1] ** 2 + kinetic
     return out
 
@@ -99,6 +120,20 @@ def make_problem(equation: str, mesh: TetMesh, order: int, fields=None,
                  params=None, seed: int = 0) -> Problem:
     disc = make_discretization(mesh, order)
     nf = {"wave": 4, "euler": 5, "maxwell": 6}[equation]
+    if params is None:
+        params = {"wave": (1.0,), "euler": (1.4,), "maxwell": (0.5, 1.0, 1.0)}[equation]
+    if fields is None:
+        fields = smooth_fields(disc, nf, equation, seed)
+    return Problem(equation, disc, fields, params,
+                   None if equation == "wave" else 0.5, "test")
+
+
+def make_problem_2d(equation: str, mesh: TriMesh, order: int, fields=None,
+                    params=None, seed: int = 0) -> Problem:
+    """A problem on a triangle mesh: fields (3, 4, 3) for wave, Euler and
+    Maxwell (TM)."""
+    disc = make_discretization_2d(mesh, order)
+    nf = {"wave": 3, "euler": 4, "maxwell": 3}[equation]
     if params is None:
         params = {"wave": (1.0,), "euler": (1.4,), "maxwell": (0.5, 1.0, 1.0)}[equation]
     if fields is None:

@@ -42,7 +42,7 @@ def test_variant_count_matches_the_header():
 
 def test_version_and_error_strings():
     L = _lib.lib()
-    assert L.dg_abi_version() == 6
+    assert L.dg_abi_version() == 7
     assert isinstance(L.dg_last_error(), bytes)
 
 
@@ -76,5 +76,18 @@ def test_argument_errors_without_device():
     assert L.dg_rhs_adjoint_stage(None, None, 1.0, None, None, None, None, 0.0, 0.0, 0.0,
                                   None, None) == _lib.DG_ERR_ARGUMENT
     assert L.dg_plan_set_variant(None, 0) == _lib.DG_ERR_ARGUMENT
+    # triangle meshes: the same argument checks before any CUDA call
+    assert L.dg_plan_create_2d(None, 0, None, None, 0) == _lib.DG_ERR_ARGUMENT
+    assert L.dg_plan_create_2d(ctypes.byref(h), 0, None, None, 0) == _lib.DG_ERR_ARGUMENT
+    d2 = _lib.MeshDesc2D()
+    d2.order = 5
+    d2.nelements = 10
+    assert L.dg_plan_create_2d(ctypes.byref(h), 0, ctypes.byref(d2), None, 0) \
+        == _lib.DG_ERR_UNSUPPORTED
+    d2.order = 2
+    assert L.dg_plan_create_2d(ctypes.byref(h), 9, ctypes.byref(d2), None, 0) \
+        == _lib.DG_ERR_ARGUMENT
+    assert L.dg_plan_create_2d(ctypes.byref(h), 0, ctypes.byref(d2), None, 0) \
+        == _lib.DG_ERR_ARGUMENT           # NULL device arrays
     with pytest.raises(_lib.DGError):
         _lib.check(L.dg_rhs(None, None, None, None))

@@ -59,8 +59,9 @@ def test_reference_initial_conditions():
     assert np.all(w.fields[1:] == 0.0) and w.params == (1.0,)
 
 
-def test_2d_not_implemented():
+def test_unsupported_dims_and_equations():
+    assert get_problem("tiny_wave", 2, 1).dim == 2      # triangles
     with pytest.raises(NotImplementedError):
-        get_problem("tiny_wave", 2, 1)
+        get_problem("tiny_wave", 1, 1)
     with pytest.raises(NotImplementedError):
         get_problem("tiny_burgers", 3, 1)
