@@ -18,6 +18,10 @@ state in and RHS out (FP64), the per-element metric (9 doubles), per-face
 normal + sJ/J (16 doubles) and one 4-byte gather index per face node.  The
 reference's ``get_footprint_bytes`` (``perf_analysis.py:581-619``) sums kernel
 arguments of its own kernel split instead.
+
+``dim=2`` (triangles, 3 edges) applies the same rules: the einsums have two
+reference axes, the state holds 3 (wave), 4 (Euler) or 3 (Maxwell TM)
+fields, the metric is 2x2 and each edge carries a 2-vector normal and sJ/J.
 """
 
 from __future__ import annotations
@@ -25,34 +29,40 @@ from __future__ import annotations
 from dataclasses import dataclass
 
 NFIELDS = {"wave": 4, "euler": 5, "maxwell": 6}
+NFIELDS_2D = {"wave": 3, "euler": 4, "maxwell": 3}
 
 
-def np_of(order: int) -> int:
+def np_of(order: int, dim: int = 3) -> int:
+    if dim == 2:
+        return (order + 1) * (order + 2) // 2
     return (order + 1) * (order + 2) * (order + 3) // 6
 
 
-def nfp_of(order: int) -> int:
+def nfp_of(order: int, dim: int = 3) -> int:
+    if dim == 2:
+        return order + 1
     return (order + 1) * (order + 2) // 2
 
 
 # {{{ einsum counts per element (suite rules; exact)
 
 
-def grad_flops(order: int) -> int:
-    """``re,rji,ej->ei``: 3 Np + 6 Np^2."""
-    n = np_of(order)
-    return 3 * n + 6 * n * n
+def grad_flops(order: int, dim: int = 3) -> int:
+    """``re,rji,ej->ei``: 3 Np + 6 Np^2 (2D: 2 Np + 4 Np^2)."""
+    n = np_of(order, dim)
+    return dim * n + 2 * dim * n * n
 
 
-def div_flops(order: int) -> int:
-    """``xre,rji,xej->ei``: 18 Np + 6 Np^2."""
-    n = np_of(order)
-    return 18 * n + 6 * n * n
+def div_flops(order: int, dim: int = 3) -> int:
+    """``xre,rji,xej->ei``: 18 Np + 6 Np^2 (2D: 8 Np + 4 Np^2)."""
+    n = np_of(order, dim)
+    return 2 * dim * dim * n + 2 * dim * n * n
 
 
-def lift_flops(order: int) -> int:
-    """``jfi,fe,fej->ei``: 4 Nfp + 8 Nfp Np."""
-    return 4 * nfp_of(order) + 8 * nfp_of(order) * np_of(order)
+def lift_flops(order: int, dim: int = 3) -> int:
+    """``jfi,fe,fej->ei``: 4 Nfp + 8 Nfp Np (2D, 3 edges: 3 Nfp + 6 Nfp Np)."""
+    nf = dim + 1
+    return nf * nfp_of(order, dim) + 2 * nf * nfp_of(order, dim) * np_of(order, dim)
 
 
 # }}}
@@ -64,25 +74,46 @@ _POINTWISE = {
     "euler": (251, 48),
     "maxwell": (72, 30),
 }
+#: the same on triangles: wave and Maxwell TM counted from the 2D flux
+#: expressions (wave: averages, jumps, v.n, u n and the upwind term with two
+#: components; Maxwell: the TM components of the alpha flux and the PEC
+#: mirror); Euler scaled from 3D by its flux components (8 of 15)
+_POINTWISE_2D = {
+    "wave": (27, 6),
+    "euler": (134, 26),
+    "maxwell": (28, 10),
+}
 
 
-def einsum_flops_per_element(equation: str, order: int) -> int:
+def einsum_flops_per_element(equation: str, order: int, dim: int = 3) -> int:
+    g, d, li = grad_flops(order, dim), div_flops(order, dim), lift_flops(order, dim)
+    if dim == 2:
+        if equation == "wave":      # 1 div + 2 grad + 3 LIFT
+            return d + 2 * g + 3 * li
+        if equation == "euler":     # 4 div + 4 LIFT
+            return 4 * d + 4 * li
+        if equation == "maxwell":   # 4 TM curl derivatives + 3 LIFT
+            return 4 * g + 3 * li
+        raise ValueError(equation)
     if equation == "wave":      # 1 div (u) + 3 grad (v) + 4 LIFT
-        return div_flops(order) + 3 * grad_flops(order) + 4 * lift_flops(order)
+        return d + 3 * g + 4 * li
     if equation == "euler":     # 5 div + 5 LIFT
-        return 5 * div_flops(order) + 5 * lift_flops(order)
+        return 5 * d + 5 * li
     if equation == "maxwell":   # 12 curl derivatives + 6 LIFT
-        return 12 * grad_flops(order) + 6 * lift_flops(order)
+        return 12 * g + 6 * li
     raise ValueError(equation)
 
 
-def flops_per_element(equation: str, order: int) -> int:
-    face, vol = _POINTWISE[equation]
-    return (einsum_flops_per_element(equation, order)
-            + face * 4 * nfp_of(order) + vol * np_of(order))
+def flops_per_element(equation: str, order: int, dim: int = 3) -> int:
+    face, vol = (_POINTWISE_2D if dim == 2 else _POINTWISE)[equation]
+    return (einsum_flops_per_element(equation, order, dim)
+            + face * (dim + 1) * nfp_of(order, dim) + vol * np_of(order, dim))
 
 
-def bytes_per_element(equation: str, order: int) -> int:
+def bytes_per_element(equation: str, order: int, dim: int = 3) -> int:
+    if dim == 2:   # metric 2x2, 3 edges x (n_x, n_y, sJ/J), 3 Nfp indices
+        return (16 * NFIELDS_2D[equation] * np_of(order, 2) + 4 * 8 + 9 * 8
+                + 3 * 4 * nfp_of(order, 2))
     return (16 * NFIELDS[equation] * np_of(order) + 9 * 8 + 16 * 8
             + 4 * 4 * nfp_of(order))
 
@@ -107,19 +138,21 @@ class RhsCost:
     equation: str
     order: int
     nelements: int
+    dim: int = 3
 
     @property
     def dofs(self) -> int:
         """DOF updates per RHS: nfields * Nel * Np."""
-        return NFIELDS[self.equation] * self.nelements * np_of(self.order)
+        nf = (NFIELDS_2D if self.dim == 2 else NFIELDS)[self.equation]
+        return nf * self.nelements * np_of(self.order, self.dim)
 
     @property
     def flops(self) -> int:
-        return self.nelements * flops_per_element(self.equation, self.order)
+        return self.nelements * flops_per_element(self.equation, self.order, self.dim)
 
     @property
     def bytes(self) -> int:
-        return self.nelements * bytes_per_element(self.equation, self.order)
+        return self.nelements * bytes_per_element(self.equation, self.order, self.dim)
 
     @property
     def fma(self) -> int:

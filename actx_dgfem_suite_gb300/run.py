@@ -50,7 +50,7 @@ def register_actx(name: str, actx_t: type) -> None:
 def _flops(equation: str, dim: int, degree: int, rhs) -> int:
     base = equation.split("_", 1)[-1] if equation.startswith(("tiny_", "large_")) \
         else equation
-    return RhsCost(base, degree, rhs.dg_operator.disc.nelements).flops
+    return RhsCost(base, degree, rhs.dg_operator.disc.nelements, dim).flops
 
 
 def peak_flop_rate(equation: str, dim: int, degree: int, nelements: int,
@@ -58,7 +58,7 @@ def peak_flop_rate(equation: str, dim: int, degree: int, nelements: int,
     """Roofline rate ``F / max(F/peakF, B/peakBW)`` (``perf_analysis.py:624-653``)."""
     base = equation.split("_", 1)[-1] if equation.startswith(("tiny_", "large_")) \
         else equation
-    c = RhsCost(base, degree, nelements)
+    c = RhsCost(base, degree, nelements, dim)
     return c.flops / c.roofline_seconds(peak_flops, peak_bw)
 
 

@@ -30,6 +30,33 @@ def test_einsum_counts_match_opt_einsum(order):
         == pm.lift_flops(order)
 
 
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_einsum_counts_match_opt_einsum_2d(order):
+    """Triangles: two reference axes, three edges."""
+    oe = pytest.importorskip("opt_einsum")
+    from math import prod
+    E = 7
+    n, nfp = pm.np_of(order, 2), pm.nfp_of(order, 2)
+
+    def count(spec, shapes):
+        ops = [np.empty(s) for s in shapes]
+        _, info = oe.contract_path(spec, *ops, optimize="optimal", use_blas=False)
+        tot = 0
+        for (_, contracted, es, _, _) in info.contraction_list:
+            it = prod(info.size_dict[c]
+                      for c in set(es.translate(str.maketrans("", "", " ->,"))))
+            tot += 2 * it if contracted else it
+        return tot // E
+
+    assert count("re,rji,ej->ei", [(2, E), (2, n, n), (E, n)]) == pm.grad_flops(order, 2)
+    assert count("xre,rji,xej->ei", [(2, 2, E), (2, n, n), (2, E, n)]) \
+        == pm.div_flops(order, 2)
+    assert count("jfi,fe,fej->ei", [(nfp, 3, n), (3, E), (3, E, nfp)]) \
+        == pm.lift_flops(order, 2)
+    c = pm.RhsCost("euler", order, 10, dim=2)
+    assert c.dofs == 4 * 10 * n and c.flops > 0 and c.bytes > 0
+
+
 def test_known_values():
     assert [pm.grad_flops(p) for p in (1, 2, 3, 4)] == [108, 630, 2460, 7455]
     assert [pm.div_flops(p) for p in (1, 2, 3, 4)] == [168, 780, 2760, 7980]
