@@ -9,9 +9,15 @@ element for each pointwise +, -, *, /, where, max, min and sqrt
 (``perf_analysis.py:265-377``).  That DAG cannot be built here, so this module
 applies the same rules to the einsums the mass-inverse fusion produces
 (``actx_dgfem_suite/arraycontext/mass_inverse_fuser.py:20-76``), which are
-exact, plus per-node / per-face-point pointwise counts of the restated flux
-and volume-flux expressions, which are estimates.  Agreement with the
-reference's own count is therefore unpinned.
+exact, plus per-node / per-face-point pointwise counts.  For the wave
+equation those are counted from the reference's own ``wave_operator`` run
+on stand-ins for its dependencies (``tests/golden/make_reference_flop_counts.py``:
+8 per node, 38 per face point of a trace pair's flux plus 1 per boundary
+face point for the mirrored state, and 8 per face point for summing the
+boundary and interior fluxes on all faces); what the reference's DAG
+transformations merge is not visible there.  Euler and Maxwell, whose
+operators live in grudge (absent), use estimates from the restated flux
+and volume-flux expressions.
 
 Bytes are the algorithmic minimum a fused implementation moves per RHS:
 state in and RHS out (FP64), the per-element metric (9 doubles), per-face
@@ -67,13 +73,17 @@ def lift_flops(order: int, dim: int = 3) -> int:
 
 # }}}
 
-#: pointwise operations per face point and per volume node (estimates from
-#: the restated expressions; see module docstring)
+#: pointwise operations per face point and per volume node: wave counted
+#: from the reference's wave_operator (38 flux + 8 all-faces sum per face
+#: point), Euler and Maxwell estimated from the restated expressions
 _POINTWISE = {
-    "wave": (38, 8),
+    "wave": (46, 8),
     "euler": (251, 48),
     "maxwell": (72, 30),
 }
+#: the wave boundary pair's extra operation per boundary face point (the
+#: mirrored exterior state -u)
+WAVE_BOUNDARY_EXTRA = 1
 #: the same on triangles: wave and Maxwell TM counted from the 2D flux
 #: expressions (wave: averages, jumps, v.n, u n and the upwind term with two
 #: components; Maxwell: the TM components of the alpha flux and the PEC
@@ -105,6 +115,7 @@ def einsum_flops_per_element(equation: str, order: int, dim: int = 3) -> int:
 
 
 def flops_per_element(equation: str, order: int, dim: int = 3) -> int:
+    """Per element, boundary terms aside (see :attr:`RhsCost.flops`)."""
     face, vol = (_POINTWISE_2D if dim == 2 else _POINTWISE)[equation]
     return (einsum_flops_per_element(equation, order, dim)
             + face * (dim + 1) * nfp_of(order, dim) + vol * np_of(order, dim))
@@ -139,6 +150,9 @@ class RhsCost:
     order: int
     nelements: int
     dim: int = 3
+    #: faces on the boundary (box of n^3 hexahedra: 12 n^2), for the wave
+    #: boundary pair's extra operation; 0 leaves it out
+    boundary_faces: int = 0
 
     @property
     def dofs(self) -> int:
@@ -148,7 +162,10 @@ class RhsCost:
 
     @property
     def flops(self) -> int:
-        return self.nelements * flops_per_element(self.equation, self.order, self.dim)
+        extra = 0
+        if self.equation == "wave" and self.dim == 3:
+            extra = WAVE_BOUNDARY_EXTRA * self.boundary_faces * nfp_of(self.order)
+        return self.nelements * flops_per_element(self.equation, self.order, self.dim) + extra
 
     @property
     def bytes(self) -> int:

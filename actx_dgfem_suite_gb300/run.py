@@ -47,10 +47,19 @@ def register_actx(name: str, actx_t: type) -> None:
     _NAME_TO_ACTX_CLASS[name] = actx_t
 
 
+def _boundary_faces(disc) -> int:
+    bd = getattr(disc, "is_boundary", None)
+    if bd is None:          # a mesh built on the device keeps no host mask:
+        return 0            # the wave boundary term (1 per boundary point) is left out
+    return int(bd.sum()) if hasattr(bd, "sum") else 0
+
+
 def _flops(equation: str, dim: int, degree: int, rhs) -> int:
     base = equation.split("_", 1)[-1] if equation.startswith(("tiny_", "large_")) \
         else equation
-    return RhsCost(base, degree, rhs.dg_operator.disc.nelements, dim).flops
+    disc = rhs.dg_operator.disc
+    return RhsCost(base, degree, disc.nelements, dim,
+                   boundary_faces=_boundary_faces(disc)).flops
 
 
 def peak_flop_rate(equation: str, dim: int, degree: int, nelements: int,

@@ -545,7 +545,8 @@ def our_arm(args) -> None:
         nel = rhs.dg_operator.disc.nelements
         runs.append(dict(eq=eq, order=order, n=n_eff, compiled=compiled,
                          call_args=call_args, q=q, out=out,
-                         cost=pm.RhsCost(eq, order, nel)))
+                         cost=pm.RhsCost(eq, order, nel,
+                                         boundary_faces=12 * n_eff * n_eff)))
         if hasattr(rhs.dg_operator.disc, "_cache"):
             rhs.dg_operator.disc._cache.clear()
     clear_box_cache()

@@ -11,8 +11,18 @@ composition of them -- signs, flux, boundary pair, which terms meet which
 operator -- against the oracle's restatement and the product, with grudge's
 trace conventions (``avg = (int + ext) / 2``, ``diff = ext - int``).
 
-Used only by ``tests/golden/make_reference_equations.py``, in a container
-that has the reference checkout; the fixtures it writes travel instead.
+Used only by ``tests/golden/make_reference_equations.py`` and
+``make_reference_flop_counts.py``, in a container that has the reference
+checkout; the fixtures they write travel instead.
+
+Operation counting (``counting()``): every arithmetic operation on DOF
+arrays adds the number of output elements, as the reference's FLOP counter
+counts its DAG's pointwise nodes (``actx_dgfem_suite/perf_analysis.py:250-377``),
+under the domain of its operands: ``"vol"`` (volume nodes), ``"bdry"``
+(traces on the boundary faces), ``"int"`` (interior-face trace pairs) or
+``"all"`` (the all-faces fluxes), the domain a DOF inherits from the
+projection or trace that made it.  The grudge operators (stand-ins over the
+oracle) are not counted here; their einsums are counted by the einsum rule.
 """
 
 from __future__ import annotations
@@ -36,21 +46,52 @@ def _is_obj(x) -> bool:
     return isinstance(x, np.ndarray) and x.dtype == object
 
 
+#: operation counts by domain while ``counting()`` is active, else None
+COUNTS = None
+
+
+class counting:
+    """Context manager: count DOF operations into a fresh ``COUNTS`` dict."""
+
+    def __enter__(self):
+        global COUNTS
+        COUNTS = {}
+        return COUNTS
+
+    def __exit__(self, *exc):
+        global COUNTS
+        COUNTS = None
+
+
+def _count(dom, out):
+    if COUNTS is not None:
+        key = dom or ("vol" if out.ndim == 2 else "all")
+        COUNTS[key] = COUNTS.get(key, 0) + out.size
+
+
 class DOF:
     """A DOFArray stand-in: one NumPy array (volume (Nel, Np) or faces
-    (Nel, 4, Nfp)).  Object arrays broadcast over it element by element."""
+    (Nel, 4, Nfp)).  Object arrays broadcast over it element by element.
+    ``dom``: the face domain the array lives on (None: volume or neutral)."""
 
     __array_ufunc__ = None   # NumPy defers to the reflected operators below
 
-    def __init__(self, a, actx=None):
+    def __init__(self, a, actx=None, dom=None):
         self.a = np.asarray(a, dtype=np.float64)
         self.array_context = actx
+        self.dom = dom
 
     def _bin(self, other, op, swap=False):
         if _is_obj(other) or (isinstance(other, np.ndarray) and other.ndim >= 1):
             return objarr([self._bin(o, op, swap) for o in other])
         o = other.a if isinstance(other, DOF) else other
-        return DOF(op(o, self.a) if swap else op(self.a, o), self.array_context)
+        odom = other.dom if isinstance(other, DOF) else None
+        dom = self.dom or odom
+        if self.dom and odom and self.dom != odom:
+            dom = "all"
+        out = op(o, self.a) if swap else op(self.a, o)
+        _count(dom, out)
+        return DOF(out, self.array_context, dom)
 
     def __add__(self, o): return self._bin(o, operator.add)
     def __radd__(self, o): return self._bin(o, operator.add, True)
@@ -61,7 +102,9 @@ class DOF:
     def __truediv__(self, o): return self._bin(o, operator.truediv)
     def __rtruediv__(self, o): return self._bin(o, operator.truediv, True)
     def __pow__(self, o): return self._bin(o, operator.pow)
-    def __neg__(self): return DOF(-self.a, self.array_context)
+    def __neg__(self):
+        _count(self.dom, self.a)
+        return DOF(-self.a, self.array_context, self.dom)
 
 
 def cmap(f, x):
@@ -79,9 +122,14 @@ def cmap(f, x):
 class _NP:
     """``actx.np``."""
     @staticmethod
-    def exp(x): return cmap(lambda d: DOF(np.exp(d.a), d.array_context), x)
+    def exp(x): return cmap(lambda d: DOF(np.exp(d.a), d.array_context, d.dom), x)
+
     @staticmethod
-    def sqrt(x): return cmap(lambda d: DOF(np.sqrt(d.a), d.array_context), x)
+    def sqrt(x):
+        def f(d):
+            _count(d.dom, d.a)
+            return DOF(np.sqrt(d.a), d.array_context, d.dom)
+        return cmap(f, x)
     @staticmethod
     def real(x): return x
 
@@ -167,10 +215,11 @@ def _build_op():
         if src.domain_tag == "vol" and tgt.domain_tag == "vol":
             return x
         if src.domain_tag == "vol":          # volume -> boundary faces: traces
-            return cmap(lambda z: DOF(_trace(d, z.a, d.int_idx), z.array_context), x)
+            return cmap(lambda z: DOF(_trace(d, z.a, d.int_idx), z.array_context,
+                                      "bdry"), x)
         if tgt.domain_tag == "all_faces":    # a face domain into all faces
             keep = d.bdry if src.domain_tag is BTAG_ALL else ~d.bdry
-            return cmap(lambda z: DOF(z.a * keep[..., None], z.array_context), x)
+            return cmap(lambda z: DOF(z.a * keep[..., None], z.array_context, "all"), x)
         if tgt.domain_tag == src.domain_tag:  # same faces, another quadrature tag
             return x
         raise NotImplementedError((src.domain_tag, tgt.domain_tag))
@@ -181,8 +230,8 @@ def _build_op():
     def interior_trace_pairs(dcoll, w, comm_tag=None):
         d = dcoll._d
         return [TracePair(DOFDesc(INT_FACES),
-                          interior=cmap(lambda z: DOF(_trace(d, z.a, d.int_idx)), w),
-                          exterior=cmap(lambda z: DOF(_trace(d, z.a, d.ext_idx)), w))]
+                          interior=cmap(lambda z: DOF(_trace(d, z.a, d.int_idx), dom="int"), w),
+                          exterior=cmap(lambda z: DOF(_trace(d, z.a, d.ext_idx), dom="int"), w))]
 
     def inverse_mass(dcoll, x):
         return cmap(lambda z: DOF(orc.inverse_mass(dcoll._d, z.a)), x)

@@ -68,3 +68,20 @@ def test_cost_object():
     assert c.dofs == 4 * 1000 * 20
     assert c.bytes == 1000 * (16 * 4 * 20 + 72 + 128 + 16 * 10)
     assert c.roofline_seconds(1e12, 1e12) == max(c.flops, c.bytes) / 1e12
+
+
+def test_wave_pointwise_counts_follow_the_reference_code():
+    """The wave equation's pointwise counts are those of the reference's own
+    wave_operator, counted on stand-ins (tests/golden/make_reference_flop_counts.py)."""
+    import json
+    from pathlib import Path
+    fx = json.loads((Path(__file__).parent / "golden" / "reference_wave_flops.json").read_text())
+    face, vol = pm._POINTWISE["wave"]
+    for order, c in fx["orders"].items():
+        assert c["per_node"] == vol
+        assert c["per_interior_face_point"] + c["per_all_faces_point"] == face
+        assert c["per_boundary_face_point"] - c["per_interior_face_point"] \
+            == pm.WAVE_BOUNDARY_EXTRA
+    n, order = 3, 2
+    c = pm.RhsCost("wave", order, 6 * n**3, boundary_faces=12 * n * n)
+    assert c.flops == 6 * n**3 * pm.flops_per_element("wave", order) + 12 * n * n * pm.nfp_of(order)
