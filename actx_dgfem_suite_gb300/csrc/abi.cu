@@ -188,6 +188,7 @@ struct dg_plan {
   int32_t precision = 0;
   int32_t order = 0;
   int dim = 3;             // 2: triangle mesh (dg_plan_create_2d)
+  int grid_stage = 0;      // 2D: persistent grid of the RK-stage kernel (grid: RHS)
   int32_t np = 0, nfp = 0, nfields = 0;
   int64_t nel = 0;
   const double* metric = nullptr;
@@ -1009,12 +1010,14 @@ int dg_plan_create_2d(dg_plan** plan_out, int32_t equation,
       return fail(DG_ERR_ARGUMENT, "metric, face_geom and gather must be device memory");
     }
   }
+  // each mode's persistent grid from its own occupancy (the RK-stage kernel
+  // may hold more registers than the RHS kernel)
   dg::LaunchShape shape, other;
   cudaError_t err = dg::shape_2d(equation, N, dg::MODE_RHS, &shape);
   if (err == cudaSuccess) err = dg::shape_2d(equation, N, dg::MODE_STAGE, &other);
   if (err != cudaSuccess) return cuda_fail(err, "2D kernel configuration");
-  if (other.blocks_per_sm < shape.blocks_per_sm) shape.blocks_per_sm = other.blocks_per_sm;
-  if (shape.blocks_per_sm < 1) return fail(DG_ERR_UNSUPPORTED, "kernel does not fit on an SM");
+  if (shape.blocks_per_sm < 1 || other.blocks_per_sm < 1)
+    return fail(DG_ERR_UNSUPPORTED, "kernel does not fit on an SM");
   const int ops_bytes = dg::pack_ops_2d(N, diff, mesh->lift, mesh->face_nodes, nullptr, 0);
   if (ops_bytes != shape.ops_bytes)
     return fail(DG_ERR_CUDA, "operator layout mismatch between host and kernel");
@@ -1060,7 +1063,9 @@ int dg_plan_create_2d(dg_plan** plan_out, int32_t equation,
   p->nsm = nsm;
   p->ntiles = (p->nel + shape.elems_per_tile - 1) / shape.elems_per_tile;
   const int64_t full = (int64_t)nsm * shape.blocks_per_sm;
+  const int64_t full_stage = (int64_t)nsm * other.blocks_per_sm;
   p->grid = (int)(p->ntiles < full ? p->ntiles : full);
+  p->grid_stage = (int)(p->ntiles < full_stage ? p->ntiles : full_stage);
   *plan_out = p;
   return DG_OK;
 }
@@ -1465,7 +1470,7 @@ int dg_rk_stage(dg_plan* p, const double* q_in, double* q_out, double* res,
   }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   if (p->dim == 2) {
-    cudaError_t err = dg::launch_2d(p->equation, p->order, dg::MODE_STAGE, a, p->grid, s);
+    cudaError_t err = dg::launch_2d(p->equation, p->order, dg::MODE_STAGE, a, p->grid_stage, s);
     if (err != cudaSuccess) return cuda_fail(err, "rk stage launch");
     return DG_OK;
   }

@@ -44,15 +44,15 @@ template <int EQ>
 struct Eq2;
 template <>
 struct Eq2<DG_WAVE> {
-  static constexpr int NF = 3, NAUX = 2;
+  static constexpr int NF = 3, NAUX = 2, NNODE = 0;
 };
 template <>
 struct Eq2<DG_EULER> {
-  static constexpr int NF = 4, NAUX = 8;
+  static constexpr int NF = 4, NAUX = 8, NNODE = 3;  // per node: p, 1/rho, |u| + c
 };
 template <>
 struct Eq2<DG_MAXWELL> {
-  static constexpr int NF = 3, NAUX = 0;
+  static constexpr int NF = 3, NAUX = 0, NNODE = 0;
 };
 
 // Operator block in bytes (global and shared): Wt[r][j][i] (2 Np Np
@@ -76,7 +76,10 @@ struct Tile2 {
   static constexpr int FLUX = AUX + pad16(NAUX * E * NP * 8);
   static constexpr int GEO = FLUX + pad16(NF * E * NFPT * 8);
   static constexpr int FGEO = GEO + pad16(4 * E * 8);
-  static constexpr int SMEM_BYTES = FGEO + pad16(12 * E * 8);
+  // Euler: pressure, 1/rho and wave speed of every node of the tile, for the
+  // interior side of its edge points
+  static constexpr int NODE = FGEO + pad16(12 * E * 8);
+  static constexpr int SMEM_BYTES = NODE + pad16(Eq2<EQ>::NNODE * E * NP * 8);
 };
 
 template <int N, int EQ, int MODE>
@@ -97,6 +100,7 @@ __global__ void __launch_bounds__(kBlock) dg_rhs2d_kernel(const RhsArgs a) {
   double* sFlux = reinterpret_cast<double*>(smem + T::FLUX);
   double* sG = reinterpret_cast<double*>(smem + T::GEO);
   double* sFG = reinterpret_cast<double*>(smem + T::FGEO);
+  [[maybe_unused]] double* sNode = reinterpret_cast<double*>(smem + T::NODE);
 
   const int t = threadIdx.x;
   if (t == 0) {
@@ -157,6 +161,9 @@ __global__ void __launch_bounds__(kBlock) dg_rhs2d_kernel(const RhsArgs a) {
         const double p = (p0 - 1.0) * (en - 0.5 * (m[0] * m[0] + m[1] * m[1]) * rinv);
         const double u[2] = {m[0] * rinv, m[1] * rinv};
         const double ep = en + p;
+        sNode[(0 * E + el) * NP + i] = p;
+        sNode[(1 * E + el) * NP + i] = rinv;
+        sNode[(2 * E + el) * NP + i] = sqrt(u[0] * u[0] + u[1] * u[1]) + sqrt(p0 * (p * rinv));
         // A_k^r = sum_x G[r][x] F_k,x with F_0 = m, F_1 = u (E + p),
         // F_{2+c} = m_c u + p e_c, through U_r = (G u)_r
 #pragma unroll
@@ -276,19 +283,30 @@ __global__ void __launch_bounds__(kBlock) dg_rhs2d_kernel(const RhsArgs a) {
           qe[3] = qi[3] - 2.0 * ny * mn;
         }
         double fn_i[4], fn_e[4], lam_i, lam_e;
-        auto side = [&](const double* q, double* fn, double& lam) {
-          const double rinv = 1.0 / q[0];
-          const double p = (p0 - 1.0) * (q[1] - 0.5 * (q[2] * q[2] + q[3] * q[3]) * rinv);
-          const double ux = q[2] * rinv, uy = q[3] * rinv;
-          const double un = ux * nx + uy * ny;
+        // normal fluxes of one side from its pressure and 1/rho
+        auto side = [&](const double* q, double p, double rinv, double* fn) {
+          const double un = (q[2] * nx + q[3] * ny) * rinv;
           fn[0] = q[2] * nx + q[3] * ny;
           fn[1] = un * (q[1] + p);
           fn[2] = q[2] * un + p * nx;
           fn[3] = q[3] * un + p * ny;
-          lam = sqrt(ux * ux + uy * uy) + sqrt(p0 * (p * rinv));
         };
-        side(qi, fn_i, lam_i);
-        side(qe, fn_e, lam_e);
+        // interior: the node's values from the pre-pass; the wall mirror
+        // keeps rho, |m| and E, so the boundary exterior shares them too
+        const double pi = sNode[(0 * E + elp) * NP + node];
+        const double ri = sNode[(1 * E + elp) * NP + node];
+        lam_i = sNode[(2 * E + elp) * NP + node];
+        side(qi, pi, ri, fn_i);
+        if (bdry) {
+          side(qe, pi, ri, fn_e);
+          lam_e = lam_i;
+        } else {
+          const double re = 1.0 / qe[0];
+          const double pe = (p0 - 1.0) * (qe[1] - 0.5 * (qe[2] * qe[2] + qe[3] * qe[3]) * re);
+          const double ux = qe[2] * re, uy = qe[3] * re;
+          side(qe, pe, re, fn_e);
+          lam_e = sqrt(ux * ux + uy * uy) + sqrt(p0 * (pe * re));
+        }
         const double lam = fmax(lam_i, lam_e);
         const double nn = nx * nx + ny * ny;
 #pragma unroll
