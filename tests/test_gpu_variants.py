@@ -216,3 +216,25 @@ def test_tcgen05_nan_stays_local(variant):
     assert finite[others].all()
     n = float(torch.linalg.norm(ref[:, others]))
     assert float(torch.linalg.norm(out[:, others] - ref[:, others])) <= RTOL[variant] * n
+
+
+def test_bounded_autotune_at_mid_size_wave_p3():
+    """Wave P3 on the benchmark definition at n = 24 (82,944 tets, where the
+    3xTF32 mma.sync variants exceed 1e-5 on the largest meshes): the
+    variant the bounded autotuner keeps is within 1e-5 of the FP64 RHS."""
+    from actx_dgfem_suite_gb300.array_context import GB300DGArrayContext
+    from actx_dgfem_suite_gb300.rhs_builder import get_rhs
+    actx = GB300DGArrayContext("cuda:0")
+    rhs, args = get_rhs("wave", actx, 3, 3, definition="baseline", nel_1d=24,
+                        device_setup=True)
+    op = rhs.dg_operator
+    q = actx.compile(rhs).stage(args[-1])
+    r64 = op.plan_for(actx).rhs(q)
+    op.precision = "fp32-mixed"
+    mixed = op.plan_for(actx)
+    res = mixed.autotune(q, reps=2, ref=r64, max_rel_l2=MIXED_RTOL)
+    chosen_err = res["rel_l2"][mixed.VARIANTS[res["chosen"]]]
+    assert chosen_err is not None and chosen_err <= MIXED_RTOL
+    out = mixed.rhs(q)
+    mixed.finish()
+    assert float(torch.linalg.norm(out - r64) / torch.linalg.norm(r64)) <= MIXED_RTOL
