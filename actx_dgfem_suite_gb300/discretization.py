@@ -244,6 +244,8 @@ def union_discretization(discs: list[DGDiscretization]) -> tuple[DGDiscretizatio
     two members.  Returns the union and the element offsets (len + 1)."""
     if not discs:
         raise ValueError("need at least one member")
+    if any(getattr(d, "dim", 3) != 3 for d in discs):
+        raise NotImplementedError("ensembles are built from tetrahedral meshes")
     order = discs[0].order
     if any(d.order != order for d in discs):
         raise ValueError("all members must have the same order")

@@ -164,3 +164,10 @@ def test_builders_2d_problem_setup(eq, nf):
     else:
         assert np.allclose(p.fields[0], np.sin(2 * np.pi * x) * np.sin(3 * np.pi * y))
         assert not p.fields[1:].any()
+
+
+def test_ensembles_refuse_triangle_meshes():
+    from actx_dgfem_suite_gb300.discretization import union_discretization
+    d = make_box_discretization_2d(2, 3)
+    with pytest.raises(NotImplementedError):
+        union_discretization([d, d])
