@@ -515,6 +515,7 @@ def our_arm(args) -> None:
     import torch
     import torch.distributed as dist
 
+    from actx_dgfem_suite_gb300 import hostmem
     from actx_dgfem_suite_gb300 import perf_model as pm
     from actx_dgfem_suite_gb300.array_context import GB300DGArrayContext
     from actx_dgfem_suite_gb300.containers import leaves
@@ -760,6 +761,9 @@ def our_arm(args) -> None:
                                  for k, v in split.items()},
                     "logged_steps": [{k: (round(v, 1) if v is not None else None)
                                       for k, v in r.items()} for r in logged],
+                    # page-locked host buffers: on huge pages, or from
+                    # cudaHostAlloc where the host granted no huge pages
+                    "host_state_buffers": dict(hostmem.stats),
                     "overlap": ("all cases' calls issued before their results are read "
                                 "(highest kernel time per input byte first), then every "
                                 "result's copy back in the same order (to_numpy_batch, "
