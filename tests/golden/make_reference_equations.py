@@ -15,6 +15,10 @@ here), and records in ``reference_equations.npz``:
 ``tests/test_reference_equations.py`` checks the package's initial states,
 the oracle's restated wave operator and (on a GPU) the product against them.
 
+``--dim 2`` writes ``reference_equations_2d.npz`` instead: the same records
+on triangle meshes (the reference's ``wave.py`` is dimension-generic: the
+bump's centre is its first ``dim`` entries, v has ``dim`` components).
+
 Usage, from the repository root, with the reference checked out at ``$REF``
 (default ``/root/reference``)::
 
@@ -86,5 +90,42 @@ def main() -> None:
     np.savez_compressed(HERE / "reference_equations.npz", **out)
 
 
+def main_2d() -> None:
+    from tests.golden import reference_stubs as rs
+    rs.install()
+    sys.path.insert(0, os.environ.get("REF", "/root/reference"))
+    from actx_dgfem_suite.equations import wave as ref_wave
+
+    from actx_dgfem_suite_gb300.mesh import generate_box_tri_mesh
+    from oracle.geometry import build_oracle_disc_2d
+    from tests._helpers import jittered_square_mesh
+
+    out = {}
+    actx = rs.StubActx()
+    mesh = generate_box_tri_mesh(-0.5, 0.5, 4)      # reference definition's square
+    d = build_oracle_disc_2d(mesh.vertices, mesh.elements, IC_ORDER)
+    dcoll = rs.StubDcoll(d, actx)
+    out["ic_vertices"] = mesh.vertices
+    out["ic_elements"] = mesh.elements
+    out["ic_nodes"] = d.nodes
+    out["ic_wave_u"] = ref_wave.bump(actx, dcoll).a
+
+    mesh = jittered_square_mesh(3)
+    out["wave_vertices"] = mesh.vertices
+    out["wave_elements"] = mesh.elements
+    rng = np.random.default_rng(0)
+    for order in (1, 2, 3, 4):
+        d = build_oracle_disc_2d(mesh.vertices, mesh.elements, order)
+        dcoll = rs.StubDcoll(d, actx)
+        shape = d.nodes.shape[1:]
+        u = rng.standard_normal(shape)
+        v = rng.standard_normal((2,) + shape)
+        w = ref_wave.WaveState(u=rs.DOF(u), v=rs.objarr([rs.DOF(v[x]) for x in range(2)]))
+        r = ref_wave.wave_operator(actx, dcoll, c=1, w=w, quad_tag=None)
+        out[f"wave_P{order}_state"] = np.concatenate([u[None], v])
+        out[f"wave_P{order}_rhs"] = np.stack([r.u.a] + [r.v[x].a for x in range(2)])
+    np.savez_compressed(HERE / "reference_equations_2d.npz", **out)
+
+
 if __name__ == "__main__":
-    main()
+    main_2d() if "--dim" in sys.argv and sys.argv[-1] == "2" else main()

@@ -193,10 +193,10 @@ class StubDcoll:
     def __init__(self, d, actx):
         self._d = d
         self._actx = actx
-        self.dim = 3
+        self.dim = d.nodes.shape[0]          # 3 (tetrahedra) or 2 (triangles)
 
     def nodes(self):
-        return objarr([DOF(self._d.nodes[x], self._actx) for x in range(3)])
+        return objarr([DOF(self._d.nodes[x], self._actx) for x in range(self.dim)])
 
     def zeros(self, actx):
         return DOF(np.zeros(self._d.nodes.shape[1:]), actx)
@@ -241,7 +241,7 @@ def _build_op():
 
     def weak_local_grad(dcoll, dd, u):
         g = orc.weak_grad(dcoll._d, u.a)
-        return objarr([DOF(g[x]) for x in range(3)])
+        return objarr([DOF(g[x]) for x in range(dcoll.dim)])
 
     def face_mass(dcoll, dd, x):
         return cmap(lambda z: DOF(orc.face_mass(dcoll._d, z.a)), x)
@@ -307,7 +307,7 @@ def install() -> None:
     geometry = mod("grudge.geometry")
     geometry.normal = lambda actx, dcoll, dd: objarr(
         [DOF(np.broadcast_to(dcoll._d.normal[..., x][..., None],
-                             dcoll._d.int_idx.shape).copy()) for x in range(3)])
+                             dcoll._d.int_idx.shape).copy()) for x in range(dcoll.dim)])
     grudge.geometry = geometry
     op = _build_op()
     sys.modules["grudge.op"] = op

@@ -68,3 +68,53 @@ def test_product_wave_operator_matches_the_reference_code(order, precision):
     plan.finish()
     ref = GOLDEN[f"wave_P{order}_rhs"]
     assert np.linalg.norm(got - ref) <= FP64_RTOL * np.linalg.norm(ref)
+
+
+# {{{ triangle meshes (tests/golden/reference_equations_2d.npz, from the
+# same run of the reference's wave.py with dim = 2)
+
+GOLDEN_2D = np.load(Path(__file__).resolve().parent / "golden" / "reference_equations_2d.npz")
+
+
+def test_2d_initial_state_matches_the_reference_code():
+    from actx_dgfem_suite_gb300.discretization2d import make_discretization_2d
+    from actx_dgfem_suite_gb300.equations import wave
+    from actx_dgfem_suite_gb300.mesh import TriMesh
+    nodes = GOLDEN_2D["ic_nodes"]
+    np.testing.assert_allclose(wave.bump(nodes), GOLDEN_2D["ic_wave_u"], rtol=1e-15,
+                               atol=1e-300)
+    disc = make_discretization_2d(TriMesh(GOLDEN_2D["ic_vertices"],
+                                          GOLDEN_2D["ic_elements"]), 3)
+    assert np.abs(disc.nodes() - nodes).max() <= 1e-14
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_oracle_2d_wave_operator_matches_the_reference_code(order):
+    from oracle.geometry import build_oracle_disc_2d
+    from oracle.rhs import wave_rhs
+    d = build_oracle_disc_2d(GOLDEN_2D["wave_vertices"], GOLDEN_2D["wave_elements"], order)
+    st = GOLDEN_2D[f"wave_P{order}_state"]
+    ru, rv = wave_rhs(d, st[0], st[1:])
+    got = np.concatenate([ru[None], rv])
+    ref = GOLDEN_2D[f"wave_P{order}_rhs"]
+    assert np.linalg.norm(got - ref) <= 1e-14 * np.linalg.norm(ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_product_2d_wave_operator_matches_the_reference_code(order):
+    import torch
+
+    from actx_dgfem_suite_gb300.mesh import TriMesh
+    from actx_dgfem_suite_gb300.plan import DeviceMesh, DevicePlan
+    from tests._helpers import make_problem_2d
+    st = GOLDEN_2D[f"wave_P{order}_state"]
+    prob = make_problem_2d("wave", TriMesh(GOLDEN_2D["wave_vertices"],
+                                           GOLDEN_2D["wave_elements"]), order, fields=st)
+    plan = DevicePlan(DeviceMesh(prob.disc, "cuda:0"), "wave", (1.0,), "fp64")
+    got = plan.rhs(torch.from_numpy(st).cuda()).cpu().numpy()
+    plan.finish()
+    ref = GOLDEN_2D[f"wave_P{order}_rhs"]
+    assert np.linalg.norm(got - ref) <= FP64_RTOL * np.linalg.norm(ref)
+
+# }}}
