@@ -84,12 +84,13 @@ _POINTWISE = {
 #: the wave boundary pair's extra operation per boundary face point (the
 #: mirrored exterior state -u)
 WAVE_BOUNDARY_EXTRA = 1
-#: the same on triangles: wave and Maxwell TM counted from the 2D flux
-#: expressions (wave: averages, jumps, v.n, u n and the upwind term with two
-#: components; Maxwell: the TM components of the alpha flux and the PEC
-#: mirror); Euler scaled from 3D by its flux components (8 of 15)
+#: the same on triangles: wave counted from the reference's wave_operator
+#: with dim = 2 (27 flux + 6 all-faces sum per face point, 6 per node);
+#: Maxwell TM counted from the 2D flux expressions (the TM components of the
+#: alpha flux and the PEC mirror); Euler scaled from 3D by its flux
+#: components (8 of 15)
 _POINTWISE_2D = {
-    "wave": (27, 6),
+    "wave": (33, 6),
     "euler": (134, 26),
     "maxwell": (28, 10),
 }
@@ -163,8 +164,8 @@ class RhsCost:
     @property
     def flops(self) -> int:
         extra = 0
-        if self.equation == "wave" and self.dim == 3:
-            extra = WAVE_BOUNDARY_EXTRA * self.boundary_faces * nfp_of(self.order)
+        if self.equation == "wave":
+            extra = WAVE_BOUNDARY_EXTRA * self.boundary_faces * nfp_of(self.order, self.dim)
         return self.nelements * flops_per_element(self.equation, self.order, self.dim) + extra
 
     @property

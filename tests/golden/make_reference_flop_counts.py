@@ -44,30 +44,33 @@ def main() -> None:
     sys.path.insert(0, os.environ.get("REF", "/root/reference"))
     from actx_dgfem_suite.equations import wave as ref_wave
 
-    from actx_dgfem_suite_gb300.mesh import generate_box_tet_mesh
-    from oracle.geometry import build_oracle_disc
+    from actx_dgfem_suite_gb300.mesh import generate_box_tet_mesh, generate_box_tri_mesh
+    from oracle.geometry import build_oracle_disc, build_oracle_disc_2d
 
     actx = rs.StubActx()
-    mesh = generate_box_tet_mesh(0.0, 1.0, 2)
-    out = {"mesh": "box, 2 hexahedra per axis (48 tetrahedra)", "orders": {}}
-    for order in (1, 2, 3, 4):
-        d = build_oracle_disc(mesh.vertices, mesh.elements, order)
-        dcoll = rs.StubDcoll(d, actx)
-        rng = np.random.default_rng(order)
-        shape = d.nodes.shape[1:]
-        w = ref_wave.WaveState(u=rs.DOF(rng.standard_normal(shape)),
-                               v=rs.objarr([rs.DOF(rng.standard_normal(shape))
-                                            for _ in range(3)]))
-        with rs.counting() as counts:
-            ref_wave.wave_operator(actx, dcoll, c=1, w=w, quad_tag=None)
-        nvol = d.nel * d.nodes.shape[2]
-        nface = d.int_idx.size          # the stand-ins keep every face array full size
-        out["orders"][str(order)] = {
-            "per_node": counts.get("vol", 0) / nvol,
-            "per_boundary_face_point": counts.get("bdry", 0) / nface,
-            "per_interior_face_point": counts.get("int", 0) / nface,
-            "per_all_faces_point": counts.get("all", 0) / nface,
-        }
+    out = {"mesh": "box, 2 hexahedra per axis (48 tetrahedra)", "orders": {},
+           "mesh_2d": "square, 2 squares per axis (8 triangles)", "orders_2d": {}}
+    for dim, build, mesh, key in (
+            (3, build_oracle_disc, generate_box_tet_mesh(0.0, 1.0, 2), "orders"),
+            (2, build_oracle_disc_2d, generate_box_tri_mesh(0.0, 1.0, 2), "orders_2d")):
+        for order in (1, 2, 3, 4):
+            d = build(mesh.vertices, mesh.elements, order)
+            dcoll = rs.StubDcoll(d, actx)
+            rng = np.random.default_rng(order)
+            shape = d.nodes.shape[1:]
+            w = ref_wave.WaveState(u=rs.DOF(rng.standard_normal(shape)),
+                                   v=rs.objarr([rs.DOF(rng.standard_normal(shape))
+                                                for _ in range(dim)]))
+            with rs.counting() as counts:
+                ref_wave.wave_operator(actx, dcoll, c=1, w=w, quad_tag=None)
+            nvol = d.nel * d.nodes.shape[2]
+            nface = d.int_idx.size      # the stand-ins keep every face array full size
+            out[key][str(order)] = {
+                "per_node": counts.get("vol", 0) / nvol,
+                "per_boundary_face_point": counts.get("bdry", 0) / nface,
+                "per_interior_face_point": counts.get("int", 0) / nface,
+                "per_all_faces_point": counts.get("all", 0) / nface,
+            }
     (HERE / "reference_wave_flops.json").write_text(json.dumps(out, indent=1) + "\n")
     print(json.dumps(out, indent=1))
 

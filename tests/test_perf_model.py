@@ -76,12 +76,13 @@ def test_wave_pointwise_counts_follow_the_reference_code():
     import json
     from pathlib import Path
     fx = json.loads((Path(__file__).parent / "golden" / "reference_wave_flops.json").read_text())
-    face, vol = pm._POINTWISE["wave"]
-    for order, c in fx["orders"].items():
-        assert c["per_node"] == vol
-        assert c["per_interior_face_point"] + c["per_all_faces_point"] == face
-        assert c["per_boundary_face_point"] - c["per_interior_face_point"] \
-            == pm.WAVE_BOUNDARY_EXTRA
+    for key, table in (("orders", pm._POINTWISE), ("orders_2d", pm._POINTWISE_2D)):
+        face, vol = table["wave"]
+        for order, c in fx[key].items():
+            assert c["per_node"] == vol
+            assert c["per_interior_face_point"] + c["per_all_faces_point"] == face
+            assert c["per_boundary_face_point"] - c["per_interior_face_point"] \
+                == pm.WAVE_BOUNDARY_EXTRA
     n, order = 3, 2
     c = pm.RhsCost("wave", order, 6 * n**3, boundary_faces=12 * n * n)
     assert c.flops == 6 * n**3 * pm.flops_per_element("wave", order) + 12 * n * n * pm.nfp_of(order)
