@@ -94,6 +94,7 @@ def main_2d() -> None:
     from tests.golden import reference_stubs as rs
     rs.install()
     sys.path.insert(0, os.environ.get("REF", "/root/reference"))
+    from actx_dgfem_suite.equations import euler as ref_euler
     from actx_dgfem_suite.equations import wave as ref_wave
 
     from actx_dgfem_suite_gb300.mesh import generate_box_tri_mesh
@@ -109,6 +110,9 @@ def main_2d() -> None:
     out["ic_elements"] = mesh.elements
     out["ic_nodes"] = d.nodes
     out["ic_wave_u"] = ref_wave.bump(actx, dcoll).a
+    q = ref_euler.acoustic_pulse_condition(dcoll.nodes())
+    out["ic_euler"] = np.stack([q.mass.a, q.energy.a]
+                               + [np.broadcast_to(m.a, q.mass.a.shape) for m in q.momentum])
 
     mesh = jittered_square_mesh(3)
     out["wave_vertices"] = mesh.vertices

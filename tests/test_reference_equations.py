@@ -80,9 +80,12 @@ def test_2d_initial_state_matches_the_reference_code():
     from actx_dgfem_suite_gb300.discretization2d import make_discretization_2d
     from actx_dgfem_suite_gb300.equations import wave
     from actx_dgfem_suite_gb300.mesh import TriMesh
+    from actx_dgfem_suite_gb300.equations import euler
     nodes = GOLDEN_2D["ic_nodes"]
     np.testing.assert_allclose(wave.bump(nodes), GOLDEN_2D["ic_wave_u"], rtol=1e-15,
                                atol=1e-300)
+    np.testing.assert_allclose(euler.acoustic_pulse_condition(nodes), GOLDEN_2D["ic_euler"],
+                               rtol=1e-15, atol=1e-300)
     disc = make_discretization_2d(TriMesh(GOLDEN_2D["ic_vertices"],
                                           GOLDEN_2D["ic_elements"]), 3)
     assert np.abs(disc.nodes() - nodes).max() <= 1e-14
