@@ -89,7 +89,7 @@ def test_argument_errors_without_device():
         == _lib.DG_ERR_ARGUMENT
     assert L.dg_plan_create_2d(ctypes.byref(h), 0, ctypes.byref(d2), None, 0) \
         == _lib.DG_ERR_ARGUMENT           # NULL device arrays
-    d2.nelements = (1 << 31) // 6         # Nel * Np >= 2^31 at P2 (Np = 6)
+    d2.nelements = (1 << 31) // 6 + 1     # Nel * Np >= 2^31 at P2 (Np = 6)
     assert L.dg_plan_create_2d(ctypes.byref(h), 0, ctypes.byref(d2), None, 0) \
         == _lib.DG_ERR_ARGUMENT
     assert b"2^31" in L.dg_last_error()
