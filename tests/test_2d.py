@@ -171,3 +171,23 @@ def test_ensembles_refuse_triangle_meshes():
     d = make_box_discretization_2d(2, 3)
     with pytest.raises(NotImplementedError):
         union_discretization([d, d])
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_oracle_2d_maxwell_tm_curls_are_exact(order):
+    """Continuous polynomial TM fields of degree <= N: away from the boundary
+    (no jumps, so no flux) the RHS is E_z' = dH_y/dx - dH_x/dy,
+    H_x' = -dE_z/dy, H_y' = dE_z/dx (epsilon = mu = 1)."""
+    from oracle.rhs import maxwell_rhs
+    d = _od(order)
+    x, y = d.nodes
+    ez = x ** order + 2 * y
+    hx = y ** order - x
+    hy = x * y ** (order - 1) + 3 * x
+    r = maxwell_rhs(d, np.stack([ez, hx, hy]), 0.5)
+    inner = ~d.bdry.any(axis=1)
+    dhy_dx = y ** (order - 1) + 3
+    dhx_dy = order * y ** (order - 1)
+    assert np.abs(r[0] - (dhy_dx - dhx_dy))[inner].max() < 1e-10
+    assert np.abs(r[1] - (-2.0))[inner].max() < 1e-10
+    assert np.abs(r[2] - order * x ** (order - 1))[inner].max() < 1e-10
