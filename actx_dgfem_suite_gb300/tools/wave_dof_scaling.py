@@ -39,10 +39,12 @@ def sweep(degrees, ndofs_list, precision: str = "fp64", dim: int = 3,
         for ndofs in ndofs_list:
             nel_1d = get_nel_1d_for_regular_rect_mesh(dim, degree, int(ndofs))
             if device_setup:
+                if dim != 3:
+                    raise NotImplementedError("device-side setup builds 3D meshes only")
                 from actx_dgfem_suite_gb300.device_setup import device_problem
                 prob = device_problem("wave", degree, nel_1d, "reference", actx.device)
             else:
-                prob = wave_problem(degree, nel_1d, "reference")
+                prob = wave_problem(degree, nel_1d, "reference", dim=dim)
             plan = DevicePlan(DeviceMesh(prob.disc, actx.device), "wave",
                               prob.params, precision)
             q = torch.as_tensor(prob.fields).to(actx.device)
@@ -90,15 +92,18 @@ def main(argv=None):
     ap.add_argument("--degrees", default="1,2,3,4")
     ap.add_argument("--ndofs", default=",".join(str(n) for n in GB300_NDOFS))
     ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32-mixed"))
+    ap.add_argument("--dim", type=int, default=3, choices=(2, 3),
+                    help="topological dimension (the reference's --dim; 2: "
+                         "triangles, FP64)")
     ap.add_argument("--json", action="store_true")
     a = ap.parse_args(argv)
     degrees = [int(x) for x in a.degrees.split(",")]
     ndofs = [int(float(x)) for x in a.ndofs.split(",")]
-    res = sweep(degrees, ndofs, a.precision)
+    res = sweep(degrees, ndofs, a.precision, dim=a.dim)
     if a.json:
         print(json.dumps({f"P{d}@{n}": v for (d, n), v in res.items()}))
         return res
-    print("GDOFS/s for 3D-wave:")
+    print(f"GDOFS/s for {a.dim}D-wave:")
     print("      " + "".join(f"{n / 1e6:>10.1f}M" for n in ndofs))
     for d in degrees:
         print(f"P{d:<5d}" + "".join(f"{res[(d, n)] * 1e-9:>11.3f}" for n in ndofs))

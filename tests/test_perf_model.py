@@ -86,3 +86,12 @@ def test_wave_pointwise_counts_follow_the_reference_code():
     n, order = 3, 2
     c = pm.RhsCost("wave", order, 6 * n**3, boundary_faces=12 * n * n)
     assert c.flops == 6 * n**3 * pm.flops_per_element("wave", order) + 12 * n * n * pm.nfp_of(order)
+
+
+def test_print_roofline_dims_2_and_3(capsys):
+    from actx_dgfem_suite_gb300.tools.print_roofline import main
+    rows = main(["--equations", "tiny_wave,euler", "--dims", "2,3", "--degrees", "1,4"])
+    assert {(r[0], r[1], r[2]) for r in rows} == {
+        (dim, eq, d) for dim in (2, 3) for eq in ("tiny_wave", "euler") for d in (1, 4)}
+    assert all(r[4] > 0 and r[5] > 0 and r[6] > 0 for r in rows)
+    assert " 2 euler" in capsys.readouterr().out
